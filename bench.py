@@ -1,0 +1,408 @@
+"""Benchmark: k-mers inserted/s into dBG<ByteStorage, CanLemireShifter> on one GB300.
+
+Workload (large count-min insert): K=31, 4 uint8 saturating tables of prime
+size just below 2^30 cells (4 GiB, HBM-resident, far beyond the 129 MB L2),
+reads of 150 bp sampled uniformly from either strand of a 50 Mbp seeded
+random genome with 0.5% substitutions; 2% of reads carry an 'N' and are
+dropped by the FASTX policy before packing.  One step inserts one batch of
+1M reads (about 117M k-mers) in batch order with exact per-read new-k-mer
+counts.  Tables persist across steps.
+
+  value     k-mers/s with the batch already in HBM (device-pointer entry point)
+  e2e       k-mers/s through the host-buffer C-ABI call, H2D of the packed
+            batch and D2H of the per-read new counts inside the timed region
+  plain     k-mers/s of the drop-in per-read insert_sequence call
+  roofline  the insert path against the measured HBM copy bandwidth, with
+            256 algorithmic bytes per k-mer (4 tables x 32 B sector, read +
+            write)
+
+``--impl reference`` times the reference algorithm on the host cores (the C
+restatement in oracle/, all threads, shared tables) on the same workload.
+Multi-GPU runs are independent replicas (the path does not shard here).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "k-mers inserted/s (K=31) plain vs batched/served on 1 GB300; p50/p99 chunk latency"
+WORKLOAD = "large count-min insert: dBG<ByteStorage,CanLemireShifter> K=31, 4 x ~2^30 uint8 cells"
+K = 31
+N_TABLES = 4
+MAX_TABLE = 1 << 30
+READ_LEN = 150
+GENOME_LEN = 50_000_000
+SUB_RATE = 0.005
+N_READ_FRAC = 0.02
+BYTES_PER_KMER = 256    # 4 tables x 32 B sector x (read + write)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+def make_batches(n_batches, reads_per_step, seed0=4):
+    """Seeded batches of packed reads (N-reads already dropped)."""
+    from goetia_gb300 import synth
+    g = synth.genome(GENOME_LEN, 3)
+    out = []
+    for b in range(n_batches):
+        rows = synth.sample_reads(g, reads_per_step, READ_LEN, SUB_RATE, seed0 + 1000 * b)
+        keep = ~synth.n_read_mask(reads_per_step, N_READ_FRAC, seed0 + 1000 * b + 1)
+        pr = synth.rows_to_packed(rows[keep])
+        pr.n_skipped = int((~keep).sum())
+        out.append(pr)
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic_per_kmer():
+    """DRAM bytes per k-mer of the insert kernels from the committed ncu
+    summary (profiles/insert_byte_k31_traffic.txt), or None."""
+    p = os.path.join(HERE, "profiles", "insert_byte_k31_traffic.txt")
+    try:
+        for ln in open(p):
+            if ln.startswith("dram_bytes_per_kmer="):
+                return float(ln.split("=", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline_port(batches, sample_reads, threads):
+    """The oracle's C restatement on the host cores: one thread by default
+    (the reference's execution model), on a bounded sample of the workload."""
+    import oracle
+    sizes = oracle.primes(N_TABLES, MAX_TABLE)
+    st = oracle.Storage("byte", sizes)
+    pr = batches[0]
+    n = min(sample_reads, pr.n_reads)
+    off = pr.offsets[:n + 1].copy()
+    # warm the table pages with a small insert first
+    warm = min(2000, n)
+    st.insert_reads_mt(True, K, pr.packed, pr.offsets[:warm + 1].copy(), threads)
+    t0 = time.perf_counter()
+    if threads == 1:
+        total, _ = st.insert_reads(True, K, pr.packed, off)
+    else:
+        total = st.insert_reads_mt(True, K, pr.packed, off, threads)
+    dt = time.perf_counter() - t0
+    return total / dt, total, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    threads = os.cpu_count() or 1
+    batches = make_batches(1 + 0, args.reads_per_step)
+    sizes = oracle.primes(N_TABLES, MAX_TABLE)
+    st = oracle.Storage("byte", sizes)
+    pr = batches[0]
+    n = min(args.reference_sample_reads, pr.n_reads)
+    off = pr.offsets[:n + 1].copy()
+    for _ in range(args.warmup):
+        st.insert_reads_mt(True, K, pr.packed, off, threads)
+    t0 = time.perf_counter()
+    total = 0
+    for _ in range(args.steps):
+        total += st.insert_reads_mt(True, K, pr.packed, off, threads)
+    dt = time.perf_counter() - t0
+    v = total / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "k-mers/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64/u8",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "reads_per_step": int(n), "read_len": READ_LEN,
+                   "table_cells": sizes},
+        "cpu_baseline": {"value": v, "unit": "k-mers/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} reads x {READ_LEN} bp per step of the same workload, "
+                                   f"C restatement of the reference insert, {threads} threads "
+                                   "on one shared storage"},
+        "e2e": {"value": v, "unit": "k-mers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    import goetia_gb300 as G
+    from goetia_gb300 import build as gbuild
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    gbuild.build()
+    dev = torch.device("cuda", local)
+
+    n_batches = args.warmup + args.steps
+    batches = make_batches(n_batches, args.reads_per_step, seed0=4 + 7919 * rank)
+
+    storage = G.ByteStorage.build(MAX_TABLE, N_TABLES)
+    Graph = G.dBG[G.ByteStorage, G.CanLemireShifter]
+    g = Graph.build(storage, K)
+    if args.window:
+        g.set_insert_schedule(args.window, args.kpt)
+    stream = torch.cuda.Stream(dev)
+    g.set_stream(stream.cuda_stream)
+
+    # device-resident inputs
+    d_batches = []
+    for pr in batches:
+        d_packed = torch.from_numpy(pr.packed.view(np.int32)).to(dev)
+        d_off = torch.from_numpy(pr.offsets.view(np.int64)).to(dev)
+        d_new = torch.empty(pr.n_reads, dtype=torch.int64, device=dev)
+        d_batches.append((d_packed, d_off, d_new, pr.n_reads, pr.n_kmers(K)))
+    torch.cuda.synchronize(dev)
+
+    def step(i):
+        d_packed, d_off, d_new, n_reads, nk = d_batches[i]
+        g.insert_device(d_packed.data_ptr(), d_packed.numel(), d_off.data_ptr(), n_reads,
+                        n_kmers=nk, n_new_ptr=d_new.data_ptr(), stream=stream.cuda_stream)
+        return nk
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+
+    launches0 = g.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kmers = 0
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for i in range(args.warmup, n_batches):
+            kmers += step(i)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = g.launch_count() - launches0
+    g.synchronize()   # raises if a device-side check fired
+    dt = e0.elapsed_time(e1) / 1000.0
+    if world > 1:
+        t = torch.tensor([dt], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t.item())
+        kt = torch.tensor([kmers], device=dev, dtype=torch.float64)
+        dist.all_reduce(kt)
+        total_kmers = float(kt.item())
+    else:
+        total_kmers = float(kmers)
+    value = total_kmers / dt
+
+    # e2e: host-buffer C-ABI call on a fresh graph, copies inside the timed region
+    g2 = Graph.build(storage, K)
+    if args.window:
+        g2.set_insert_schedule(args.window, args.kpt)
+    pinned = []
+    for pr in batches:
+        hp = torch.from_numpy(pr.packed.view(np.int32)).pin_memory().numpy().view(np.uint32)
+        ho = torch.from_numpy(pr.offsets.view(np.int64)).pin_memory().numpy().view(np.uint64)
+        hn = torch.empty(max(pr.n_reads, 1), dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+        pinned.append((G.PackedReads(hp, ho), hn))
+    import ctypes
+    from goetia_gb300 import _lib
+
+    def e2e_step(i):
+        pr, hn = pinned[i]
+        nk = _lib.c_u64()
+        _lib.call("gdbg_insert_batch", g2._h, pr.packed.ctypes.data_as(_lib.u32p), pr.packed.size,
+                  pr.offsets.ctypes.data_as(_lib.u64p), pr.n_reads, hn.ctypes.data_as(_lib.u64p),
+                  ctypes.byref(nk))
+        return int(nk.value), pr.packed.nbytes + pr.offsets.nbytes, pr.n_reads * 8
+
+    for i in range(args.warmup):
+        e2e_step(i)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e2e_kmers = h2d = d2h = 0
+    for i in range(args.warmup, n_batches):
+        a, b, c = e2e_step(i)
+        e2e_kmers += a
+        h2d += b
+        d2h += c
+    torch.cuda.synchronize(dev)
+    e2e_dt = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_dt], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_dt = float(t.item())
+    e2e_value = e2e_kmers * world / e2e_dt
+    # parity spot check of the two arms: same batches into fresh tables
+    same = bool(np.array_equal(pinned[-1][1][:batches[-1].n_reads],
+                               d_batches[-1][2].cpu().numpy().view(np.uint64)))
+
+    # plain drop-in: one insert_sequence call per read
+    from goetia_gb300.reads import codes_to_str
+    g3 = Graph.build(storage, K)
+    pr0 = batches[0]
+    n_plain = min(args.plain_reads, pr0.n_reads)
+    j = np.arange(int(pr0.offsets[n_plain]))
+    codes = ((pr0.packed[j >> 4] >> (2 * (j & 15)).astype(np.uint32)) & 3).astype(np.uint8)
+    seqs = [codes_to_str(codes[int(pr0.offsets[r]):int(pr0.offsets[r + 1])]).encode()
+            for r in range(n_plain)]
+    for s in seqs[:20]:
+        g3.insert_sequence(s)
+    t0 = time.perf_counter()
+    pk = 0
+    for s in seqs[20:]:
+        pk += g3.insert_sequence(s)
+    plain_dt = time.perf_counter() - t0
+    plain_value = pk / plain_dt
+
+    peak, peak_kind = measured_peak()
+    achieved = value / world * BYTES_PER_KMER / 1e9
+    tpk = profile_traffic_per_kmer()
+    per_launch_kmers = kmers / max(args.steps, 1)
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_kind,
+        "kernel": "insert (probe + commit passes per window)",
+        "algorithmic_bytes_per_kmer": BYTES_PER_KMER,
+        "traffic": (tpk * per_launch_kmers) if tpk else None,
+        "traffic_unit": "DRAM bytes per step (ncu, scaled by k-mers)" if tpk else None,
+    }
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            v, tot, cdt = cpu_baseline_port(batches, args.cpu_sample_reads, 1)
+            cpu = {"value": v, "unit": "k-mers/s", "cores": 1, "kind": "port",
+                   "sample": f"{min(args.cpu_sample_reads, batches[0].n_reads)} reads x "
+                             f"{READ_LEN} bp of step 0 ({tot} k-mers, {cdt:.1f} s), one thread, "
+                             "4 x ~2^30-cell Byte tables"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "k-mers/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64/u8", "data": "synthetic (seeded genome and reads)",
+            "config": {"workload": WORKLOAD, "storage": "ByteStorage",
+                       "shifter": "CanLemireShifter", "K": K, "n_tables": N_TABLES,
+                       "table_cells": storage.get_tablesizes(),
+                       "reads_per_step": int(batches[0].n_reads), "read_len": READ_LEN,
+                       "genome_bp": GENOME_LEN, "substitution_rate": SUB_RATE,
+                       "n_reads_dropped_per_step": int(batches[0].n_skipped),
+                       "insert_schedule": list(g.insert_schedule()),
+                       "l2": "inputs larger than L2: 4 GiB of tables, random cells",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "k-mers/s", "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps, "same_new_counts_as_value_arm": same},
+            "plain": {"value": plain_value, "unit": "k-mers/s",
+                      "sample": f"{n_plain - 20} reads, one insert_sequence call each"},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--reads-per-step", type=int, default=1_000_000)
+    ap.add_argument("--window", type=int, default=0)
+    ap.add_argument("--kpt", type=int, default=0)
+    ap.add_argument("--plain-reads", type=int, default=2000)
+    ap.add_argument("--cpu-sample-reads", type=int, default=300_000)
+    ap.add_argument("--reference-sample-reads", type=int, default=1_000_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

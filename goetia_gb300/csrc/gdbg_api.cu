@@ -1,0 +1,847 @@
+// C ABI of the GB300 dBG hot path (declared in include/goetia_gb300.h).
+//
+// One gdbg_graph owns: the device tables (one allocation, each table padded
+// to 256 bytes), its CUDA stream, the insert scratch (window buffers and the
+// first-touch claims map), batch scratch (k-mer prefix, tile map) and
+// staging buffers for the host-pointer entry points.  All device work of a
+// handle runs on its stream in submission order.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "gdbg_launch.h"
+#include "goetia_gb300.h"
+
+using namespace gdbg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define GDBG_CUDA(call)                                                                      \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(e_ == cudaErrorMemoryAllocation ? GDBG_ERR_OOM : GDBG_ERR_CUDA,      \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+#define GDBG_TRY(call)                       \
+    do {                                     \
+        int rc_ = (call);                    \
+        if (rc_ != GDBG_OK) return rc_;      \
+    } while (0)
+
+uint64_t host_rotl(uint64_t x, unsigned r) {
+    r &= 63u;
+    return r ? (x << r) | (x >> (64u - r)) : x;
+}
+
+constexpr uint64_t HSYM[4] = {16664410744025174816ull, 15956807086001210932ull,
+                              9404339731978646439ull, 836480985777824379ull};
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;  // elements
+    int ensure(size_t n) {
+        if (n <= cap) return GDBG_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(n + n / 4, 64);
+        cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return fail(GDBG_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+        cap = want;
+        return GDBG_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+uint32_t next_pow2(uint64_t x) {
+    uint64_t p = 1;
+    while (p < x) p <<= 1;
+    return (uint32_t)p;
+}
+
+}  // namespace
+
+struct gdbg_graph {
+    int storage = 0, shifter = 0;
+    uint16_t K = 0;
+    int device = 0;
+    std::vector<uint64_t> sizes, bytes, word_off, words;
+    uint32_t* d_tables = nullptr;
+    uint64_t total_words = 0;
+    TableParams tp{};
+    HashParams hp{};
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    unsigned long long* d_counters = nullptr;  // [0] n_unique, [1] n_occupied
+    uint32_t* d_err = nullptr;
+    // insert scratch
+    uint32_t window = 262144, kpt = 4;
+    DevBuf<uint32_t> fresh, words_seen;
+    DevBuf<uint64_t> claims;
+    uint32_t claims_mask = 0, epoch = 0;
+    // batch scratch
+    DevBuf<uint64_t> kofs, partials;
+    DevBuf<uint32_t> tile_read;
+    // staging for host-pointer calls
+    DevBuf<uint32_t> st_packed;
+    DevBuf<uint64_t> st_offsets, st_out64, st_out64b, st_out64c;
+    DevBuf<int16_t> st_counts;
+    DevBuf<uint8_t> st_u8;
+    uint64_t launches = 0;
+    bool live_hint_valid = false;
+
+    LaunchShape shape(int kpt_) const {
+        return LaunchShape{shifter == GDBG_CAN_LEMIRE, kpt_, (int)sizes.size()};
+    }
+};
+
+namespace {
+
+int set_device(const gdbg_graph* g) {
+    GDBG_CUDA(cudaSetDevice(g->device));
+    return GDBG_OK;
+}
+
+cudaStream_t pick_stream(gdbg_graph* g, void* s) {
+    return s ? (cudaStream_t)s : g->stream;
+}
+
+int make_graph(int storage, int shifter, uint16_t K, const uint64_t* sizes, uint16_t n,
+               gdbg_graph** out) {
+    if (!out) return fail(GDBG_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (storage < GDBG_BIT || storage > GDBG_NIBBLE)
+        return fail(GDBG_ERR_INVALID_ARG, "unknown storage kind");
+    if (shifter != GDBG_FWD_LEMIRE && shifter != GDBG_CAN_LEMIRE)
+        return fail(GDBG_ERR_INVALID_ARG, "unknown shifter kind");
+    if (K == 0) return fail(GDBG_ERR_INVALID_ARG, "K must be positive");
+    if (n == 0 || n > MAX_TABLES)
+        return fail(GDBG_ERR_INVALID_ARG, "n_tables must be in 1..32");
+    for (uint16_t i = 0; i < n; ++i)
+        if (sizes[i] == 0 || sizes[i] >= (1ull << 32))
+            return fail(GDBG_ERR_INVALID_ARG, "table sizes must be in 1..2^32-1 cells");
+
+    gdbg_graph* g = new gdbg_graph();
+    g->storage = storage;
+    g->shifter = shifter;
+    g->K = K;
+    cudaGetDevice(&g->device);
+    uint64_t off = 0;
+    for (uint16_t i = 0; i < n; ++i) {
+        uint64_t p = sizes[i];
+        uint64_t b = storage == GDBG_BIT ? p / 8 + 1 : storage == GDBG_NIBBLE ? p / 2 + 1 : p;
+        uint64_t w = ((b + 3) / 4 + 63) / 64 * 64;  // 256-byte padded
+        g->sizes.push_back(p);
+        g->bytes.push_back(b);
+        g->words.push_back(w);
+        g->word_off.push_back(off);
+        off += w;
+    }
+    g->total_words = off;
+    auto cleanup = [&](int rc) { gdbg_destroy(g); return rc; };
+    cudaError_t e = cudaMalloc((void**)&g->d_tables, off * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        g->d_tables = nullptr;
+        return cleanup(fail(GDBG_ERR_OOM, std::string("table allocation: ") + cudaGetErrorString(e)));
+    }
+    if (cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cleanup(fail(GDBG_ERR_CUDA, "cudaStreamCreate failed"));
+    g->stream = g->own_stream;
+    if (cudaMalloc((void**)&g->d_counters, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc((void**)&g->d_err, sizeof(uint32_t)) != cudaSuccess)
+        return cleanup(fail(GDBG_ERR_OOM, "counter allocation failed"));
+    cudaMemsetAsync(g->d_tables, 0, off * sizeof(uint32_t), g->stream);
+    cudaMemsetAsync(g->d_counters, 0, 2 * sizeof(unsigned long long), g->stream);
+    cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
+    for (uint16_t i = 0; i < n; ++i) {
+        g->tp.words[i] = g->d_tables + g->word_off[i];
+        g->tp.p[i] = sizes[i];
+        g->tp.m[i] = ~0ull / sizes[i];
+    }
+    g->tp.n = n;
+    g->hp.K = K;
+    for (int c = 0; c < 4; ++c) g->hp.tk[c] = host_rotl(HSYM[c], K % 64u);
+    e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return cleanup(fail(GDBG_ERR_CUDA, cudaGetErrorString(e)));
+    *out = g;
+    return GDBG_OK;
+}
+
+int check_device_status(gdbg_graph* g) {
+    uint32_t err = 0;
+    GDBG_CUDA(cudaMemcpyAsync(&err, g->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    if (err) {
+        cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
+        char buf[160];
+        std::snprintf(buf, sizeof buf,
+                      "device status 0x%x (1=CAS cap, 2=claims map full, 4=barrier timeout, "
+                      "8=bad read offsets)", err);
+        return fail(GDBG_ERR_DEVICE, buf);
+    }
+    return GDBG_OK;
+}
+
+// Per-read k-mer prefix + tile map for a device-resident batch.
+int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                  const uint64_t* offsets, uint64_t n_reads, uint64_t hint, cudaStream_t st,
+                  BatchView* view) {
+    GDBG_TRY(g->kofs.ensure(n_reads + 1));
+    GDBG_TRY(g->partials.ensure(n_reads / 1024 + 2));
+    int nl = 0;
+    GDBG_CUDA(launch_kmer_prefix(offsets, n_reads, g->K, packed_words * 16ull, g->partials.p,
+                                 g->kofs.p, g->d_err, st, &nl));
+    g->launches += nl;
+    uint64_t total = hint;
+    if (total == UINT64_MAX) {
+        GDBG_CUDA(cudaMemcpyAsync(&total, g->kofs.p + n_reads, sizeof(uint64_t),
+                                  cudaMemcpyDeviceToHost, st));
+        GDBG_CUDA(cudaStreamSynchronize(st));
+    }
+    uint64_t tiles = (total + MAP_TILE - 1) / MAP_TILE;
+    GDBG_TRY(g->tile_read.ensure(tiles + 1));
+    if (total) {
+        GDBG_CUDA(launch_tile_map(g->kofs.p, n_reads, tiles, g->tile_read.p, st));
+        g->launches += 1;
+    }
+    view->packed = packed;
+    view->offsets = offsets;
+    view->kofs = g->kofs.p;
+    view->tile_read = g->tile_read.p;
+    view->n_reads = n_reads;
+    view->n_kmers = total;
+    view->n_map_tiles = tiles;
+    return GDBG_OK;
+}
+
+int ensure_insert_scratch(gdbg_graph* g, cudaStream_t st) {
+    const uint64_t W = g->window, n = g->sizes.size();
+    GDBG_TRY(g->fresh.ensure(W));
+    if (g->storage != GDBG_BIT) GDBG_TRY(g->words_seen.ensure(W * n));
+    uint32_t slots = next_pow2(2 * W * n);
+    if (g->claims.cap < slots) {
+        g->claims.release();
+        GDBG_TRY(g->claims.ensure(slots));
+        GDBG_CUDA(cudaMemsetAsync(g->claims.p, 0, g->claims.cap * sizeof(uint64_t), st));
+        g->epoch = 0;
+    }
+    g->claims_mask = slots - 1;
+    return GDBG_OK;
+}
+
+int next_epoch(gdbg_graph* g, cudaStream_t st) {
+    // epochs 1..127; slot value 0 (epoch 0) means empty
+    if (g->epoch >= 127) {
+        GDBG_CUDA(cudaMemsetAsync(g->claims.p, 0, g->claims.cap * sizeof(uint64_t), st));
+        g->epoch = 0;
+    }
+    ++g->epoch;
+    return GDBG_OK;
+}
+
+int launch_pass(gdbg_graph* g, int pass, const LaunchShape& s, uint64_t n_threads, cudaStream_t st,
+                const BatchView& b, const uint64_t* hashes, const WindowParams& w) {
+    cudaError_t e;
+    switch (g->storage) {
+    case GDBG_BIT: e = launch_insert_pass<GDBG_BIT>(pass, s, n_threads, st, b, hashes, g->hp, g->tp, w); break;
+    case GDBG_BYTE: e = launch_insert_pass<GDBG_BYTE>(pass, s, n_threads, st, b, hashes, g->hp, g->tp, w); break;
+    default: e = launch_insert_pass<GDBG_NIBBLE>(pass, s, n_threads, st, b, hashes, g->hp, g->tp, w); break;
+    }
+    if (e != cudaSuccess) return fail(GDBG_ERR_CUDA, std::string("insert launch: ") + cudaGetErrorString(e));
+    g->launches += 1;
+    return GDBG_OK;
+}
+
+// Windowed probe + commit over n_total k-mers (from the batch or a hash array).
+int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64_t n_total,
+               uint64_t* n_new, cudaStream_t st) {
+    if (n_total == 0) return GDBG_OK;
+    GDBG_TRY(ensure_insert_scratch(g, st));
+    const int kpt = hashes ? 4 : (int)g->kpt;
+    LaunchShape s = g->shape(kpt);
+    for (uint64_t start = 0; start < n_total; start += g->window) {
+        uint64_t end = std::min<uint64_t>(n_total, start + g->window);
+        GDBG_TRY(next_epoch(g, st));
+        WindowParams w;
+        w.start = start;
+        w.end = end;
+        w.fresh = g->fresh.p;
+        w.words = g->words_seen.p;
+        w.claims = g->claims.p;
+        w.claims_mask = g->claims_mask;
+        w.epoch = g->epoch;
+        w.n_new = (unsigned long long*)n_new;
+        w.counters = g->d_counters;
+        w.err = g->d_err;
+        uint64_t n_threads = (end - start + kpt - 1) / kpt;
+        GDBG_TRY(launch_pass(g, 0, s, n_threads, st, b, hashes, w));
+        GDBG_TRY(launch_pass(g, 1, s, n_threads, st, b, hashes, w));
+    }
+    return GDBG_OK;
+}
+
+int run_query(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64_t n_total,
+              int16_t* counts, uint64_t* values, cudaStream_t st) {
+    if (n_total == 0) return GDBG_OK;
+    LaunchShape s = g->shape(4);
+    cudaError_t e;
+    switch (g->storage) {
+    case GDBG_BIT: e = launch_query<GDBG_BIT>(s, n_total, st, b, hashes, g->hp, g->tp, counts, values); break;
+    case GDBG_BYTE: e = launch_query<GDBG_BYTE>(s, n_total, st, b, hashes, g->hp, g->tp, counts, values); break;
+    default: e = launch_query<GDBG_NIBBLE>(s, n_total, st, b, hashes, g->hp, g->tp, counts, values); break;
+    }
+    if (e != cudaSuccess) return fail(GDBG_ERR_CUDA, std::string("query launch: ") + cudaGetErrorString(e));
+    g->launches += 1;
+    return GDBG_OK;
+}
+
+int run_masks(gdbg_graph* g, const BatchView& b, uint8_t* masks, cudaStream_t st) {
+    if (b.n_kmers == 0) return GDBG_OK;
+    LaunchShape s = g->shape(2);
+    cudaError_t e;
+    switch (g->storage) {
+    case GDBG_BIT: e = launch_masks<GDBG_BIT>(s, st, b, g->hp, g->tp, masks); break;
+    case GDBG_BYTE: e = launch_masks<GDBG_BYTE>(s, st, b, g->hp, g->tp, masks); break;
+    default: e = launch_masks<GDBG_NIBBLE>(s, st, b, g->hp, g->tp, masks); break;
+    }
+    if (e != cudaSuccess) return fail(GDBG_ERR_CUDA, std::string("mask launch: ") + cudaGetErrorString(e));
+    g->launches += 1;
+    return GDBG_OK;
+}
+
+uint64_t host_kmer_total(const uint64_t* off, uint64_t n, uint16_t K) {
+    uint64_t t = 0;
+    for (uint64_t r = 0; r < n; ++r) {
+        if (off[r + 1] < off[r]) return UINT64_MAX;
+        uint64_t L = off[r + 1] - off[r];
+        if (L >= K) t += L - K + 1;
+    }
+    return t;
+}
+
+int check_host_batch(const gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                     const uint64_t* offsets, uint64_t n_reads, uint64_t* total) {
+    if (!offsets || (n_reads && !packed && n_words))
+        return fail(GDBG_ERR_INVALID_ARG, "NULL batch buffers");
+    for (uint64_t r = 0; r < n_reads; ++r)
+        if (offsets[r + 1] < offsets[r]) return fail(GDBG_ERR_INVALID_ARG, "offsets must be non-decreasing");
+    if (n_reads && offsets[n_reads] > n_words * 16ull)
+        return fail(GDBG_ERR_INVALID_ARG, "offsets run past the packed stream");
+    *total = host_kmer_total(offsets, n_reads, g->K);
+    return GDBG_OK;
+}
+
+// Copy a host batch into the handle's staging buffers and prepare it.
+int stage_host_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                     const uint64_t* offsets, uint64_t n_reads, BatchView* view) {
+    uint64_t total = 0;
+    GDBG_TRY(check_host_batch(g, packed, n_words, offsets, n_reads, &total));
+    GDBG_TRY(g->st_packed.ensure(n_words + 1));
+    GDBG_TRY(g->st_offsets.ensure(n_reads + 1));
+    if (n_words)
+        GDBG_CUDA(cudaMemcpyAsync(g->st_packed.p, packed, n_words * sizeof(uint32_t),
+                                  cudaMemcpyHostToDevice, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(g->st_offsets.p, offsets, (n_reads + 1) * sizeof(uint64_t),
+                              cudaMemcpyHostToDevice, g->stream));
+    return prepare_batch(g, g->st_packed.p, n_words, g->st_offsets.p, n_reads, total, g->stream,
+                         view);
+}
+
+// Validate a string against DNA_SIMPLE and pack it as a one-read batch.
+int pack_string(const char* seq, uint64_t len, std::vector<uint32_t>& packed) {
+    if (!seq && len) return fail(GDBG_ERR_INVALID_ARG, "NULL sequence");
+    packed.assign(len / 16 + 1, 0u);
+    for (uint64_t i = 0; i < len; ++i) {
+        uint32_t c;
+        switch (seq[i]) {
+        case 'A': c = 0; break;
+        case 'C': c = 1; break;
+        case 'G': c = 2; break;
+        case 'T': c = 3; break;
+        default:
+            return fail(GDBG_ERR_INVALID_SEQUENCE,
+                        std::string("Alphabet: Invalid symbol '") + seq[i] + "' (alphabet=ACGT)");
+        }
+        packed[i >> 4] |= c << ((i & 15u) << 1);
+    }
+    return GDBG_OK;
+}
+
+int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view) {
+    if (len < g->K) return fail(GDBG_ERR_SEQUENCE_LENGTH, "Sequence must have length >= K");
+    std::vector<uint32_t> packed;
+    GDBG_TRY(pack_string(seq, len, packed));
+    uint64_t off[2] = {0, len};
+    return stage_host_batch(g, packed.data(), packed.size(), off, 1, view);
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* gdbg_last_error(void) { return g_last_error.c_str(); }
+const char* gdbg_version(void) { return "goetia_gb300 0.1 (sm_103a)"; }
+
+int gdbg_primes_near(uint32_t n, uint64_t x, uint64_t* out, uint32_t* n_out) {
+    if (!out || !n_out) return fail(GDBG_ERR_INVALID_ARG, "NULL output");
+    uint32_t got = 0;
+    if (x == 1) {
+        out[0] = 1;
+        *n_out = 1;
+        return GDBG_OK;
+    }
+    if (x == 0) {
+        *n_out = 0;
+        return GDBG_OK;
+    }
+    auto is_prime = [](uint64_t v) {
+        if (v < 2) return false;
+        if (v == 2) return true;
+        if (v % 2 == 0) return false;
+        for (uint64_t i = 3; i * i <= v; i += 2)
+            if (v % i == 0) return false;
+        return true;
+    };
+    uint64_t i = x - 1;
+    if (i % 2 == 0) i--;
+    while (got != n) {
+        if (is_prime(i)) out[got++] = i;
+        if (i <= 1) break;
+        i -= 2;
+    }
+    *n_out = got;
+    return GDBG_OK;
+}
+
+int gdbg_create(int storage, int shifter, uint16_t K, uint64_t max_table, uint16_t n_tables,
+                gdbg_graph** out) {
+    if (n_tables == 0 || n_tables > MAX_TABLES)
+        return fail(GDBG_ERR_INVALID_ARG, "n_tables must be in 1..32");
+    std::vector<uint64_t> sizes(n_tables);
+    uint32_t got = 0;
+    GDBG_TRY(gdbg_primes_near(n_tables, max_table, sizes.data(), &got));
+    if (got == 0) return fail(GDBG_ERR_INVALID_ARG, "no table sizes below max_table");
+    return make_graph(storage, shifter, K, sizes.data(), (uint16_t)got, out);
+}
+
+int gdbg_create_sized(int storage, int shifter, uint16_t K, const uint64_t* sizes,
+                      uint16_t n_tables, gdbg_graph** out) {
+    if (!sizes) return fail(GDBG_ERR_INVALID_ARG, "NULL sizes");
+    return make_graph(storage, shifter, K, sizes, n_tables, out);
+}
+
+int gdbg_destroy(gdbg_graph* g) {
+    if (!g) return GDBG_OK;
+    cudaSetDevice(g->device);
+    if (g->own_stream) cudaStreamSynchronize(g->own_stream);
+    if (g->stream && g->stream != g->own_stream) cudaStreamSynchronize(g->stream);
+    if (g->d_tables) cudaFree(g->d_tables);
+    if (g->d_counters) cudaFree(g->d_counters);
+    if (g->d_err) cudaFree(g->d_err);
+    g->fresh.release(); g->words_seen.release(); g->claims.release();
+    g->kofs.release(); g->partials.release(); g->tile_read.release();
+    g->st_packed.release(); g->st_offsets.release(); g->st_out64.release();
+    g->st_out64b.release(); g->st_out64c.release(); g->st_counts.release(); g->st_u8.release();
+    if (g->own_stream) cudaStreamDestroy(g->own_stream);
+    delete g;
+    return GDBG_OK;
+}
+
+int gdbg_clone(const gdbg_graph* g, gdbg_graph** out) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    GDBG_TRY(make_graph(g->storage, g->shifter, g->K, g->sizes.data(), (uint16_t)g->sizes.size(), out));
+    (*out)->window = g->window;
+    (*out)->kpt = g->kpt;
+    return GDBG_OK;
+}
+
+int gdbg_reset(gdbg_graph* g) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    GDBG_CUDA(cudaMemsetAsync(g->d_tables, 0, g->total_words * sizeof(uint32_t), g->stream));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    return GDBG_OK;
+}
+
+int gdbg_info(const gdbg_graph* g, int* storage, int* shifter, uint16_t* K, uint16_t* n_tables) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    if (storage) *storage = g->storage;
+    if (shifter) *shifter = g->shifter;
+    if (K) *K = g->K;
+    if (n_tables) *n_tables = (uint16_t)g->sizes.size();
+    return GDBG_OK;
+}
+
+int gdbg_get_tablesizes(const gdbg_graph* g, uint64_t* out) {
+    if (!g || !out) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    std::copy(g->sizes.begin(), g->sizes.end(), out);
+    return GDBG_OK;
+}
+
+int gdbg_table_bytes(const gdbg_graph* g, uint64_t* out) {
+    if (!g || !out) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    std::copy(g->bytes.begin(), g->bytes.end(), out);
+    return GDBG_OK;
+}
+
+int gdbg_get_tables(gdbg_graph* g, uint8_t* out, uint64_t out_len) {
+    if (!g || !out) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    uint64_t need = 0;
+    for (auto b : g->bytes) need += b;
+    if (out_len < need) return fail(GDBG_ERR_INVALID_ARG, "output buffer too small");
+    GDBG_TRY(set_device(g));
+    uint64_t pos = 0;
+    for (size_t i = 0; i < g->sizes.size(); ++i) {
+        GDBG_CUDA(cudaMemcpyAsync(out + pos, g->d_tables + g->word_off[i], g->bytes[i],
+                                  cudaMemcpyDeviceToHost, g->stream));
+        pos += g->bytes[i];
+    }
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    return GDBG_OK;
+}
+
+int gdbg_set_tables(gdbg_graph* g, const uint8_t* in, uint64_t in_len) {
+    if (!g || !in) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    uint64_t need = 0;
+    for (auto b : g->bytes) need += b;
+    if (in_len != need) return fail(GDBG_ERR_INVALID_ARG, "input length does not match the tables");
+    GDBG_TRY(set_device(g));
+    uint64_t pos = 0;
+    for (size_t i = 0; i < g->sizes.size(); ++i) {
+        GDBG_CUDA(cudaMemcpyAsync(g->d_tables + g->word_off[i], in + pos, g->bytes[i],
+                                  cudaMemcpyHostToDevice, g->stream));
+        pos += g->bytes[i];
+    }
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    return GDBG_OK;
+}
+
+int gdbg_stats(gdbg_graph* g, uint64_t* n_unique, uint64_t* n_occupied) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    unsigned long long c[2];
+    GDBG_CUDA(cudaMemcpyAsync(c, g->d_counters, sizeof c, cudaMemcpyDeviceToHost, g->stream));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    if (n_unique) *n_unique = c[0];
+    if (n_occupied) *n_occupied = c[1];
+    return GDBG_OK;
+}
+
+int gdbg_set_stream(gdbg_graph* g, void* stream) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    g->stream = stream ? (cudaStream_t)stream : g->own_stream;
+    return GDBG_OK;
+}
+
+int gdbg_synchronize(gdbg_graph* g) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    return check_device_status(g);
+}
+
+// ---- single sequences -------------------------------------------------------
+
+int gdbg_hash(gdbg_graph* g, const char* kmer, uint64_t len, uint64_t* value, uint64_t* fw,
+              uint64_t* rc) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    if (len < g->K)
+        return fail(GDBG_ERR_INVALID_SEQUENCE, "HashShifter::hash: Sequence must at least length K");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_string(g, kmer, g->K, &b));  // symbols past K are ignored, as in the reference
+    GDBG_TRY(g->st_out64.ensure(3));
+    GDBG_CUDA(launch_hashes(g->shifter == GDBG_CAN_LEMIRE, g->stream, b, g->hp, g->st_out64.p,
+                            g->st_out64.p + 1, g->st_out64.p + 2));
+    g->launches += 1;
+    uint64_t h[3];
+    GDBG_CUDA(cudaMemcpyAsync(h, g->st_out64.p, sizeof h, cudaMemcpyDeviceToHost, g->stream));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    if (value) *value = h[0];
+    if (fw) *fw = h[1];
+    if (rc) *rc = h[2];
+    return GDBG_OK;
+}
+
+int gdbg_insert_sequence(gdbg_graph* g, const char* seq, uint64_t len, uint64_t* n_kmers,
+                         uint64_t* n_new) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_string(g, seq, len, &b));
+    GDBG_TRY(g->st_out64.ensure(1));
+    GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, sizeof(uint64_t), g->stream));
+    GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, g->st_out64.p, g->stream));
+    uint64_t nn = 0;
+    GDBG_CUDA(cudaMemcpyAsync(&nn, g->st_out64.p, sizeof nn, cudaMemcpyDeviceToHost, g->stream));
+    GDBG_TRY(check_device_status(g));
+    if (n_kmers) *n_kmers = len - g->K + 1;
+    if (n_new) *n_new = nn;
+    return GDBG_OK;
+}
+
+int gdbg_query_sequence(gdbg_graph* g, const char* seq, uint64_t len, int16_t* counts,
+                        uint64_t* hashes) {
+    if (!g || !counts) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_string(g, seq, len, &b));
+    GDBG_TRY(g->st_counts.ensure(b.n_kmers));
+    if (hashes) GDBG_TRY(g->st_out64.ensure(b.n_kmers));
+    GDBG_TRY(run_query(g, b, nullptr, b.n_kmers, g->st_counts.p, hashes ? g->st_out64.p : nullptr,
+                       g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(counts, g->st_counts.p, b.n_kmers * sizeof(int16_t),
+                              cudaMemcpyDeviceToHost, g->stream));
+    if (hashes)
+        GDBG_CUDA(cudaMemcpyAsync(hashes, g->st_out64.p, b.n_kmers * sizeof(uint64_t),
+                                  cudaMemcpyDeviceToHost, g->stream));
+    return check_device_status(g);
+}
+
+int gdbg_hashes(gdbg_graph* g, const char* seq, uint64_t len, uint64_t* values, uint64_t* fw,
+                uint64_t* rc) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_string(g, seq, len, &b));
+    GDBG_TRY(g->st_out64.ensure(b.n_kmers));
+    GDBG_TRY(g->st_out64b.ensure(b.n_kmers));
+    GDBG_TRY(g->st_out64c.ensure(b.n_kmers));
+    GDBG_CUDA(launch_hashes(g->shifter == GDBG_CAN_LEMIRE, g->stream, b, g->hp, g->st_out64.p,
+                            g->st_out64b.p, g->st_out64c.p));
+    g->launches += 1;
+    const size_t nb = b.n_kmers * sizeof(uint64_t);
+    if (values) GDBG_CUDA(cudaMemcpyAsync(values, g->st_out64.p, nb, cudaMemcpyDeviceToHost, g->stream));
+    if (fw) GDBG_CUDA(cudaMemcpyAsync(fw, g->st_out64b.p, nb, cudaMemcpyDeviceToHost, g->stream));
+    if (rc) GDBG_CUDA(cudaMemcpyAsync(rc, g->st_out64c.p, nb, cudaMemcpyDeviceToHost, g->stream));
+    return check_device_status(g);
+}
+
+int gdbg_insert_hashes(gdbg_graph* g, const uint64_t* hashes, uint64_t n, uint8_t* is_new) {
+    if (!g || (n && !hashes)) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    if (n == 0) return GDBG_OK;
+    if (n >= (1ull << 32)) return fail(GDBG_ERR_INVALID_ARG, "at most 2^32-1 hashes per call");
+    GDBG_TRY(set_device(g));
+    GDBG_TRY(g->st_out64b.ensure(n));
+    GDBG_TRY(g->st_out64.ensure(n));
+    GDBG_CUDA(cudaMemcpyAsync(g->st_out64b.p, hashes, n * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                              g->stream));
+    GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, n * sizeof(uint64_t), g->stream));
+    BatchView b{};
+    b.n_kmers = n;
+    GDBG_TRY(run_insert(g, b, g->st_out64b.p, n, g->st_out64.p, g->stream));
+    std::vector<uint64_t> nn(is_new ? n : 0);
+    if (is_new)
+        GDBG_CUDA(cudaMemcpyAsync(nn.data(), g->st_out64.p, n * sizeof(uint64_t),
+                                  cudaMemcpyDeviceToHost, g->stream));
+    GDBG_TRY(check_device_status(g));
+    for (uint64_t i = 0; is_new && i < n; ++i) is_new[i] = nn[i] ? 1 : 0;
+    return GDBG_OK;
+}
+
+int gdbg_query_hashes(gdbg_graph* g, const uint64_t* hashes, uint64_t n, int16_t* counts) {
+    if (!g || (n && (!hashes || !counts))) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    if (n == 0) return GDBG_OK;
+    GDBG_TRY(set_device(g));
+    GDBG_TRY(g->st_out64b.ensure(n));
+    GDBG_TRY(g->st_counts.ensure(n));
+    GDBG_CUDA(cudaMemcpyAsync(g->st_out64b.p, hashes, n * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                              g->stream));
+    BatchView b{};
+    b.n_kmers = n;
+    GDBG_TRY(run_query(g, b, g->st_out64b.p, n, g->st_counts.p, nullptr, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(counts, g->st_counts.p, n * sizeof(int16_t), cudaMemcpyDeviceToHost,
+                              g->stream));
+    return check_device_status(g);
+}
+
+int gdbg_neighbor_masks(gdbg_graph* g, const char* seq, uint64_t len, uint8_t* masks) {
+    if (!g || !masks) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_string(g, seq, len, &b));
+    GDBG_TRY(g->st_u8.ensure(b.n_kmers));
+    GDBG_TRY(run_masks(g, b, g->st_u8.p, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(masks, g->st_u8.p, b.n_kmers, cudaMemcpyDeviceToHost, g->stream));
+    return check_device_status(g);
+}
+
+// ---- packed batches, host buffers ----------------------------------------
+
+int gdbg_insert_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                      const uint64_t* offsets, uint64_t n_reads, uint64_t* n_new,
+                      uint64_t* n_kmers) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b));
+    GDBG_TRY(g->st_out64.ensure(n_reads + 1));
+    if (n_new) GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, n_reads * sizeof(uint64_t), g->stream));
+    GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, n_new ? g->st_out64.p : nullptr, g->stream));
+    if (n_new && n_reads)
+        GDBG_CUDA(cudaMemcpyAsync(n_new, g->st_out64.p, n_reads * sizeof(uint64_t),
+                                  cudaMemcpyDeviceToHost, g->stream));
+    GDBG_TRY(check_device_status(g));
+    if (n_kmers) *n_kmers = b.n_kmers;
+    return GDBG_OK;
+}
+
+int gdbg_query_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                     const uint64_t* offsets, uint64_t n_reads, int16_t* counts) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b));
+    if (b.n_kmers && !counts) return fail(GDBG_ERR_INVALID_ARG, "NULL counts");
+    GDBG_TRY(g->st_counts.ensure(b.n_kmers + 1));
+    GDBG_TRY(run_query(g, b, nullptr, b.n_kmers, g->st_counts.p, nullptr, g->stream));
+    if (b.n_kmers)
+        GDBG_CUDA(cudaMemcpyAsync(counts, g->st_counts.p, b.n_kmers * sizeof(int16_t),
+                                  cudaMemcpyDeviceToHost, g->stream));
+    return check_device_status(g);
+}
+
+int gdbg_hashes_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                      const uint64_t* offsets, uint64_t n_reads, uint64_t* values, uint64_t* fw,
+                      uint64_t* rc) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b));
+    const uint64_t n = b.n_kmers + 1;
+    GDBG_TRY(g->st_out64.ensure(n));
+    GDBG_TRY(g->st_out64b.ensure(n));
+    GDBG_TRY(g->st_out64c.ensure(n));
+    GDBG_CUDA(launch_hashes(g->shifter == GDBG_CAN_LEMIRE, g->stream, b, g->hp, g->st_out64.p,
+                            fw ? g->st_out64b.p : nullptr, rc ? g->st_out64c.p : nullptr));
+    g->launches += 1;
+    const size_t nb = b.n_kmers * sizeof(uint64_t);
+    if (nb && values) GDBG_CUDA(cudaMemcpyAsync(values, g->st_out64.p, nb, cudaMemcpyDeviceToHost, g->stream));
+    if (nb && fw) GDBG_CUDA(cudaMemcpyAsync(fw, g->st_out64b.p, nb, cudaMemcpyDeviceToHost, g->stream));
+    if (nb && rc) GDBG_CUDA(cudaMemcpyAsync(rc, g->st_out64c.p, nb, cudaMemcpyDeviceToHost, g->stream));
+    return check_device_status(g);
+}
+
+int gdbg_neighbor_masks_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                              const uint64_t* offsets, uint64_t n_reads, uint8_t* masks) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b));
+    if (b.n_kmers && !masks) return fail(GDBG_ERR_INVALID_ARG, "NULL masks");
+    GDBG_TRY(g->st_u8.ensure(b.n_kmers + 1));
+    GDBG_TRY(run_masks(g, b, g->st_u8.p, g->stream));
+    if (b.n_kmers)
+        GDBG_CUDA(cudaMemcpyAsync(masks, g->st_u8.p, b.n_kmers, cudaMemcpyDeviceToHost, g->stream));
+    return check_device_status(g);
+}
+
+// ---- packed batches, device buffers ---------------------------------------
+
+int gdbg_insert_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                             const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
+                             uint64_t* n_new, void* stream) {
+    if (!g || !offsets) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    cudaStream_t st = pick_stream(g, stream);
+    BatchView b;
+    GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b));
+    if (n_new && n_reads) GDBG_CUDA(cudaMemsetAsync(n_new, 0, n_reads * sizeof(uint64_t), st));
+    return run_insert(g, b, nullptr, b.n_kmers, n_new, st);
+}
+
+int gdbg_query_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                            const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
+                            int16_t* counts, void* stream) {
+    if (!g || !offsets) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    cudaStream_t st = pick_stream(g, stream);
+    BatchView b;
+    GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b));
+    return run_query(g, b, nullptr, b.n_kmers, counts, nullptr, st);
+}
+
+int gdbg_hashes_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                             const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
+                             uint64_t* values, uint64_t* fw, uint64_t* rc, void* stream) {
+    if (!g || !offsets) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    cudaStream_t st = pick_stream(g, stream);
+    BatchView b;
+    GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b));
+    GDBG_CUDA(launch_hashes(g->shifter == GDBG_CAN_LEMIRE, st, b, g->hp, values, fw, rc));
+    g->launches += 1;
+    return GDBG_OK;
+}
+
+int gdbg_neighbor_masks_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                                     const uint64_t* offsets, uint64_t n_reads,
+                                     uint64_t n_kmers_hint, uint8_t* masks, void* stream) {
+    if (!g || !offsets) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    cudaStream_t st = pick_stream(g, stream);
+    BatchView b;
+    GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b));
+    return run_masks(g, b, masks, st);
+}
+
+// ---- tuning and diagnostics ------------------------------------------------
+
+int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmers_per_thread) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    if (window_kmers > (1u << 20))
+        return fail(GDBG_ERR_INVALID_ARG, "window must be at most 2^20 k-mers");
+    if (kmers_per_thread && kmers_per_thread != 4 && kmers_per_thread != 8)
+        return fail(GDBG_ERR_INVALID_ARG, "k-mers per thread must be 4 or 8");
+    if (window_kmers) g->window = window_kmers;
+    if (kmers_per_thread) g->kpt = kmers_per_thread;
+    return GDBG_OK;
+}
+
+int gdbg_get_insert_schedule(const gdbg_graph* g, uint32_t* window_kmers, uint32_t* kpt) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    if (window_kmers) *window_kmers = g->window;
+    if (kpt) *kpt = g->kpt;
+    return GDBG_OK;
+}
+
+int gdbg_device_status(gdbg_graph* g, uint32_t* status) {
+    if (!g || !status) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    GDBG_CUDA(cudaMemcpyAsync(status, g->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    GDBG_CUDA(cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    return GDBG_OK;
+}
+
+int gdbg_launch_count(const gdbg_graph* g, uint64_t* launches) {
+    if (!g || !launches) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    *launches = g->launches;
+    return GDBG_OK;
+}
+
+}  // extern "C"

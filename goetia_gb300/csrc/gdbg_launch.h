@@ -1,0 +1,47 @@
+// Host-side launchers.  Each storage translation unit defines the
+// launch_*<STORAGE> specialisations; the API code dispatches on the
+// handle's storage kind.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "gdbg_types.h"
+
+namespace gdbg {
+
+struct LaunchShape {
+    bool canonical;
+    int kmers_per_thread;   // 4 or 8
+    int n_tables;           // 4 uses the unrolled kernels, others the generic ones
+};
+
+// pass 0 = probe, 1 = commit; hashes != nullptr selects the hash-array source
+template <int STORAGE>
+cudaError_t launch_insert_pass(int pass, const LaunchShape& s, uint64_t n_threads,
+                               cudaStream_t st, const BatchView& b, const uint64_t* hashes,
+                               const HashParams& hp, const TableParams& tp,
+                               const WindowParams& w);
+
+template <int STORAGE>
+cudaError_t launch_query(const LaunchShape& s, uint64_t n_total, cudaStream_t st,
+                         const BatchView& b, const uint64_t* hashes, const HashParams& hp,
+                         const TableParams& tp, int16_t* counts, uint64_t* values);
+
+template <int STORAGE>
+cudaError_t launch_masks(const LaunchShape& s, cudaStream_t st, const BatchView& b,
+                         const HashParams& hp, const TableParams& tp, uint8_t* masks);
+
+cudaError_t launch_hashes(bool canonical, cudaStream_t st, const BatchView& b,
+                          const HashParams& hp, uint64_t* values, uint64_t* fw, uint64_t* rc);
+
+// Batch preparation (gdbg_batch.cu): per-read k-mer prefix and tile map.
+// Validates offsets (non-decreasing, within max_bases) on the device; a bad
+// read counts as zero k-mers and sets GDBG_ERR_BAD_OFFSETS in *err.
+cudaError_t launch_kmer_prefix(const uint64_t* offsets, uint64_t n_reads, uint32_t K,
+                               uint64_t max_bases, uint64_t* partials, uint64_t* kofs,
+                               uint32_t* err, cudaStream_t st, int* launches);
+cudaError_t launch_tile_map(const uint64_t* kofs, uint64_t n_reads, uint64_t n_tiles,
+                            uint32_t* tile_read, cudaStream_t st);
+
+constexpr uint32_t GDBG_ERR_BAD_OFFSETS = 8u;
+
+}  // namespace gdbg

@@ -1,0 +1,107 @@
+// Launcher definitions, instantiated once per storage kind by
+// gdbg_kernels_{bit,byte,nibble}.cu.
+#pragma once
+#include "gdbg_kernels.cuh"
+#include "gdbg_launch.h"
+
+namespace gdbg {
+
+inline unsigned grid_for(uint64_t n_threads) {
+    return (unsigned)((n_threads + BLOCK - 1) / BLOCK);
+}
+
+template <int ST, bool C, int H, int NT, bool FH>
+cudaError_t insert_pass_one(int pass, uint64_t n_threads, cudaStream_t st, const BatchView& b,
+                            const uint64_t* hashes, const HashParams& hp, const TableParams& tp,
+                            const WindowParams& w) {
+    if (n_threads == 0) return cudaSuccess;
+    if (pass == 0)
+        k_probe<ST, C, H, NT, FH><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hashes, hp, tp, w);
+    else
+        k_commit<ST, C, H, NT, FH><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hashes, hp, tp, w);
+    return cudaGetLastError();
+}
+
+template <int ST>
+cudaError_t launch_insert_pass(int pass, const LaunchShape& s, uint64_t n_threads,
+                               cudaStream_t st, const BatchView& b, const uint64_t* hashes,
+                               const HashParams& hp, const TableParams& tp,
+                               const WindowParams& w) {
+    const bool fh = hashes != nullptr;
+    const bool t4 = s.n_tables == 4;
+#define GDBG_PASS(C, H, NT, FH)                                                              \
+    if (s.canonical == C && s.kmers_per_thread == H && (NT == 4) == t4 && fh == FH)          \
+        return insert_pass_one<ST, C, H, NT, FH>(pass, n_threads, st, b, hashes, hp, tp, w);
+    GDBG_PASS(true, 4, 4, false) GDBG_PASS(true, 8, 4, false)
+    GDBG_PASS(false, 4, 4, false) GDBG_PASS(false, 8, 4, false)
+    GDBG_PASS(true, 4, 0, false) GDBG_PASS(true, 8, 0, false)
+    GDBG_PASS(false, 4, 0, false) GDBG_PASS(false, 8, 0, false)
+    if (fh) {
+        if (t4) return insert_pass_one<ST, false, 4, 4, true>(pass, n_threads, st, b, hashes, hp, tp, w);
+        return insert_pass_one<ST, false, 4, 0, true>(pass, n_threads, st, b, hashes, hp, tp, w);
+    }
+#undef GDBG_PASS
+    return cudaErrorInvalidValue;
+}
+
+template <int ST, bool C, int NT, bool FH>
+cudaError_t query_one(uint64_t n_total, cudaStream_t st, const BatchView& b, const uint64_t* hashes,
+                      const HashParams& hp, const TableParams& tp, int16_t* counts,
+                      uint64_t* values) {
+    constexpr int H = 4;
+    uint64_t n_threads = (n_total + H - 1) / H;
+    if (n_threads == 0) return cudaSuccess;
+    k_query<ST, C, H, NT, FH><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hashes, hp, tp, n_total,
+                                                                     counts, values);
+    return cudaGetLastError();
+}
+
+template <int ST>
+cudaError_t launch_query(const LaunchShape& s, uint64_t n_total, cudaStream_t st,
+                         const BatchView& b, const uint64_t* hashes, const HashParams& hp,
+                         const TableParams& tp, int16_t* counts, uint64_t* values) {
+    const bool t4 = s.n_tables == 4;
+    if (hashes) {
+        if (t4) return query_one<ST, false, 4, true>(n_total, st, b, hashes, hp, tp, counts, values);
+        return query_one<ST, false, 0, true>(n_total, st, b, hashes, hp, tp, counts, values);
+    }
+    if (s.canonical) {
+        if (t4) return query_one<ST, true, 4, false>(n_total, st, b, hashes, hp, tp, counts, values);
+        return query_one<ST, true, 0, false>(n_total, st, b, hashes, hp, tp, counts, values);
+    }
+    if (t4) return query_one<ST, false, 4, false>(n_total, st, b, hashes, hp, tp, counts, values);
+    return query_one<ST, false, 0, false>(n_total, st, b, hashes, hp, tp, counts, values);
+}
+
+template <int ST, bool C, int NT>
+cudaError_t masks_one(cudaStream_t st, const BatchView& b, const HashParams& hp,
+                      const TableParams& tp, uint8_t* masks) {
+    constexpr int H = 2;
+    uint64_t n_threads = (b.n_kmers + H - 1) / H;
+    if (n_threads == 0) return cudaSuccess;
+    k_masks<ST, C, H, NT><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hp, tp, masks);
+    return cudaGetLastError();
+}
+
+template <int ST>
+cudaError_t launch_masks(const LaunchShape& s, cudaStream_t st, const BatchView& b,
+                         const HashParams& hp, const TableParams& tp, uint8_t* masks) {
+    const bool t4 = s.n_tables == 4;
+    if (s.canonical) return t4 ? masks_one<ST, true, 4>(st, b, hp, tp, masks)
+                               : masks_one<ST, true, 0>(st, b, hp, tp, masks);
+    return t4 ? masks_one<ST, false, 4>(st, b, hp, tp, masks)
+              : masks_one<ST, false, 0>(st, b, hp, tp, masks);
+}
+
+#define GDBG_INSTANTIATE_LAUNCHERS(ST)                                                         \
+    template cudaError_t launch_insert_pass<ST>(int, const LaunchShape&, uint64_t, cudaStream_t, \
+                                                const BatchView&, const uint64_t*,             \
+                                                const HashParams&, const TableParams&,         \
+                                                const WindowParams&);                          \
+    template cudaError_t launch_query<ST>(const LaunchShape&, uint64_t, cudaStream_t,          \
+                                          const BatchView&, const uint64_t*, const HashParams&, \
+                                          const TableParams&, int16_t*, uint64_t*);            \
+    template cudaError_t launch_masks<ST>(const LaunchShape&, cudaStream_t, const BatchView&,  \
+                                          const HashParams&, const TableParams&, uint8_t*);
+
+}  // namespace gdbg

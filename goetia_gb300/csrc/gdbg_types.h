@@ -1,0 +1,56 @@
+// Parameter blocks shared by the host launchers and the kernels.
+#pragma once
+#include <cstdint>
+
+#include "goetia_gb300.h"
+
+namespace gdbg {
+
+constexpr int MAX_TABLES = 32;
+
+// Error bits accumulated in a device status word and surfaced by the C ABI.
+enum : uint32_t {
+    GDBG_ERR_CAS_LIMIT = 1u,      // a saturating compare-and-swap loop hit its cap
+    GDBG_ERR_CLAIMS_FULL = 2u,    // the first-touch map overflowed
+    GDBG_ERR_BARRIER_TIMEOUT = 4u // a grid barrier wait hit its cap
+};
+
+struct HashParams {
+    uint64_t tk[4];   // rotl(T[c], K mod 64) for the four codes
+    uint32_t K;
+};
+
+struct TableParams {
+    uint32_t* words[MAX_TABLES];  // table i as 32-bit words
+    uint64_t p[MAX_TABLES];       // table size (prime) in cells
+    uint64_t m[MAX_TABLES];       // floor((2^64-1)/p)
+    int n;
+};
+
+// A batch of reads already resident on the device.
+struct BatchView {
+    const uint32_t* packed;    // 2-bit base stream
+    const uint64_t* offsets;   // n_reads+1 base offsets
+    const uint64_t* kofs;      // n_reads+1 exclusive prefix of per-read k-mer counts
+    const uint32_t* tile_read; // read holding k-mer t*MAP_TILE, per map tile
+    uint64_t n_reads;
+    uint64_t n_kmers;          // host copy of kofs[n_reads]
+    uint64_t n_map_tiles;
+};
+
+constexpr uint64_t MAP_TILE = 1024;  // k-mers per entry of tile_read
+
+// One window of the insert: k-mers [start, end) of the batch.
+struct WindowParams {
+    uint64_t start, end;
+    uint32_t* fresh;       // per k-mer: bit i set when table i's cell was zero
+    uint32_t* words;       // per k-mer x table: word seen by the probe pass
+    uint64_t* claims;      // first-touch map
+    uint32_t claims_mask;
+    uint32_t epoch;
+    unsigned long long* n_new;   // per read (may be null)
+    unsigned long long* counters;// [0] n_unique, [1] n_occupied
+    uint32_t* err;
+};
+
+}  // namespace gdbg

@@ -1,0 +1,86 @@
+"""Packed read batches: the 2-bit base stream plus base offsets.
+
+``pack_reads`` applies goetia's FASTX-parser policy for DNA_SIMPLE
+(FastxParser::next, include/goetia/parsing/readers.hh:150-219): lowercase
+acgt are upper-cased, reads holding any other symbol or shorter than
+``min_length`` are dropped and counted.
+"""
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+
+
+@dataclass
+class PackedReads:
+    packed: np.ndarray    # uint32, 16 bases per word
+    offsets: np.ndarray   # uint64, n_reads + 1 base offsets
+    n_skipped: int = 0
+
+    @property
+    def n_reads(self):
+        return len(self.offsets) - 1
+
+    @property
+    def n_bases(self):
+        return int(self.offsets[-1]) if len(self.offsets) else 0
+
+    def n_kmers(self, K):
+        lens = np.diff(self.offsets.astype(np.int64))
+        return int(np.maximum(lens - K + 1, 0).sum())
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def pack_reads(seqs, min_length=0):
+    """Text reads (str or bytes) -> PackedReads, dropping invalid reads."""
+    enc = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+    data = b"".join(enc)
+    so = np.zeros(len(enc) + 1, np.uint64)
+    if enc:
+        so[1:] = np.cumsum([len(s) for s in enc], dtype=np.uint64)
+    words = len(data) // 16 + 1
+    packed = np.zeros(words, np.uint32)
+    offsets = np.zeros(len(enc) + 1, np.uint64)
+    kept = _lib.c_u64()
+    skipped = _lib.c_u64()
+    _lib.call("gdbg_pack_reads", data, _p(so, _lib.u64p), len(enc), min_length,
+              _p(packed, _lib.u32p), words, _p(offsets, _lib.u64p), kept, skipped)
+    n = int(kept.value)
+    used = (int(offsets[n]) + 15) // 16
+    return PackedReads(packed[:max(used, 1)].copy(), offsets[:n + 1].copy(), int(skipped.value))
+
+
+def pack_codes(codes):
+    """uint8 codes (A=0 C=1 G=2 T=3) -> uint32 packed stream."""
+    codes = np.ascontiguousarray(codes, np.uint8)
+    packed = np.zeros(len(codes) // 16 + 1, np.uint32)
+    _lib.call("gdbg_pack_codes", _p(codes, _lib.u8p), len(codes), _p(packed, _lib.u32p))
+    return packed
+
+
+def from_codes(reads):
+    """List / 2-D array of code rows -> PackedReads (no filtering)."""
+    if isinstance(reads, np.ndarray) and reads.ndim == 2:
+        flat = np.ascontiguousarray(reads, np.uint8).reshape(-1)
+        L = reads.shape[1]
+        offsets = np.arange(reads.shape[0] + 1, dtype=np.uint64) * np.uint64(L)
+    else:
+        rows = [np.asarray(r, np.uint8) for r in reads]
+        flat = np.concatenate(rows) if rows else np.zeros(0, np.uint8)
+        offsets = np.zeros(len(rows) + 1, np.uint64)
+        if rows:
+            offsets[1:] = np.cumsum([len(r) for r in rows], dtype=np.uint64)
+    return PackedReads(pack_codes(flat), offsets, 0)
+
+
+def codes_to_str(codes):
+    return "".join("ACGT"[int(c)] for c in codes)
+
+
+def str_to_codes(s):
+    t = {"A": 0, "C": 1, "G": 2, "T": 3}
+    return np.array([t[c] for c in s], np.uint8)

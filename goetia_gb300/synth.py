@@ -1,0 +1,99 @@
+"""Seeded synthetic genomes and reads (numpy), shared by the tests and bench.
+
+No public dataset is involved anywhere: every workload is generated here
+from fixed seeds with the shapes of the benchmark configurations (uniform
+random ACGT genomes; reads sampled uniformly from either strand with i.i.d.
+errors).  Codes are A=0 C=1 G=2 T=3.
+"""
+import numpy as np
+
+from .reads import PackedReads, pack_codes
+
+
+def genome(n, seed):
+    return np.random.default_rng(seed).integers(0, 4, n, dtype=np.uint8)
+
+
+def revcomp(codes):
+    return (3 - codes[..., ::-1]).astype(np.uint8)
+
+
+def substitute(rows, rate, rng):
+    """i.i.d. substitutions to a different base, in place on a 2-D code array."""
+    n = rows.size
+    k = rng.binomial(n, rate)
+    if k:
+        idx = rng.integers(0, n, k)
+        flat = rows.reshape(-1)
+        flat[idx] = (flat[idx] + rng.integers(1, 4, k, dtype=np.uint8)) & 3
+    return rows
+
+
+def sample_reads(g, n_reads, length, sub_rate, seed, rc_frac=0.5):
+    """n_reads x length code array: uniform starts, strand flip, substitutions."""
+    rng = np.random.default_rng(seed)
+    starts = rng.integers(0, len(g) - length + 1, n_reads)
+    win = np.lib.stride_tricks.sliding_window_view(g, length)
+    rows = win[starts].copy()
+    flip = rng.random(n_reads) < rc_frac
+    if flip.any():
+        rows[flip] = 3 - rows[flip][:, ::-1]
+    substitute(rows, sub_rate, rng)
+    return rows
+
+
+def rows_to_packed(rows):
+    rows = np.ascontiguousarray(rows, np.uint8)
+    n, L = rows.shape
+    offsets = np.arange(n + 1, dtype=np.uint64) * np.uint64(L)
+    return PackedReads(pack_codes(rows.reshape(-1)), offsets, 0)
+
+
+def n_read_mask(n_reads, frac, seed):
+    """Reads that carry an 'N' (dropped by the FASTX policy before packing)."""
+    return np.random.default_rng(seed).random(n_reads) < frac
+
+
+def uneven_reads(genomes, abundances, n_reads, median, sigma, lo, hi, sub, ins, dele, seed):
+    """Log-normal read lengths from several genomes with indel errors.
+
+    Returns a list of code arrays.  Each read is drawn from genome i with
+    probability proportional to abundances[i]; errors are applied per base:
+    substitution (to a different base), insertion (a random base before it)
+    or deletion, with the given rates.
+    """
+    rng = np.random.default_rng(seed)
+    w = np.asarray(abundances, float)
+    src = rng.choice(len(genomes), n_reads, p=w / w.sum())
+    lens = np.clip(np.exp(rng.normal(np.log(median), sigma, n_reads)), lo, hi).astype(np.int64)
+    out = []
+    for i in range(n_reads):
+        g = genomes[src[i]]
+        L = int(min(lens[i], len(g)))
+        s = int(rng.integers(0, len(g) - L + 1))
+        r = g[s:s + L].copy()
+        if rng.random() < 0.5:
+            r = revcomp(r)
+        u = rng.random(L)
+        keep = u >= dele
+        subm = (u >= dele) & (u < dele + sub)
+        r[subm] = (r[subm] + rng.integers(1, 4, int(subm.sum()), dtype=np.uint8)) & 3
+        insm = (u >= dele + sub) & (u < dele + sub + ins)
+        pieces = []
+        ins_pos = np.nonzero(insm)[0]
+        prev = 0
+        for p in ins_pos:
+            pieces.append(r[prev:p][keep[prev:p]])
+            pieces.append(rng.integers(0, 4, 1, dtype=np.uint8))
+            prev = p
+        pieces.append(r[prev:][keep[prev:]])
+        out.append(np.concatenate(pieces).astype(np.uint8))
+    return out
+
+
+def list_to_packed(reads):
+    flat = np.concatenate(reads) if reads else np.zeros(0, np.uint8)
+    offsets = np.zeros(len(reads) + 1, np.uint64)
+    if reads:
+        offsets[1:] = np.cumsum([len(r) for r in reads], dtype=np.uint64)
+    return PackedReads(pack_codes(flat), offsets, 0)

@@ -1,0 +1,191 @@
+/*
+ * goetia_gb300 -- C ABI of the GB300 (sm_103a) dBG hot path.
+ *
+ * A drop-in for goetia's dBG<Storage, Shifter> hashing / insert / query /
+ * neighbour-mask path (include/goetia/dbg.hh:39-438 and the layers under
+ * it).  One opaque graph handle owns its device tables, its CUDA stream and
+ * its scratch.  Every entry point returns GDBG_OK (0) or an error code; the
+ * message of the last error on the calling thread is gdbg_last_error().
+ * The reference throws C++ exceptions in the same places (see each entry).
+ *
+ * Reads enter in one of two forms:
+ *   - strings (char*, len), the reference's own argument type, validated
+ *     against DNA_SIMPLE ("ACGT");
+ *   - packed batches: a 2-bit base stream (A=0 C=1 G=2 T=3, 16 bases per
+ *     uint32_t, base j in bits 2*(j%16) of word j/16) plus n_reads+1 base
+ *     offsets.  gdbg_pack_reads builds one from text reads.
+ * k-mer outputs of a batch are flattened in read order; a read of length L
+ * has L-K+1 k-mers, reads shorter than K have none.
+ *
+ * Calls on one handle must be serialised by the caller; different handles
+ * may be used from different threads.  Functions named *_device take device
+ * pointers and are asynchronous on `stream` (NULL = the handle's stream;
+ * pass cudaStreamLegacy for the legacy default stream); all others take
+ * host pointers and return when results are on the host.
+ *
+ * File:line citations are relative to the goetia source tree.
+ */
+#ifndef GOETIA_GB300_H
+#define GOETIA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GDBG_OK 0
+#define GDBG_ERR_INVALID_ARG 1
+#define GDBG_ERR_SEQUENCE_LENGTH 2   /* SequenceLengthException, kmeriterator.hh:57-59,72-74 */
+#define GDBG_ERR_INVALID_SEQUENCE 3  /* InvalidCharacterException, alphabets.hh:41-56 */
+#define GDBG_ERR_CUDA 4
+#define GDBG_ERR_OOM 5
+#define GDBG_ERR_DEVICE 6            /* a device-side check failed (status word) */
+#define GDBG_ERR_IO 7                /* GoetiaFileException, bitstorage.cc:151-307 */
+#define GDBG_ERR_UNSUPPORTED 8
+
+/* storage kinds: BitStorage (bitstorage.hh:93), ByteStorage
+ * (bytestorage.hh:97), NibbleStorage (nibblestorage.hh:89) */
+#define GDBG_BIT 0
+#define GDBG_BYTE 1
+#define GDBG_NIBBLE 2
+/* shifter kinds: FwdLemireShifter / CanLemireShifter (hashshifter.hh:204-205) */
+#define GDBG_FWD_LEMIRE 0
+#define GDBG_CAN_LEMIRE 1
+
+typedef struct gdbg_graph gdbg_graph;
+
+const char* gdbg_last_error(void);
+const char* gdbg_version(void);
+
+/* ---- sizing and lifetime ---------------------------------------------- */
+
+/* get_n_primes_near_x(n, x): the n largest odd primes below x, descending
+ * (storage.hh:166-190).  *n_out may be < n when x is small. */
+int gdbg_primes_near(uint32_t n, uint64_t x, uint64_t* out, uint32_t* n_out);
+
+/* Storage::build(max_table, N) then dBG::build(storage, K)
+ * (bitstorage.hh:69-71, dbg.hh:108-121).  Table sizes come from
+ * gdbg_primes_near(n_tables, max_table). */
+int gdbg_create(int storage, int shifter, uint16_t K, uint64_t max_table,
+                uint16_t n_tables, gdbg_graph** out);
+/* Storage(const std::vector<uint64_t>& tablesizes) (bitstorage.hh:73-81). */
+int gdbg_create_sized(int storage, int shifter, uint16_t K, const uint64_t* sizes,
+                      uint16_t n_tables, gdbg_graph** out);
+int gdbg_destroy(gdbg_graph* g);
+/* dBG::clone: a new graph with empty storage of the same shape (dbg.hh:128-131). */
+int gdbg_clone(const gdbg_graph* g, gdbg_graph** out);
+/* dBG::reset / Storage::reset: zero every table (bitstorage.cc:140-148).
+ * Like the reference, the n_unique / n_occupied counters are kept. */
+int gdbg_reset(gdbg_graph* g);
+int gdbg_info(const gdbg_graph* g, int* storage, int* shifter, uint16_t* K, uint16_t* n_tables);
+/* Storage::get_tablesizes (bitstorage.hh:160-163). */
+int gdbg_get_tablesizes(const gdbg_graph* g, uint64_t* out);
+/* Byte length of each table in the reference layout (size/8+1, size, size/2+1). */
+int gdbg_table_bytes(const gdbg_graph* g, uint64_t* out);
+/* dBG::get_raw (dbg.hh:224-226): all tables, concatenated, reference byte layout. */
+int gdbg_get_tables(gdbg_graph* g, uint8_t* out, uint64_t out_len);
+int gdbg_set_tables(gdbg_graph* g, const uint8_t* in, uint64_t in_len);
+/* dBG::n_unique / n_occupied (dbg.hh:184-196). */
+int gdbg_stats(gdbg_graph* g, uint64_t* n_unique, uint64_t* n_occupied);
+/* Use the caller's CUDA stream (cudaStream_t) for this handle; NULL restores
+ * the handle's own stream. */
+int gdbg_set_stream(gdbg_graph* g, void* stream);
+int gdbg_synchronize(gdbg_graph* g);
+
+/* ---- single sequences (the reference's per-read API) ------------------- */
+
+/* HashShifter::hash(seq, K) on the first K symbols (hashshifter.hh:177-194);
+ * fw/rc may be NULL (rc is 0 for the forward shifter). */
+int gdbg_hash(gdbg_graph* g, const char* kmer, uint64_t len, uint64_t* value,
+              uint64_t* fw, uint64_t* rc);
+/* dBG::insert_sequence(seq, n_new) (dbg.hh:296-305): returns the k-mer count
+ * in *n_kmers and the number of new k-mers in *n_new (either may be NULL). */
+int gdbg_insert_sequence(gdbg_graph* g, const char* seq, uint64_t len,
+                         uint64_t* n_kmers, uint64_t* n_new);
+/* dBG::query_sequence(seq, counts, hashes) (dbg.hh:364-376); counts holds
+ * len-K+1 entries, hashes may be NULL. */
+int gdbg_query_sequence(gdbg_graph* g, const char* seq, uint64_t len, int16_t* counts,
+                        uint64_t* hashes);
+/* get_hash_iter over a sequence (dbg.hh:421-425): len-K+1 values; fw/rc may be NULL. */
+int gdbg_hashes(gdbg_graph* g, const char* seq, uint64_t len, uint64_t* values,
+                uint64_t* fw, uint64_t* rc);
+/* Storage insert / query / insert_and_query of hash values, in order
+ * (dbg.hh:144-177): n hashes; is_new / counts may be NULL. */
+int gdbg_insert_hashes(gdbg_graph* g, const uint64_t* hashes, uint64_t n, uint8_t* is_new);
+int gdbg_query_hashes(gdbg_graph* g, const uint64_t* hashes, uint64_t n, int16_t* counts);
+/* Neighbour masks of every k-mer of seq: bit i = left extension "ACGT"[i]
+ * present, bit 4+i = right extension present (set_cursor + in_degree /
+ * out_degree, unitig_walker.hh:322-330, hashextender.hh:352-396).  A k-mer
+ * is a decision k-mer iff popcount(mask & 15) > 1 or popcount(mask >> 4) > 1
+ * (is_decision_kmer, unitig_walker.hh:1003-1023). */
+int gdbg_neighbor_masks(gdbg_graph* g, const char* seq, uint64_t len, uint8_t* masks);
+
+/* ---- packed batches, host buffers -------------------------------------- */
+
+/* FastxParser<DNA_SIMPLE>::next policy (readers.hh:150-219): uppercase
+ * acgt, drop (and count) reads holding any other symbol or shorter than
+ * min_length.  packed needs total_len/16+1 words, offsets n_seqs+1. */
+int gdbg_pack_reads(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
+                    uint32_t min_length, uint32_t* packed, uint64_t packed_words,
+                    uint64_t* offsets, uint64_t* n_kept, uint64_t* n_skipped);
+/* 2-bit codes (one byte each, values 0..3) to the packed stream. */
+int gdbg_pack_codes(const uint8_t* codes, uint64_t n, uint32_t* packed);
+
+/* insert_sequence(seq, n_new) for every read in batch order (dbg.hh:296-305
+ * called by InserterProcessor, processors.hh:304-331).  n_new (per read,
+ * may be NULL) equals the reference's sequential result exactly. */
+int gdbg_insert_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                      const uint64_t* offsets, uint64_t n_reads, uint64_t* n_new,
+                      uint64_t* n_kmers);
+/* query_sequence for every read (dbg.hh:349-362): flattened counts. */
+int gdbg_query_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                     const uint64_t* offsets, uint64_t n_reads, int16_t* counts);
+/* get_hash_iter for every read: flattened values (and fw/rc, may be NULL). */
+int gdbg_hashes_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                      const uint64_t* offsets, uint64_t n_reads, uint64_t* values,
+                      uint64_t* fw, uint64_t* rc);
+/* Neighbour masks for every k-mer of every read (find_decision_kmers,
+ * unitig_walker.hh:1025-1045, with the per-k-mer mask kept). */
+int gdbg_neighbor_masks_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                              const uint64_t* offsets, uint64_t n_reads, uint8_t* masks);
+
+/* ---- packed batches, device buffers (asynchronous) --------------------- */
+
+/* Same as gdbg_insert_batch with device pointers, asynchronous on `stream`.
+ * packed_words bounds the packed stream: reads whose offsets decrease or run
+ * past 16*packed_words are rejected on the device (GDBG_ERR_DEVICE at the next
+ * synchronising call).  n_kmers_hint is the batch's k-mer count when the
+ * caller knows it (saves one device-to-host read), else UINT64_MAX.  n_new
+ * (device, one uint64 per read) may be NULL. */
+int gdbg_insert_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                             const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
+                             uint64_t* n_new, void* stream);
+int gdbg_query_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                            const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
+                            int16_t* counts, void* stream);
+int gdbg_hashes_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                             const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
+                             uint64_t* values, uint64_t* fw, uint64_t* rc, void* stream);
+int gdbg_neighbor_masks_batch_device(gdbg_graph* g, const uint32_t* packed,
+                                     uint64_t packed_words, const uint64_t* offsets,
+                                     uint64_t n_reads, uint64_t n_kmers_hint, uint8_t* masks,
+                                     void* stream);
+
+/* ---- tuning and diagnostics ------------------------------------------- */
+
+/* Insert schedule: k-mers per window (<= 2^20; each window is a probe pass
+ * then a commit pass) and k-mers per thread (1..16).  0 keeps a value. */
+int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmers_per_thread);
+int gdbg_get_insert_schedule(const gdbg_graph* g, uint32_t* window_kmers,
+                             uint32_t* kmers_per_thread);
+/* Device status word (GDBG_ERR_* device bits); cleared by reading. */
+int gdbg_device_status(gdbg_graph* g, uint32_t* status);
+/* Kernel launches issued by this handle since creation. */
+int gdbg_launch_count(const gdbg_graph* g, uint64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GOETIA_GB300_H */

@@ -1,0 +1,200 @@
+"""CPU oracle for the goetia dBG hot path -- TEST INFRASTRUCTURE ONLY.
+
+ctypes front end over ``oracle/_build/liboracle.so``, the plain-C restatement
+of the reference algorithm in ``goetia_oracle.c``.  Only the tests, the smoke
+check and the benchmark's CPU-baseline leg use this module, as the checker;
+the product path (``goetia_gb300``) never imports it.
+
+Read batches use the same encoding as the GPU library: a packed 2-bit base
+stream (``uint32``, 16 bases per word) plus ``n_reads + 1`` base offsets.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+BIT, BYTE, NIBBLE = 0, 1, 2
+KINDS = {"bit": BIT, "byte": BYTE, "nibble": NIBBLE}
+
+_lib = None
+
+u64p = ctypes.POINTER(ctypes.c_uint64)
+u32p = ctypes.POINTER(ctypes.c_uint32)
+u8p = ctypes.POINTER(ctypes.c_uint8)
+i16p = ctypes.POINTER(ctypes.c_int16)
+
+
+def build():
+    """Compile the C restatement (gcc, a second or two)."""
+    os.makedirs(os.path.join(HERE, "_build"), exist_ok=True)
+    src = os.path.join(HERE, "goetia_oracle.c")
+    tmp = LIB_PATH + ".tmp"
+    subprocess.check_call(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-pthread",
+                           "-o", tmp, src])
+    os.replace(tmp, LIB_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        src = os.path.join(HERE, "goetia_oracle.c")
+        if (not os.path.exists(LIB_PATH)
+                or os.path.getmtime(LIB_PATH) < os.path.getmtime(src)):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_storage_new.restype = ctypes.c_void_p
+        L.orc_storage_new.argtypes = [ctypes.c_int, u64p, ctypes.c_int]
+        L.orc_storage_free.argtypes = [ctypes.c_void_p]
+        L.orc_table_bytes.restype = ctypes.c_uint64
+        L.orc_table_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_table.restype = u8p
+        L.orc_table.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_stats.argtypes = [ctypes.c_void_p, u64p, u64p]
+        L.orc_insert.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.orc_query.restype = ctypes.c_int16
+        L.orc_query.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.orc_insert_and_query.restype = ctypes.c_int16
+        L.orc_insert_and_query.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.orc_primes.restype = ctypes.c_uint32
+        L.orc_primes.argtypes = [ctypes.c_uint32, ctypes.c_uint64, u64p]
+        L.orc_hash_codes.argtypes = [u8p, ctypes.c_uint64, ctypes.c_uint16, u64p, u64p]
+        L.orc_count_kmers.restype = ctypes.c_uint64
+        L.orc_count_kmers.argtypes = [ctypes.c_uint16, u64p, ctypes.c_uint64]
+        batch = [ctypes.c_int, ctypes.c_uint16, u32p, u64p, ctypes.c_uint64]
+        L.orc_hash_reads.argtypes = batch + [u64p, u64p, u64p]
+        L.orc_insert_reads.restype = ctypes.c_uint64
+        L.orc_insert_reads.argtypes = [ctypes.c_void_p] + batch + [u64p]
+        L.orc_insert_and_query_reads.argtypes = [ctypes.c_void_p] + batch + [i16p]
+        L.orc_query_reads.argtypes = [ctypes.c_void_p] + batch + [i16p]
+        L.orc_decision_masks.argtypes = [ctypes.c_void_p] + batch + [u8p]
+        L.orc_insert_reads_mt.restype = ctypes.c_uint64
+        L.orc_insert_reads_mt.argtypes = [ctypes.c_void_p] + batch + [ctypes.c_int]
+        L.orc_pack_ascii.restype = ctypes.c_int64
+        L.orc_pack_ascii.argtypes = [ctypes.c_char_p, u64p, ctypes.c_uint64, ctypes.c_uint32,
+                                     u32p, u64p, u64p]
+        L.orc_symbol_table.argtypes = [u64p]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def primes(n, x):
+    out = np.zeros(max(n, 1), np.uint64)
+    got = lib().orc_primes(n, x, _p(out, u64p))
+    return [int(v) for v in out[:got]]
+
+
+def hash_codes(codes, K):
+    """fw/rc rolling hashes of a code array (eat + update, cyclichash.h)."""
+    codes = np.ascontiguousarray(codes, np.uint8)
+    n = max(len(codes) - K + 1, 0)
+    fw = np.zeros(n, np.uint64)
+    rc = np.zeros(n, np.uint64)
+    if n:
+        lib().orc_hash_codes(_p(codes, u8p), len(codes), K, _p(fw, u64p), _p(rc, u64p))
+    return fw, rc
+
+
+class Storage:
+    """Bit/Byte/Nibble storage with the reference's sequential semantics."""
+
+    def __init__(self, kind, sizes):
+        self.kind = KINDS[kind] if isinstance(kind, str) else kind
+        self.sizes = np.ascontiguousarray(sizes, np.uint64)
+        self.h = lib().orc_storage_new(self.kind, _p(self.sizes, u64p), len(self.sizes))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_storage_free(self.h)
+            self.h = None
+
+    def insert(self, h):
+        return bool(lib().orc_insert(self.h, int(h)))
+
+    def query(self, h):
+        return int(lib().orc_query(self.h, int(h)))
+
+    def insert_and_query(self, h):
+        return int(lib().orc_insert_and_query(self.h, int(h)))
+
+    def tables(self):
+        L = lib()
+        out = []
+        for i in range(len(self.sizes)):
+            n = L.orc_table_bytes(self.h, i)
+            out.append(np.ctypeslib.as_array(L.orc_table(self.h, i), shape=(n,)).copy())
+        return out
+
+    def stats(self):
+        u, o = ctypes.c_uint64(), ctypes.c_uint64()
+        lib().orc_stats(self.h, ctypes.byref(u), ctypes.byref(o))
+        return int(u.value), int(o.value)
+
+    # -- read batches ------------------------------------------------------
+    def insert_reads(self, canonical, K, packed, offsets):
+        n = len(offsets) - 1
+        n_new = np.zeros(max(n, 1), np.uint64)
+        total = lib().orc_insert_reads(self.h, int(canonical), K, _p(packed, u32p),
+                                       _p(offsets, u64p), n, _p(n_new, u64p))
+        return int(total), n_new[:n]
+
+    def insert_reads_mt(self, canonical, K, packed, offsets, threads):
+        n = len(offsets) - 1
+        return int(lib().orc_insert_reads_mt(self.h, int(canonical), K, _p(packed, u32p),
+                                             _p(offsets, u64p), n, threads))
+
+    def insert_and_query_reads(self, canonical, K, packed, offsets):
+        nk = count_kmers(K, offsets)
+        out = np.zeros(max(nk, 1), np.int16)
+        lib().orc_insert_and_query_reads(self.h, int(canonical), K, _p(packed, u32p),
+                                         _p(offsets, u64p), len(offsets) - 1, _p(out, i16p))
+        return out[:nk]
+
+    def query_reads(self, canonical, K, packed, offsets):
+        nk = count_kmers(K, offsets)
+        out = np.zeros(max(nk, 1), np.int16)
+        lib().orc_query_reads(self.h, int(canonical), K, _p(packed, u32p), _p(offsets, u64p),
+                              len(offsets) - 1, _p(out, i16p))
+        return out[:nk]
+
+    def decision_masks(self, canonical, K, packed, offsets):
+        nk = count_kmers(K, offsets)
+        out = np.zeros(max(nk, 1), np.uint8)
+        lib().orc_decision_masks(self.h, int(canonical), K, _p(packed, u32p), _p(offsets, u64p),
+                                 len(offsets) - 1, _p(out, u8p))
+        return out[:nk]
+
+
+def count_kmers(K, offsets):
+    offsets = np.ascontiguousarray(offsets, np.uint64)
+    return int(lib().orc_count_kmers(K, _p(offsets, u64p), len(offsets) - 1))
+
+
+def hash_reads(canonical, K, packed, offsets):
+    nk = count_kmers(K, offsets)
+    val = np.zeros(max(nk, 1), np.uint64)
+    fw = np.zeros(max(nk, 1), np.uint64)
+    rc = np.zeros(max(nk, 1), np.uint64)
+    lib().orc_hash_reads(int(canonical), K, _p(packed, u32p), _p(offsets, u64p),
+                         len(offsets) - 1, _p(val, u64p), _p(fw, u64p), _p(rc, u64p))
+    return val[:nk], fw[:nk], rc[:nk]
+
+
+def pack_ascii(seqs, min_length=0):
+    """FASTX-parser policy packer: returns (packed, offsets, n_skipped)."""
+    data = b"".join(s.encode() if isinstance(s, str) else s for s in seqs)
+    so = np.zeros(len(seqs) + 1, np.uint64)
+    so[1:] = np.cumsum([len(s) for s in seqs])
+    packed = np.zeros(len(data) // 16 + 2, np.uint32)
+    offsets = np.zeros(len(seqs) + 1, np.uint64)
+    skipped = ctypes.c_uint64()
+    kept = lib().orc_pack_ascii(data, _p(so, u64p), len(seqs), min_length, _p(packed, u32p),
+                                _p(offsets, u64p), ctypes.byref(skipped))
+    return packed, offsets[:kept + 1].copy(), int(skipped.value)

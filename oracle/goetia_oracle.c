@@ -1,0 +1,481 @@
+/*
+ * CPU oracle for the goetia dBG hot path -- TEST INFRASTRUCTURE ONLY.
+ * See goetia_oracle.h for scope and encoding.  Every function restates the
+ * reference's sequential algorithm; file:line citations are relative to the
+ * goetia source tree.
+ */
+#define _GNU_SOURCE
+#include "goetia_oracle.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* CharacterHash::hashvalues entries for 'A', 'C', 'G', 'T'
+ * (include/goetia/hashing/rollinghash/characterhash.h:49-56; Lemire's
+ * rollinghashcpp, Apache-2.0), indexed by 2-bit code. */
+static const uint64_t SYM[4] = {
+    16664410744025174816ull, /* 'A' = 65 */
+    15956807086001210932ull, /* 'C' = 67 */
+    9404339731978646439ull,  /* 'G' = 71 */
+    836480985777824379ull,   /* 'T' = 84 */
+};
+
+void orc_symbol_table(uint64_t out[4]) { memcpy(out, SYM, sizeof(SYM)); }
+
+/* ---- CyclicHash<uint64_t> (rollinghash/cyclichash.h:24-138) ------------ */
+
+static inline uint64_t rotl64(uint64_t x, unsigned r) {
+    r &= 63u;
+    return r ? (x << r) | (x >> (64u - r)) : x;
+}
+
+typedef struct { uint64_t h; unsigned myr; } cyclic;
+
+static inline void cyc_reset(cyclic* c, uint16_t K) { c->h = 0; c->myr = K % 64u; }
+/* eat: fastleftshift1 then xor (cyclichash.h:105-108) */
+static inline void cyc_eat(cyclic* c, int sym) { c->h = rotl64(c->h, 1) ^ SYM[sym]; }
+/* update(out, in): rotl1(h) ^ rotl_{n mod 64}(T[out]) ^ T[in] (cyclichash.h:85-92) */
+static inline void cyc_update(cyclic* c, int out, int in) {
+    c->h = rotl64(c->h, 1) ^ rotl64(SYM[out], c->myr) ^ SYM[in];
+}
+/* reverse_update(out, in): h ^= rotl_n(T[out]) ^ T[in]; h = rotr1(h) (cyclichash.h:96-101) */
+static inline void cyc_reverse_update(cyclic* c, int out, int in) {
+    uint64_t x = c->h ^ rotl64(SYM[out], c->myr) ^ SYM[in];
+    c->h = (x >> 1) | (x << 63);
+}
+
+/* DNA_SIMPLE::complement on codes (alphabets.hh:132-144) */
+static inline int comp(int c) { return 3 - c; }
+
+/* ---- LemireShifterPolicy fw / canonical (rollinghashshifter.hh) -------- */
+
+typedef struct { cyclic fw, rc; int canonical; uint16_t K; } shifter;
+
+static void sh_init(shifter* s, int canonical, uint16_t K) {
+    s->canonical = canonical; s->K = K;
+    cyc_reset(&s->fw, K); cyc_reset(&s->rc, K);
+}
+
+typedef uint8_t (*base_fn)(const void* ctx, uint64_t i);
+
+/* hash_base_impl (rollinghashshifter.hh:65-77, canonical :180-197) */
+static void sh_hash_base(shifter* s, base_fn get, const void* ctx, uint64_t start) {
+    cyc_reset(&s->fw, s->K); cyc_reset(&s->rc, s->K);
+    for (uint16_t i = 0; i < s->K; ++i) {
+        cyc_eat(&s->fw, get(ctx, start + i));
+        if (s->canonical) cyc_eat(&s->rc, comp(get(ctx, start + s->K - 1 - i)));
+    }
+}
+/* shift_right_impl (rollinghashshifter.hh:100-103, canonical :200-208) */
+static inline void sh_shift_right(shifter* s, int out, int in) {
+    cyc_update(&s->fw, out, in);
+    if (s->canonical) cyc_reverse_update(&s->rc, comp(in), comp(out));
+}
+/* shift_left_impl (rollinghashshifter.hh:94-97, canonical :211-219) */
+static inline void sh_shift_left(shifter* s, int in, int out) {
+    cyc_reverse_update(&s->fw, in, out);
+    if (s->canonical) cyc_update(&s->rc, comp(out), comp(in));
+}
+/* Hash::value / Canonical::value (canonical.hh:58-60, 124-126) */
+static inline uint64_t sh_value(const shifter* s) {
+    if (!s->canonical) return s->fw.h;
+    return s->fw.h < s->rc.h ? s->fw.h : s->rc.h;
+}
+
+static uint8_t code_at(const void* ctx, uint64_t i) { return ((const uint8_t*)ctx)[i]; }
+static uint8_t packed_at(const void* ctx, uint64_t i) {
+    return (uint8_t)((((const uint32_t*)ctx)[i >> 4] >> ((i & 15u) << 1)) & 3u);
+}
+
+void orc_hash_codes(const uint8_t* codes, uint64_t len, uint16_t K,
+                    uint64_t* fw, uint64_t* rc) {
+    if (len < K) return;
+    shifter s; sh_init(&s, 1, K);
+    sh_hash_base(&s, code_at, codes, 0);
+    fw[0] = s.fw.h; rc[0] = s.rc.h;
+    for (uint64_t i = 1; i + K <= len; ++i) {
+        sh_shift_right(&s, codes[i - 1], codes[i + K - 1]);
+        fw[i] = s.fw.h; rc[i] = s.rc.h;
+    }
+}
+
+/* ---- table sizing (storage.hh:146-190) -------------------------------- */
+
+static int is_prime(uint64_t n) {
+    if (n < 2) return 0;
+    if (n == 2) return 1;
+    if (n % 2 == 0) return 0;
+    for (uint64_t i = 3; i * i <= n; i += 2)
+        if (n % i == 0) return 0;
+    return 1;
+}
+
+uint32_t orc_primes(uint32_t n, uint64_t x, uint64_t* out) {
+    uint32_t got = 0;
+    if (x == 1) { out[0] = 1; return 1; }
+    uint64_t i = x - 1;
+    if (i % 2 == 0) i--;
+    while (got != n) {
+        if (is_prime(i)) out[got++] = i;
+        if (i == 1) break;
+        i -= 2;
+    }
+    return got;
+}
+
+/* ---- storages ---------------------------------------------------------- */
+
+struct orc_storage {
+    int kind;
+    int n;
+    uint64_t sizes[64];
+    uint8_t* t[64];
+    uint64_t bytes[64];
+    uint64_t n_unique, n_occupied;
+};
+
+orc_storage* orc_storage_new(int kind, const uint64_t* sizes, int n_tables) {
+    if (n_tables < 1 || n_tables > 64) return NULL;
+    orc_storage* s = (orc_storage*)calloc(1, sizeof(*s));
+    s->kind = kind; s->n = n_tables;
+    for (int i = 0; i < n_tables; ++i) {
+        s->sizes[i] = sizes[i];
+        /* BitStorage: size/8+1 (bitstorage.hh:143-156); ByteStorage: size
+         * (bytestorage.hh:128-136); NibbleStorage: size/2+1 (nibblestorage.hh:166-177) */
+        s->bytes[i] = kind == ORC_BIT ? sizes[i] / 8 + 1
+                    : kind == ORC_NIBBLE ? sizes[i] / 2 + 1 : sizes[i];
+        s->t[i] = (uint8_t*)calloc(s->bytes[i], 1);
+    }
+    return s;
+}
+
+void orc_storage_free(orc_storage* s) {
+    if (!s) return;
+    for (int i = 0; i < s->n; ++i) free(s->t[i]);
+    free(s);
+}
+
+int orc_n_tables(const orc_storage* s) { return s->n; }
+uint64_t orc_table_bytes(const orc_storage* s, int i) { return s->bytes[i]; }
+const uint8_t* orc_table(const orc_storage* s, int i) { return s->t[i]; }
+void orc_stats(const orc_storage* s, uint64_t* u, uint64_t* o) { *u = s->n_unique; *o = s->n_occupied; }
+
+void orc_reset(orc_storage* s) {
+    for (int i = 0; i < s->n; ++i) memset(s->t[i], 0, s->bytes[i]);
+}
+
+/* BitStorage::insert (bitstorage.hh:195-219) */
+static int bit_insert(orc_storage* s, uint64_t h) {
+    int is_new = 0;
+    for (int i = 0; i < s->n; ++i) {
+        uint64_t bin = h % s->sizes[i];
+        uint8_t bit = (uint8_t)(1u << (bin % 8));
+        uint8_t orig = s->t[i][bin / 8];
+        s->t[i][bin / 8] = orig | bit;
+        if (!(orig & bit)) {
+            if (i == 0) s->n_occupied++;
+            is_new = 1;
+        }
+    }
+    if (is_new) s->n_unique++;
+    return is_new;
+}
+
+/* ByteStorage::insert without bigcount (bytestorage.cc:60-113) */
+static int byte_insert(orc_storage* s, uint64_t h) {
+    int is_new = 0;
+    for (int i = 0; i < s->n; ++i) {
+        uint64_t bin = h % s->sizes[i];
+        uint8_t cur = s->t[i][bin];
+        if (!is_new && cur == 0) {
+            is_new = 1;
+            if (i == 0) s->n_occupied++;
+        }
+        if (cur < 255) s->t[i][bin] = (uint8_t)(cur + 1);
+    }
+    if (is_new) s->n_unique++;
+    return is_new;
+}
+
+/* NibbleStorage layout: byte c/2, even c -> high nibble, odd -> low
+ * (nibblestorage.hh:109-122); insert (nibblestorage.cc:60-100) */
+static int nib_insert(orc_storage* s, uint64_t h) {
+    int is_new = 0;
+    for (int i = 0; i < s->n; ++i) {
+        uint64_t c = h % s->sizes[i];
+        uint64_t idx = c / 2;
+        uint8_t mask = (c % 2) ? 0x0F : 0xF0;
+        uint8_t shift = (c % 2) ? 0 : 4;
+        uint8_t cur = (uint8_t)((s->t[i][idx] & mask) >> shift);
+        if (!is_new && cur == 0) {
+            is_new = 1;
+            if (i == 0) s->n_occupied++;
+        }
+        if (cur == 15) continue;
+        uint8_t nc = (uint8_t)((cur + 1) << shift);
+        s->t[i][idx] = (uint8_t)((s->t[i][idx] & ~mask) | (nc & mask));
+    }
+    if (is_new) s->n_unique++;
+    return is_new;
+}
+
+int orc_insert(orc_storage* s, uint64_t h) {
+    switch (s->kind) {
+    case ORC_BIT: return bit_insert(s, h);
+    case ORC_BYTE: return byte_insert(s, h);
+    default: return nib_insert(s, h);
+    }
+}
+
+/* BitStorage::query (bitstorage.cc:87-100); ByteStorage::query
+ * (bytestorage.cc:116-139); NibbleStorage::query (nibblestorage.cc:112-130) */
+int16_t orc_query(const orc_storage* s, uint64_t h) {
+    if (s->kind == ORC_BIT) {
+        for (int i = 0; i < s->n; ++i) {
+            uint64_t bin = h % s->sizes[i];
+            if (!(s->t[i][bin / 8] & (1u << (bin % 8)))) return 0;
+        }
+        return 1;
+    }
+    if (s->kind == ORC_BYTE) {
+        int16_t m = 255;
+        for (int i = 0; i < s->n; ++i) {
+            int16_t c = s->t[i][h % s->sizes[i]];
+            if (c < m) m = c;
+        }
+        return m;
+    }
+    uint8_t m = 15;
+    for (int i = 0; i < s->n; ++i) {
+        uint64_t c = h % s->sizes[i];
+        uint8_t v = (uint8_t)((s->t[i][c / 2] & ((c % 2) ? 0x0F : 0xF0)) >> ((c % 2) ? 0 : 4));
+        if (v < m) m = v;
+    }
+    return m;
+}
+
+/* insert_and_query: Bit -> insert, 1 (bitstorage.cc:78-84); Byte/Nibble ->
+ * 1 if new else query (bytestorage.cc:142-150, nibblestorage.cc:102-109) */
+int16_t orc_insert_and_query(orc_storage* s, uint64_t h) {
+    int is_new = orc_insert(s, h);
+    if (s->kind == ORC_BIT) return 1;
+    return is_new ? 1 : orc_query(s, h);
+}
+
+/* ---- dBG over read batches (dbg.hh:249-394, kmeriterator.hh:63-123) ---- */
+
+uint64_t orc_count_kmers(uint16_t K, const uint64_t* off, uint64_t n) {
+    uint64_t t = 0;
+    for (uint64_t r = 0; r < n; ++r) {
+        uint64_t L = off[r + 1] - off[r];
+        if (L >= K) t += L - K + 1;
+    }
+    return t;
+}
+
+typedef void (*kmer_cb)(void* ctx, uint64_t read, uint64_t pos, const shifter* s);
+
+/* KmerIterator: hash_base over the first K bases, then
+ * shift_right(seq[i-1], seq[i+K-1]) per step (kmeriterator.hh:63-123).
+ * Reads shorter than K raise SequenceLengthException in the reference
+ * (kmeriterator.hh:72-74); here they are skipped, as InserterProcessor does. */
+static void walk_reads(int canonical, uint16_t K, const uint32_t* packed,
+                       const uint64_t* off, uint64_t n, uint64_t r0, uint64_t stride,
+                       kmer_cb cb, void* ctx) {
+    shifter s; sh_init(&s, canonical, K);
+    for (uint64_t r = r0; r < n; r += stride) {
+        uint64_t b = off[r], L = off[r + 1] - off[r];
+        if (L < K) continue;
+        sh_hash_base(&s, packed_at, packed, b);
+        cb(ctx, r, 0, &s);
+        for (uint64_t i = 1; i + K <= L; ++i) {
+            sh_shift_right(&s, packed_at(packed, b + i - 1), packed_at(packed, b + i + K - 1));
+            cb(ctx, r, i, &s);
+        }
+    }
+}
+
+typedef struct { uint64_t* val; uint64_t* fw; uint64_t* rc; uint64_t k; } hash_ctx;
+static void hash_cb(void* c, uint64_t r, uint64_t p, const shifter* s) {
+    hash_ctx* h = (hash_ctx*)c;
+    if (h->val) h->val[h->k] = sh_value(s);
+    if (h->fw) h->fw[h->k] = s->fw.h;
+    if (h->rc) h->rc[h->k] = s->canonical ? s->rc.h : 0;
+    h->k++;
+}
+
+void orc_hash_reads(int canonical, uint16_t K, const uint32_t* packed,
+                    const uint64_t* off, uint64_t n, uint64_t* val, uint64_t* fw, uint64_t* rc) {
+    hash_ctx h = {val, fw, rc, 0};
+    walk_reads(canonical, K, packed, off, n, 0, 1, hash_cb, &h);
+}
+
+typedef struct { orc_storage* s; uint64_t* n_new; uint64_t total; } ins_ctx;
+static void ins_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    ins_ctx* x = (ins_ctx*)c;
+    int nw = orc_insert(x->s, sh_value(sh));
+    if (x->n_new) x->n_new[r] += (uint64_t)nw;
+    x->total++;
+}
+
+/* dBG::insert_sequence(seq, n_new) per read in batch order (dbg.hh:296-305) */
+uint64_t orc_insert_reads(orc_storage* s, int canonical, uint16_t K, const uint32_t* packed,
+                          const uint64_t* off, uint64_t n, uint64_t* n_new) {
+    if (n_new) memset(n_new, 0, n * sizeof(uint64_t));
+    ins_ctx x = {s, n_new, 0};
+    walk_reads(canonical, K, packed, off, n, 0, 1, ins_cb, &x);
+    return x.total;
+}
+
+typedef struct { orc_storage* s; int16_t* counts; uint64_t k; } iq_ctx;
+static void iq_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    iq_ctx* x = (iq_ctx*)c;
+    x->counts[x->k++] = orc_insert_and_query(x->s, sh_value(sh));
+}
+
+/* dBG::insert_and_query_sequence (dbg.hh:327-340) */
+void orc_insert_and_query_reads(orc_storage* s, int canonical, uint16_t K, const uint32_t* packed,
+                                const uint64_t* off, uint64_t n, int16_t* counts) {
+    iq_ctx x = {s, counts, 0};
+    walk_reads(canonical, K, packed, off, n, 0, 1, iq_cb, &x);
+}
+
+typedef struct { const orc_storage* s; int16_t* counts; uint64_t k; } q_ctx;
+static void q_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    q_ctx* x = (q_ctx*)c;
+    x->counts[x->k++] = orc_query(x->s, sh_value(sh));
+}
+
+/* dBG::query_sequence (dbg.hh:349-362) */
+void orc_query_reads(const orc_storage* s, int canonical, uint16_t K, const uint32_t* packed,
+                     const uint64_t* off, uint64_t n, int16_t* counts) {
+    q_ctx x = {s, counts, 0};
+    walk_reads(canonical, K, packed, off, n, 0, 1, q_cb, &x);
+}
+
+/* Neighbour mask per k-mer: the cursor is the current k-mer;
+ * left_extensions = for sym in "ACGT": shift_left(sym, back), record,
+ * shift_right(sym, back) (hashextender.hh:352-364); right_extensions =
+ * shift_right(front, sym), record, shift_left(front, sym) (:386-396); a
+ * neighbour is present when query() != 0 (unitig_walker.hh:361-372).
+ * bit i = left "ACGT"[i], bit 4+i = right "ACGT"[i]. */
+typedef struct { const orc_storage* s; uint8_t* masks; uint64_t k;
+                 const uint32_t* packed; const uint64_t* off; uint16_t K; } m_ctx;
+static void m_cb(void* c, uint64_t r, uint64_t p, const shifter* cur) {
+    m_ctx* x = (m_ctx*)c;
+    uint64_t b = x->off[r] + p;
+    int front = packed_at(x->packed, b), back = packed_at(x->packed, b + x->K - 1);
+    shifter s = *cur;
+    uint8_t m = 0;
+    for (int sym = 0; sym < 4; ++sym) {
+        sh_shift_left(&s, sym, back);
+        if (orc_query(x->s, sh_value(&s))) m |= (uint8_t)(1u << sym);
+        sh_shift_right(&s, sym, back);
+    }
+    for (int sym = 0; sym < 4; ++sym) {
+        sh_shift_right(&s, front, sym);
+        if (orc_query(x->s, sh_value(&s))) m |= (uint8_t)(1u << (4 + sym));
+        sh_shift_left(&s, front, sym);
+    }
+    x->masks[x->k++] = m;
+}
+
+void orc_decision_masks(const orc_storage* s, int canonical, uint16_t K, const uint32_t* packed,
+                        const uint64_t* off, uint64_t n, uint8_t* masks) {
+    m_ctx x = {s, masks, 0, packed, off, K};
+    walk_reads(canonical, K, packed, off, n, 0, 1, m_cb, &x);
+}
+
+/* ---- multi-threaded insert (throughput baseline) ----------------------- */
+/* Atomic cell updates in the spirit of the reference's thread-safe storages
+ * (__sync_fetch_and_or bitstorage.hh:203-209; __sync_add_and_fetch
+ * bytestorage.cc:89).  Saturation uses compare-and-swap so final bytes stay
+ * exact. */
+static void atomic_insert(orc_storage* s, uint64_t h) {
+    for (int i = 0; i < s->n; ++i) {
+        uint64_t c = h % s->sizes[i];
+        if (s->kind == ORC_BIT) {
+            __atomic_fetch_or(&s->t[i][c / 8], (uint8_t)(1u << (c % 8)), __ATOMIC_RELAXED);
+        } else if (s->kind == ORC_BYTE) {
+            uint8_t* p = &s->t[i][c];
+            uint8_t cur = __atomic_load_n(p, __ATOMIC_RELAXED);
+            while (cur < 255 && !__atomic_compare_exchange_n(p, &cur, (uint8_t)(cur + 1), 1,
+                                                             __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {}
+        } else {
+            uint8_t* p = &s->t[i][c / 2];
+            unsigned sh = (c % 2) ? 0 : 4;
+            uint8_t cur = __atomic_load_n(p, __ATOMIC_RELAXED);
+            while (((cur >> sh) & 15u) < 15u &&
+                   !__atomic_compare_exchange_n(p, &cur, (uint8_t)(cur + (1u << sh)), 1,
+                                                __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {}
+        }
+    }
+}
+
+typedef struct { orc_storage* s; uint64_t total; } mt_ctx;
+static void mt_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    mt_ctx* x = (mt_ctx*)c;
+    atomic_insert(x->s, sh_value(sh));
+    x->total++;
+}
+
+typedef struct {
+    orc_storage* s; int canonical; uint16_t K; const uint32_t* packed;
+    const uint64_t* off; uint64_t n; uint64_t r0, stride; uint64_t total;
+} mt_job;
+
+static void* mt_run(void* arg) {
+    mt_job* j = (mt_job*)arg;
+    mt_ctx x = {j->s, 0};
+    walk_reads(j->canonical, j->K, j->packed, j->off, j->n, j->r0, j->stride, mt_cb, &x);
+    j->total = x.total;
+    return NULL;
+}
+
+uint64_t orc_insert_reads_mt(orc_storage* s, int canonical, uint16_t K, const uint32_t* packed,
+                             const uint64_t* off, uint64_t n, int n_threads) {
+    if (n_threads < 1) n_threads = 1;
+    pthread_t* th = (pthread_t*)calloc((size_t)n_threads, sizeof(pthread_t));
+    mt_job* jobs = (mt_job*)calloc((size_t)n_threads, sizeof(mt_job));
+    for (int t = 0; t < n_threads; ++t) {
+        mt_job j = {s, canonical, K, packed, off, n, (uint64_t)t, (uint64_t)n_threads, 0};
+        jobs[t] = j;
+        pthread_create(&th[t], NULL, mt_run, &jobs[t]);
+    }
+    uint64_t total = 0;
+    for (int t = 0; t < n_threads; ++t) { pthread_join(th[t], NULL); total += jobs[t].total; }
+    free(th); free(jobs);
+    return total;
+}
+
+/* ---- FASTX parser policy (readers.hh:150-219, alphabets.hh:41-56,107-130) */
+
+int64_t orc_pack_ascii(const char* seqs, const uint64_t* so, uint64_t n, uint32_t min_length,
+                       uint32_t* packed, uint64_t* off, uint64_t* n_skipped) {
+    uint64_t kept = 0, pos = 0, skipped = 0;
+    off[0] = 0;
+    for (uint64_t r = 0; r < n; ++r) {
+        const char* s = seqs + so[r];
+        uint64_t L = so[r + 1] - so[r];
+        int ok = 1;
+        for (uint64_t i = 0; i < L && ok; ++i) {
+            char c = s[i];
+            ok = c == 'A' || c == 'C' || c == 'G' || c == 'T' ||
+                 c == 'a' || c == 'c' || c == 'g' || c == 't';
+        }
+        if (!ok || L < min_length) { skipped++; continue; }
+        for (uint64_t i = 0; i < L; ++i) {
+            char c = s[i];
+            uint32_t code = (c == 'A' || c == 'a') ? 0 : (c == 'C' || c == 'c') ? 1
+                          : (c == 'G' || c == 'g') ? 2 : 3;
+            uint64_t j = pos + i;
+            if ((j & 15u) == 0) packed[j >> 4] = 0;
+            packed[j >> 4] |= code << ((j & 15u) << 1);
+        }
+        pos += L;
+        off[++kept] = pos;
+    }
+    *n_skipped = skipped;
+    return (int64_t)kept;
+}

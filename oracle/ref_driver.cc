@@ -1,0 +1,156 @@
+// Golden-vector driver for the reference goetia C++ hot path.
+//
+// Test infrastructure only: this program links the reference's own objects
+// (built by oracle/Makefile from the read-only reference sources into
+// oracle/_ref/) and writes the reference's answers for a set of reads, so the
+// C restatement in oracle/goetia_oracle.c and the CUDA library can be pinned
+// against the real thing.  Nothing in the product links or runs it.
+//
+// Usage:
+//   ref_driver <bit|byte|nibble> <can|fwd> <K> <n_tables> <max_table> <reads.txt> <outdir>
+//
+// reads.txt holds one read per line.  For every read, in file order, the
+// driver calls dBG::insert_sequence(seq, n_new) (dbg.hh:296-305), catching the
+// SequenceLengthException thrown for reads shorter than K the way
+// InserterProcessor does (processors.hh:304-331).  After all inserts it
+// records, per k-mer of every read:
+//   - the hash from get_hash_iter (dbg.hh:421-425), fw/rc for canonical;
+//   - query_sequence counts (dbg.hh:349-362);
+//   - an 8-bit neighbour mask: bit i = left extension "ACGT"[i] present,
+//     bit 4+i = right extension present, from set_cursor + left/right_extensions
+//     + query (hashextender.hh:352-396, unitig_walker.hh:361-397);
+// plus find_decision_kmers positions (unitig_walker.hh:1025-1045), the raw
+// table bytes (get_raw) and n_unique / n_occupied.
+#include "goetia/dbg.hh"
+#include "goetia/storage/bitstorage.hh"
+#include "goetia/storage/bytestorage.hh"
+#include "goetia/storage/nibblestorage.hh"
+#include "goetia/hashing/shifter_types.hh"
+
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+using namespace goetia;
+
+template <class T>
+static void dump(const std::string& path, const std::vector<T>& v) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) { std::perror(path.c_str()); std::exit(2); }
+    if (!v.empty()) std::fwrite(v.data(), sizeof(T), v.size(), f);
+    std::fclose(f);
+}
+
+template <class T> static uint64_t fw_of(const T& h);
+template <> uint64_t fw_of(const Canonical<uint64_t>& h) { return h.fw_hash; }
+template <> uint64_t fw_of(const Hash<uint64_t>& h) { return h.value(); }
+template <class T> static uint64_t rc_of(const T& h);
+template <> uint64_t rc_of(const Canonical<uint64_t>& h) { return h.rc_hash; }
+template <> uint64_t rc_of(const Hash<uint64_t>& h) { return 0; }
+
+template <class Storage, class Shifter>
+static int run(uint16_t K, uint16_t n_tables, uint64_t max_table,
+               const std::vector<std::string>& reads, const std::string& out) {
+    auto storage = Storage::build(max_table, n_tables);
+    auto graph = dBG<Storage, Shifter>::build(storage, K);
+    using hash_type = typename dBG<Storage, Shifter>::hash_type;
+
+    std::vector<uint64_t> n_new(reads.size(), 0), n_kmers(reads.size(), 0);
+    for (size_t r = 0; r < reads.size(); ++r) {
+        try {
+            uint64_t nn = 0;
+            n_kmers[r] = graph->insert_sequence(reads[r], nn);
+            n_new[r] = nn;
+        } catch (SequenceLengthException&) {
+            n_kmers[r] = 0;
+            n_new[r] = 0;
+        }
+    }
+
+    std::vector<uint64_t> fw, rc, val, dpos_read, dpos_pos;
+    std::vector<int16_t> counts;
+    std::vector<uint8_t> masks;
+    for (size_t r = 0; r < reads.size(); ++r) {
+        const std::string& s = reads[r];
+        if (s.size() < K) continue;
+        auto it = graph->get_hash_iter(s);
+        while (!it->done()) {
+            hash_type h = it->next();
+            fw.push_back(fw_of(h));
+            rc.push_back(rc_of(h));
+            val.push_back(h.value());
+        }
+        auto c = graph->query_sequence(s);
+        counts.insert(counts.end(), c.begin(), c.end());
+        for (size_t p = 0; p + K <= s.size(); ++p) {
+            graph->set_cursor(s.substr(p, K));
+            auto left = graph->left_extensions();
+            auto right = graph->right_extensions();
+            uint8_t m = 0;
+            for (size_t i = 0; i < left.size(); ++i)
+                if (graph->query(left[i])) m |= (uint8_t)(1u << i);
+            for (size_t i = 0; i < right.size(); ++i)
+                if (graph->query(right[i])) m |= (uint8_t)(1u << (4 + i));
+            masks.push_back(m);
+        }
+        std::vector<uint32_t> positions;
+        std::vector<hash_type> dhashes;
+        std::vector<typename dBG<Storage, Shifter>::neighbor_pair_type> neighbors;
+        graph->find_decision_kmers(s, positions, dhashes, neighbors);
+        for (auto p : positions) { dpos_read.push_back(r); dpos_pos.push_back(p); }
+    }
+
+    auto sizes = storage->get_tablesizes();
+    dump(out + "/sizes.u64", sizes);
+    dump(out + "/n_new.u64", n_new);
+    dump(out + "/n_kmers.u64", n_kmers);
+    dump(out + "/fw.u64", fw);
+    dump(out + "/rc.u64", rc);
+    dump(out + "/val.u64", val);
+    dump(out + "/counts.i16", counts);
+    dump(out + "/masks.u8", masks);
+    dump(out + "/dpos_read.u64", dpos_read);
+    dump(out + "/dpos_pos.u64", dpos_pos);
+    uint8_t** raw = graph->get_raw();
+    for (size_t i = 0; i < sizes.size(); ++i) {
+        uint64_t nbytes = std::is_same<Storage, BitStorage>::value ? sizes[i] / 8 + 1
+                        : std::is_same<Storage, NibbleStorage>::value ? sizes[i] / 2 + 1
+                        : sizes[i];
+        std::vector<uint8_t> t(raw[i], raw[i] + nbytes);
+        dump(out + "/table" + std::to_string(i) + ".u8", t);
+    }
+    std::vector<uint64_t> stats = {graph->n_unique(), graph->n_occupied()};
+    dump(out + "/stats.u64", stats);
+    return 0;
+}
+
+int main(int argc, char** argv) {
+    if (argc != 8) {
+        std::fprintf(stderr, "usage: %s <bit|byte|nibble> <can|fwd> <K> <n_tables> <max_table> <reads.txt> <outdir>\n", argv[0]);
+        return 1;
+    }
+    std::string kind = argv[1], shifter = argv[2];
+    uint16_t K = (uint16_t)std::atoi(argv[3]);
+    uint16_t N = (uint16_t)std::atoi(argv[4]);
+    uint64_t max_table = std::strtoull(argv[5], nullptr, 10);
+    std::vector<std::string> reads;
+    std::ifstream in(argv[6]);
+    std::string line;
+    while (std::getline(in, line)) reads.push_back(line);
+    std::string out = argv[7];
+    bool can = shifter == "can";
+    if (kind == "bit")
+        return can ? run<BitStorage, CanLemireShifter>(K, N, max_table, reads, out)
+                   : run<BitStorage, FwdLemireShifter>(K, N, max_table, reads, out);
+    if (kind == "byte")
+        return can ? run<ByteStorage, CanLemireShifter>(K, N, max_table, reads, out)
+                   : run<ByteStorage, FwdLemireShifter>(K, N, max_table, reads, out);
+    if (kind == "nibble")
+        return can ? run<NibbleStorage, CanLemireShifter>(K, N, max_table, reads, out)
+                   : run<NibbleStorage, FwdLemireShifter>(K, N, max_table, reads, out);
+    std::fprintf(stderr, "unknown storage %s\n", kind.c_str());
+    return 1;
+}

@@ -1,0 +1,93 @@
+"""The C ABI library: builds, loads, exports every declared symbol, and its
+host-only helpers (table sizing, read packing) agree with the oracle.
+CPU only -- nothing here launches a kernel."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from goetia_gb300 import _lib, build, reads
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))
+           if f.endswith(".h")]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def declared():
+    out = set()
+    for h in HEADERS:
+        text = open(h).read()
+        out |= set(re.findall(r"^\s*(?:int|const char\*)\s+(gdbg_\w+)\s*\(", text, re.M))
+    return out
+
+
+def test_header_declares_entry_points():
+    names = declared()
+    assert "gdbg_insert_batch" in names and "gdbg_create" in names
+    assert len(names) > 30
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared():
+        assert hasattr(lib, name), name
+
+
+def test_binding_table_matches_header():
+    names = declared() - {"gdbg_last_error", "gdbg_version"}
+    assert set(_lib.SIGNATURES) <= declared()
+    missing = names - set(_lib.SIGNATURES)
+    assert not missing, missing
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.gdbg_version()
+
+
+@pytest.mark.parametrize("n,x", [(4, 4194304), (4, 1 << 30), (3, 10), (1, 1), (4, 1000), (5, 12)])
+def test_primes_near(lib, n, x):
+    out = np.zeros(n, np.uint64)
+    got = ctypes.c_uint32()
+    _lib.call("gdbg_primes_near", n, x, out.ctypes.data_as(_lib.u64p), ctypes.byref(got))
+    assert [int(v) for v in out[:got.value]] == oracle.primes(n, x)
+
+
+def test_pack_reads_matches_parser_policy():
+    rng = np.random.default_rng(3)
+    alphabet = np.array(list("ACGTacgtNnXY"))
+    seqs = []
+    for i in range(300):
+        L = int(rng.integers(0, 70))
+        p = np.r_[np.full(8, 0.12), np.full(4, 0.01)]
+        seqs.append("".join(rng.choice(alphabet, L, p=p / p.sum())))
+    for min_len in (0, 20):
+        got = reads.pack_reads(seqs, min_length=min_len)
+        ref_packed, ref_off, ref_skip = oracle.pack_ascii(seqs, min_length=min_len)
+        assert got.n_skipped == ref_skip
+        assert np.array_equal(got.offsets, ref_off)
+        n_words = (int(ref_off[-1]) + 15) // 16
+        assert np.array_equal(got.packed[:n_words], ref_packed[:n_words])
+
+
+def test_pack_codes_layout():
+    rng = np.random.default_rng(4)
+    c = rng.integers(0, 4, 1000, dtype=np.uint8)
+    p = reads.pack_codes(c)
+    j = np.arange(1000)
+    assert np.array_equal((p[j >> 4] >> (2 * (j & 15)).astype(np.uint32)) & 3, c)
+
+
+def test_storage_params_mirror():
+    from goetia_gb300 import BitStorage, ByteStorage, NibbleStorage
+    s = BitStorage.build(4194304, 4)
+    assert s.get_tablesizes() == [4194301, 4194287, 4194277, 4194271]
+    assert BitStorage.build().get_tablesizes() == oracle.primes(4, 1_000_000)
+    assert ByteStorage.is_counting and NibbleStorage.is_counting and not BitStorage.is_counting

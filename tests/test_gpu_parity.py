@@ -1,0 +1,233 @@
+"""GPU parity: the CUDA path against the reference's golden fixtures and the
+oracle, bit-exact (hashes, per-read new counts, table bytes, counts, masks,
+n_unique / n_occupied).  Every check here goes through libgoetia_gb300.so."""
+import numpy as np
+import pytest
+
+import oracle
+from goldens import Case, names
+import goetia_gb300 as G
+from goetia_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+STORAGES = {"bit": G.BitStorage, "byte": G.ByteStorage, "nibble": G.NibbleStorage}
+SHIFTERS = {True: G.CanLemireShifter, False: G.FwdLemireShifter}
+
+
+def graph_for(kind, canonical, K, sizes):
+    st = STORAGES[kind](tablesizes=[int(s) for s in sizes])
+    return G.dBG[STORAGES[kind], SHIFTERS[canonical]].build(st, K)
+
+
+def check_tables(g, tables):
+    got = g.get_raw()
+    assert len(got) == len(tables)
+    for a, b in zip(got, tables):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", names())
+def test_golden_plain_per_read(cuda_ready, name):
+    """insert_sequence per read (the drop-in, one call per read)."""
+    c = Case(name)
+    g = graph_for(c.storage, c.canonical, c.K, c.sizes)
+    for r, s in enumerate(c.reads):
+        if len(s) < c.K:
+            with pytest.raises(G.SequenceLengthException):
+                g.insert_sequence_new(s)
+            assert c.n_new[r] == 0
+            continue
+        nk, nn = g.insert_sequence_new(s)
+        assert nk == int(c.n_kmers[r])
+        assert nn == int(c.n_new[r]), (r, nn, int(c.n_new[r]))
+    check_tables(g, c.tables)
+    assert (g.n_unique(), g.n_occupied()) == (c.n_unique, c.n_occupied)
+    k = 0
+    for s in c.reads:
+        if len(s) < c.K:
+            continue
+        n = len(s) - c.K + 1
+        assert g.query_sequence(s) == [int(x) for x in c.counts[k:k + n]]
+        val, fw, rc = g.hash_array(s)
+        assert np.array_equal(val, c.val[k:k + n])
+        if c.canonical:
+            assert np.array_equal(fw, c.fw[k:k + n]) and np.array_equal(rc, c.rc[k:k + n])
+        assert np.array_equal(g.neighbor_masks(s), c.masks[k:k + n])
+        k += n
+
+
+@pytest.mark.parametrize("name", names())
+@pytest.mark.parametrize("window,kpt", [(262144, 4), (64, 8), (5, 4)])
+def test_golden_batched(cuda_ready, name, window, kpt):
+    """One packed batch; windows smaller than the batch exercise the
+    cross-window first-touch logic."""
+    c = Case(name)
+    g = graph_for(c.storage, c.canonical, c.K, c.sizes)
+    g.set_insert_schedule(window, kpt)
+    packed, off = c.packed()
+    pr = G.PackedReads(packed, off)
+    n_new = g.insert_packed(pr)
+    assert np.array_equal(n_new, c.n_new)
+    check_tables(g, c.tables)
+    assert (g.n_unique(), g.n_occupied()) == (c.n_unique, c.n_occupied)
+    assert np.array_equal(g.query_packed(pr), c.counts)
+    val, fw, rc = g.hashes_packed(pr)
+    assert np.array_equal(val, c.val)
+    if c.canonical:
+        assert np.array_equal(fw, c.fw) and np.array_equal(rc, c.rc)
+    masks = g.neighbor_masks_packed(pr)
+    assert np.array_equal(masks, c.masks)
+    assert c.decision_positions(masks) == c.dpos
+
+
+def test_known_answer_k27(cuda_ready):
+    g = graph_for("bit", True, 27, [1009, 1013])
+    h = g.hash("TCACCTGTGTTGTGCTACTTGCGGCGC")
+    assert h.fw_hash == 13194817695400542713 and h.rc_hash == 4324216031038051805
+    assert int(h) == 4324216031038051805
+    # symbols past K are ignored (tests/test_dbg.py:124-127)
+    assert int(g.hash("A" * 27)) == int(g.hash("A" * 27 + "TTTT"))
+
+
+def _oracle_run(kind, canonical, K, sizes, pr):
+    st = oracle.Storage(kind, sizes)
+    total, n_new = st.insert_reads(canonical, K, pr.packed, pr.offsets)
+    return st, n_new
+
+
+@pytest.mark.parametrize("kind,canonical,K,max_table", [
+    ("bit", True, 31, 1 << 22),       # config 1 shape: 4 Bloom tables of ~2^22 bits
+    ("byte", True, 31, 50021),
+    ("nibble", False, 21, 40009),
+    ("bit", False, 25, 7919),
+])
+def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table):
+    """10,000 reads of 150 bp from a 100 kb genome, 1% substitutions."""
+    gen = synth.genome(100_000, 1)
+    rows = synth.sample_reads(gen, 10_000, 150, 0.01, 2)
+    pr = synth.rows_to_packed(rows)
+    sizes = oracle.primes(4, max_table)
+    st, n_new_ref = _oracle_run(kind, canonical, K, sizes, pr)
+    g = graph_for(kind, canonical, K, sizes)
+    g.set_insert_schedule(65536, 4)
+    n_new = g.insert_packed(pr)
+    assert np.array_equal(n_new, n_new_ref)
+    check_tables(g, st.tables())
+    assert (g.n_unique(), g.n_occupied()) == st.stats()
+    assert np.array_equal(g.query_packed(pr), st.query_reads(canonical, K, pr.packed, pr.offsets))
+    assert np.array_equal(g.neighbor_masks_packed(pr),
+                          st.decision_masks(canonical, K, pr.packed, pr.offsets))
+
+
+def test_batches_in_sequence_vs_oracle(cuda_ready):
+    """Several batches into one graph equal one sequential pass."""
+    gen = synth.genome(30_000, 7)
+    sizes = oracle.primes(4, 30011)
+    st = oracle.Storage("byte", sizes)
+    g = graph_for("byte", True, 31, sizes)
+    for b in range(4):
+        rows = synth.sample_reads(gen, 700, 150, 0.02, 100 + b)
+        pr = synth.rows_to_packed(rows)
+        _, ref = st.insert_reads(True, 31, pr.packed, pr.offsets)
+        assert np.array_equal(g.insert_packed(pr), ref)
+    check_tables(g, st.tables())
+    assert (g.n_unique(), g.n_occupied()) == st.stats()
+
+
+def test_uneven_reads_vs_oracle(cuda_ready):
+    """Log-normal lengths with indels, many zero-k-mer reads mixed in."""
+    gens = [synth.genome(20_000, 50 + i) for i in range(3)]
+    rs = synth.uneven_reads(gens, [1, 2, 4], 300, 400, 1.0, 5, 3000, 0.04, 0.02, 0.02, 9)
+    pr = synth.list_to_packed(rs)
+    sizes = oracle.primes(4, 60013)
+    st, ref = _oracle_run("nibble", False, 21, sizes, pr)
+    g = graph_for("nibble", False, 21, sizes)
+    g.set_insert_schedule(4096, 8)
+    assert np.array_equal(g.insert_packed(pr), ref)
+    check_tables(g, st.tables())
+    assert (g.n_unique(), g.n_occupied()) == st.stats()
+
+
+def test_hash_array_insert_query_vs_oracle(cuda_ready):
+    """Raw hash values, with fastmod edge values and duplicates."""
+    rng = np.random.default_rng(21)
+    sizes = [1000003, 999983, 65537, 3]
+    edge = []
+    for p in sizes:
+        edge += [0, p - 1, p, p + 1, 2 * p - 1, (2**64 - 1) // p * p, 2**64 - 1]
+    h = np.concatenate([np.array(edge, np.uint64), rng.integers(0, 2**64 - 1, 20000, np.uint64,
+                                                                endpoint=True)])
+    h = np.concatenate([h, h[:500], rng.choice(h, 3000)])
+    for kind in ("bit", "byte", "nibble"):
+        st = oracle.Storage(kind, sizes)
+        ref_new = np.array([st.insert(int(x)) for x in h])
+        g = graph_for(kind, True, 31, sizes)
+        assert np.array_equal(g.insert_hashes(h), ref_new)
+        check_tables(g, st.tables())
+        assert (g.n_unique(), g.n_occupied()) == st.stats()
+        assert np.array_equal(g.query_hashes(h), np.array([st.query(int(x)) for x in h], np.int16))
+
+
+def test_mirror_semantics(cuda_ready):
+    """Presence / counting semantics of the reference's tests/test_dbg.py:19-102."""
+    rng = np.random.default_rng(8)
+    seq = "".join(rng.choice(list("ACGT"), 60))
+    for kind in ("bit", "byte", "nibble"):
+        g = graph_for(kind, True, 21, oracle.primes(4, 10007))
+        for i in range(len(seq) - 20):
+            kmer = seq[i:i + 21]
+            h = g.hash(kmer)
+            assert g.query(kmer) == 0 and g.query(h) == 0
+            assert g.insert(kmer) is True
+            assert g.query(kmer) == 1
+            assert g.insert(kmer) is False
+            assert g.query(h) == (1 if kind == "bit" else 2)
+        with pytest.raises(G.SequenceLengthException):
+            g.insert_sequence("ATGCA")
+        with pytest.raises(G.InvalidSequenceException):
+            g.insert_sequence("ACGTN" * 10)
+        c = g.clone()
+        assert c.n_unique() == 0 and g.n_unique() > 0
+        assert all(int(t.sum()) == 0 for t in c.get_raw())
+
+
+def test_device_pointer_api(cuda_ready):
+    import torch
+    gen = synth.genome(20_000, 3)
+    rows = synth.sample_reads(gen, 2000, 150, 0.01, 4)
+    pr = synth.rows_to_packed(rows)
+    sizes = oracle.primes(4, 20011)
+    st, ref = _oracle_run("bit", True, 31, sizes, pr)
+    g = graph_for("bit", True, 31, sizes)
+    d_packed = torch.from_numpy(pr.packed.view(np.int32)).cuda()
+    d_off = torch.from_numpy(pr.offsets.view(np.int64)).cuda()
+    d_new = torch.zeros(pr.n_reads, dtype=torch.int64, device="cuda")
+    s = torch.cuda.current_stream()
+    g.insert_device(d_packed.data_ptr(), d_packed.numel(), d_off.data_ptr(), pr.n_reads,
+                    n_new_ptr=d_new.data_ptr(), stream=s.cuda_stream)
+    s.synchronize()
+    assert np.array_equal(d_new.cpu().numpy().view(np.uint64), ref)
+    check_tables(g, st.tables())
+    nk = pr.n_kmers(31)
+    d_cnt = torch.zeros(nk, dtype=torch.int16, device="cuda")
+    g.query_device(d_packed.data_ptr(), d_packed.numel(), d_off.data_ptr(), pr.n_reads,
+                   d_cnt.data_ptr(), n_kmers=nk, stream=s.cuda_stream)
+    s.synchronize()
+    assert np.array_equal(d_cnt.cpu().numpy(), st.query_reads(True, 31, pr.packed, pr.offsets))
+
+
+def test_device_offsets_validated(cuda_ready):
+    """Offsets that decrease or run past the packed stream are rejected on
+    the device (counted as zero k-mers) and reported, without reading past
+    the buffers."""
+    import torch
+    g = graph_for("bit", True, 31, oracle.primes(4, 10007))
+    packed = torch.zeros(64, dtype=torch.int32, device="cuda")
+    off = torch.tensor([0, 200, 100, 5000], dtype=torch.int64, device="cuda")
+    g.insert_device(packed.data_ptr(), packed.numel(), off.data_ptr(), 3)
+    with pytest.raises(G.GoetiaError):
+        g.synchronize()
+    assert g.device_status() == 0
+    # the graph is still usable
+    assert g.insert_sequence("ACGT" * 10) == 10

@@ -1,0 +1,75 @@
+"""The CPU oracle (oracle/goetia_oracle.c) pinned against the reference.
+
+Pins: the K=27 known-answer hash from the reference's own tests
+(tests/test_hashing.py:15-19) and the golden fixtures written by the
+reference's C++ objects (tests/golden/make_golden.py).  CPU only.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from goldens import Case, names
+
+KNOWN_KMER = "TCACCTGTGTTGTGCTACTTGCGGCGC"
+KNOWN_FWD = 13194817695400542713
+KNOWN_RC = 4324216031038051805
+
+
+def codes(s):
+    return np.array(["ACGT".index(c) for c in s], np.uint8)
+
+
+def test_known_answer_k27():
+    fw, rc = oracle.hash_codes(codes(KNOWN_KMER), 27)
+    assert int(fw[0]) == KNOWN_FWD
+    assert int(rc[0]) == KNOWN_RC
+    assert min(int(fw[0]), int(rc[0])) == KNOWN_RC   # known_can = known_rc
+
+
+def test_rolling_equals_recomputed():
+    rng = np.random.default_rng(5)
+    s = rng.integers(0, 4, 300, dtype=np.uint8)
+    for K in (1, 21, 31, 63, 64, 65, 101, 128):
+        fw, rc = oracle.hash_codes(s, K)
+        for p in (0, 1, 17, len(s) - K):
+            f1, r1 = oracle.hash_codes(s[p:p + K], K)
+            assert fw[p] == f1[0] and rc[p] == r1[0]
+            # canonical == min(fw(kmer), fw(revcomp(kmer))) (test_hashing.py:161-172)
+            frc, _ = oracle.hash_codes((3 - s[p:p + K][::-1]).astype(np.uint8), K)
+            assert rc[p] == frc[0]
+
+
+def test_primes():
+    # config 1 table sizes, verified against get_n_primes_near_x
+    assert oracle.primes(4, 4194304) == [4194301, 4194287, 4194277, 4194271]
+    assert oracle.primes(3, 10) == [7, 5, 3]
+    assert oracle.primes(1, 1) == [1]
+
+
+@pytest.mark.parametrize("name", names())
+def test_oracle_matches_golden(name):
+    c = Case(name)
+    packed, off = c.packed()
+    val, fw, rc = oracle.hash_reads(c.canonical, c.K, packed, off)
+    assert np.array_equal(val, c.val)
+    if c.canonical:
+        assert np.array_equal(fw, c.fw) and np.array_equal(rc, c.rc)
+    st = oracle.Storage(c.storage, c.sizes)
+    total, n_new = st.insert_reads(c.canonical, c.K, packed, off)
+    assert total == int(c.n_kmers.sum())
+    assert np.array_equal(n_new, c.n_new)
+    for a, b in zip(st.tables(), c.tables):
+        assert np.array_equal(a, b)
+    assert st.stats() == (c.n_unique, c.n_occupied)
+    assert np.array_equal(st.query_reads(c.canonical, c.K, packed, off), c.counts)
+    masks = st.decision_masks(c.canonical, c.K, packed, off)
+    assert np.array_equal(masks, c.masks)
+    assert c.decision_positions(masks) == c.dpos
+
+
+def test_pack_policy():
+    reads = ["ACGT", "acgtN", "aCgT", "", "ACGX", "TTTT"]
+    packed, off, skipped = oracle.pack_ascii(reads)
+    assert skipped == 2
+    assert list(off) == [0, 4, 8, 8, 12]
+    assert packed[0] & 0xFF == 0b11100100  # A C G T -> 0 1 2 3
