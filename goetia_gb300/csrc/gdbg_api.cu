@@ -99,9 +99,16 @@ struct gdbg_graph {
     DevBuf<uint32_t> fresh, words_seen;
     DevBuf<uint64_t> claims;
     uint32_t claims_mask = 0, epoch = 0;
+    // persistent insert: device-owned claims epoch and grid-barrier state
+    uint32_t pwindow = 262144;
+    bool persistent = true;
+    uint32_t* d_epoch = nullptr;
+    unsigned int* d_bar = nullptr;
+    bool epoch_on_device = false;
+    uint32_t epoch_staging = 0;
     // batch scratch
-    DevBuf<uint64_t> kofs, partials;
-    DevBuf<uint32_t> tile_read;
+    DevBuf<uint64_t> kofs, tofs, partials;
+    DevBuf<uint32_t> tile_read, task_read;
     // staging for host-pointer calls
     DevBuf<uint32_t> st_packed;
     DevBuf<uint64_t> st_offsets, st_out64, st_out64b, st_out64c;
@@ -168,8 +175,12 @@ int make_graph(int storage, int shifter, uint16_t K, const uint64_t* sizes, uint
         return cleanup(fail(GDBG_ERR_CUDA, "cudaStreamCreate failed"));
     g->stream = g->own_stream;
     if (cudaMalloc((void**)&g->d_counters, 2 * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMalloc((void**)&g->d_err, sizeof(uint32_t)) != cudaSuccess)
+        cudaMalloc((void**)&g->d_err, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&g->d_epoch, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&g->d_bar, 2 * sizeof(unsigned int)) != cudaSuccess)
         return cleanup(fail(GDBG_ERR_OOM, "counter allocation failed"));
+    cudaMemsetAsync(g->d_epoch, 0, sizeof(uint32_t), g->stream);
+    cudaMemsetAsync(g->d_bar, 0, 2 * sizeof(unsigned int), g->stream);
     cudaMemsetAsync(g->d_tables, 0, off * sizeof(uint32_t), g->stream);
     cudaMemsetAsync(g->d_counters, 0, 2 * sizeof(unsigned long long), g->stream);
     cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
@@ -207,22 +218,33 @@ int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                   const uint64_t* offsets, uint64_t n_reads, uint64_t hint, cudaStream_t st,
                   BatchView* view) {
     GDBG_TRY(g->kofs.ensure(n_reads + 1));
-    GDBG_TRY(g->partials.ensure(n_reads / 1024 + 2));
+    GDBG_TRY(g->tofs.ensure(n_reads + 1));
+    GDBG_TRY(g->partials.ensure(2 * (n_reads / 1024 + 2)));
     int nl = 0;
     GDBG_CUDA(launch_kmer_prefix(offsets, n_reads, g->K, packed_words * 16ull, g->partials.p,
-                                 g->kofs.p, g->d_err, st, &nl));
+                                 g->kofs.p, g->tofs.p, g->d_err, st, &nl));
     g->launches += nl;
-    uint64_t total = hint;
+    uint64_t total = hint, tasks = 0;
     if (total == UINT64_MAX) {
-        GDBG_CUDA(cudaMemcpyAsync(&total, g->kofs.p + n_reads, sizeof(uint64_t),
+        uint64_t tt[2];
+        GDBG_CUDA(cudaMemcpyAsync(&tt[0], g->kofs.p + n_reads, sizeof(uint64_t),
+                                  cudaMemcpyDeviceToHost, st));
+        GDBG_CUDA(cudaMemcpyAsync(&tt[1], g->tofs.p + n_reads, sizeof(uint64_t),
                                   cudaMemcpyDeviceToHost, st));
         GDBG_CUDA(cudaStreamSynchronize(st));
+        total = tt[0];
+        tasks = tt[1];
+    } else {
+        // every read adds at most one partly filled task
+        tasks = total / TASK_KMERS + std::min<uint64_t>(n_reads, total);
     }
     uint64_t tiles = (total + MAP_TILE - 1) / MAP_TILE;
     GDBG_TRY(g->tile_read.ensure(tiles + 1));
+    GDBG_TRY(g->task_read.ensure(tasks + 1));
     if (total) {
         GDBG_CUDA(launch_tile_map(g->kofs.p, n_reads, tiles, g->tile_read.p, st));
-        g->launches += 1;
+        GDBG_CUDA(launch_task_map(g->tofs.p, n_reads, tasks, g->task_read.p, st));
+        g->launches += 2;
     }
     view->packed = packed;
     view->offsets = offsets;
@@ -231,6 +253,9 @@ int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
     view->n_reads = n_reads;
     view->n_kmers = total;
     view->n_map_tiles = tiles;
+    view->tofs = g->tofs.p;
+    view->task_read = g->task_read.p;
+    view->task_cap = tasks;
     return GDBG_OK;
 }
 
@@ -272,11 +297,66 @@ int launch_pass(gdbg_graph* g, int pass, const LaunchShape& s, uint64_t n_thread
     return GDBG_OK;
 }
 
+// Persistent cooperative insert of a read batch (one launch per batch).
+int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaStream_t st) {
+    if (b.n_kmers == 0 || b.task_cap == 0) return GDBG_OK;
+    const uint64_t W = g->pwindow, n = g->sizes.size();
+    GDBG_TRY(g->fresh.ensure(W));
+    if (g->storage != GDBG_BIT) GDBG_TRY(g->words_seen.ensure(W * n));
+    const uint32_t slots = next_pow2(W * n + W * n / 4);
+    if (g->claims.cap < slots) {
+        g->claims.release();
+        GDBG_TRY(g->claims.ensure(slots));
+        GDBG_CUDA(cudaMemsetAsync(g->claims.p, 0, g->claims.cap * sizeof(uint64_t), st));
+        g->epoch = 0;
+        g->epoch_on_device = false;
+    }
+    if (!g->epoch_on_device) {
+        // hand the host-driven epoch counter to the device
+        g->epoch_staging = g->epoch;
+        GDBG_CUDA(cudaMemcpyAsync(g->d_epoch, &g->epoch_staging, sizeof(uint32_t),
+                                  cudaMemcpyHostToDevice, st));
+        g->epoch_on_device = true;
+    }
+    GDBG_CUDA(cudaMemsetAsync(g->d_bar, 0, 2 * sizeof(unsigned int), st));
+    PersistParams pp;
+    pp.window_tasks = (uint32_t)(W / TASK_KMERS);
+    pp.fresh = g->fresh.p;
+    pp.words = g->words_seen.p;
+    pp.claims = g->claims.p;
+    pp.claims_mask = slots - 1;
+    pp.epoch_state = g->d_epoch;
+    pp.n_new = (unsigned long long*)n_new;
+    pp.counters = g->d_counters;
+    pp.err = g->d_err;
+    pp.bar = g->d_bar;
+    LaunchShape s = g->shape(4);
+    int grid = 0;
+    cudaError_t e;
+    switch (g->storage) {
+    case GDBG_BIT: e = launch_insert_persistent<GDBG_BIT>(s, b.task_cap, st, b, g->hp, g->tp, pp, &grid); break;
+    case GDBG_BYTE: e = launch_insert_persistent<GDBG_BYTE>(s, b.task_cap, st, b, g->hp, g->tp, pp, &grid); break;
+    default: e = launch_insert_persistent<GDBG_NIBBLE>(s, b.task_cap, st, b, g->hp, g->tp, pp, &grid); break;
+    }
+    if (e != cudaSuccess)
+        return fail(GDBG_ERR_CUDA, std::string("persistent insert launch: ") + cudaGetErrorString(e));
+    g->launches += 1;
+    return GDBG_OK;
+}
+
 // Windowed probe + commit over n_total k-mers (from the batch or a hash array).
 int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64_t n_total,
                uint64_t* n_new, cudaStream_t st) {
     if (n_total == 0) return GDBG_OK;
+    if (!hashes && g->persistent) return run_insert_persistent(g, b, n_new, st);
     GDBG_TRY(ensure_insert_scratch(g, st));
+    if (g->epoch_on_device) {
+        // the device owns the epoch counter: start the host-driven windows
+        // from a cleared map
+        GDBG_CUDA(cudaMemsetAsync(g->claims.p, 0, g->claims.cap * sizeof(uint64_t), st));
+        g->epoch = 0;
+        g->epoch_on_device = false;
+    }
     const int kpt = hashes ? 4 : (int)g->kpt;
     LaunchShape s = g->shape(kpt);
     for (uint64_t start = 0; start < n_total; start += g->window) {
@@ -459,8 +539,11 @@ int gdbg_destroy(gdbg_graph* g) {
     if (g->d_tables) cudaFree(g->d_tables);
     if (g->d_counters) cudaFree(g->d_counters);
     if (g->d_err) cudaFree(g->d_err);
+    if (g->d_epoch) cudaFree(g->d_epoch);
+    if (g->d_bar) cudaFree(g->d_bar);
     g->fresh.release(); g->words_seen.release(); g->claims.release();
-    g->kofs.release(); g->partials.release(); g->tile_read.release();
+    g->kofs.release(); g->tofs.release(); g->partials.release(); g->tile_read.release();
+    g->task_read.release();
     g->st_packed.release(); g->st_offsets.release(); g->st_out64.release();
     g->st_out64b.release(); g->st_out64c.release(); g->st_counts.release(); g->st_u8.release();
     if (g->own_stream) cudaStreamDestroy(g->own_stream);
@@ -474,6 +557,8 @@ int gdbg_clone(const gdbg_graph* g, gdbg_graph** out) {
     GDBG_TRY(make_graph(g->storage, g->shifter, g->K, g->sizes.data(), (uint16_t)g->sizes.size(), out));
     (*out)->window = g->window;
     (*out)->kpt = g->kpt;
+    (*out)->pwindow = g->pwindow;
+    (*out)->persistent = g->persistent;
     return GDBG_OK;
 }
 
@@ -817,8 +902,19 @@ int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmer
         return fail(GDBG_ERR_INVALID_ARG, "window must be at most 2^20 k-mers");
     if (kmers_per_thread && kmers_per_thread != 4 && kmers_per_thread != 8)
         return fail(GDBG_ERR_INVALID_ARG, "k-mers per thread must be 4 or 8");
-    if (window_kmers) g->window = window_kmers;
+    if (window_kmers) {
+        g->window = window_kmers;
+        g->pwindow = std::max<uint32_t>(TASK_KMERS, window_kmers / TASK_KMERS * TASK_KMERS);
+    }
     if (kmers_per_thread) g->kpt = kmers_per_thread;
+    return GDBG_OK;
+}
+
+int gdbg_set_insert_path(gdbg_graph* g, int path) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    if (path != GDBG_PATH_PERSISTENT && path != GDBG_PATH_WINDOWED)
+        return fail(GDBG_ERR_INVALID_ARG, "unknown insert path");
+    g->persistent = path == GDBG_PATH_PERSISTENT;
     return GDBG_OK;
 }
 

@@ -47,53 +47,72 @@ __device__ __forceinline__ uint64_t block_inclusive_scan(uint64_t v, uint64_t* w
     return v;
 }
 
+// Per read: v.x = k-mers, v.y = warp tasks (ceil(k-mers / 32)).
+__device__ __forceinline__ ulonglong2 read_counts(const uint64_t* __restrict__ off, uint64_t r,
+                                                 uint32_t K, uint64_t max_bases, uint32_t* err) {
+    uint64_t nk = read_kmers(off, r, K, max_bases, err);
+    return make_ulonglong2(nk, (nk + TASK_KMERS - 1) / TASK_KMERS);
+}
+
 __global__ void __launch_bounds__(SCAN_BLOCK)
 k_prefix_partials(const uint64_t* __restrict__ off, uint64_t n, uint32_t K, uint64_t max_bases,
                   uint64_t* __restrict__ partials, uint32_t* err) {
-    __shared__ uint64_t ws[32];
+    __shared__ uint64_t ws[32], wt[32];
     uint64_t r = (uint64_t)blockIdx.x * SCAN_BLOCK + threadIdx.x;
-    uint64_t v = r < n ? read_kmers(off, r, K, max_bases, err) : 0;
-    uint64_t s = block_inclusive_scan(v, ws);
-    if (threadIdx.x == SCAN_BLOCK - 1) partials[blockIdx.x] = s;
+    ulonglong2 v = r < n ? read_counts(off, r, K, max_bases, err) : make_ulonglong2(0, 0);
+    uint64_t s = block_inclusive_scan(v.x, ws);
+    uint64_t t = block_inclusive_scan(v.y, wt);
+    if (threadIdx.x == SCAN_BLOCK - 1) {
+        partials[2 * blockIdx.x] = s;
+        partials[2 * blockIdx.x + 1] = t;
+    }
 }
 
-// Exclusive scan of the block partials in place, one block.
+// Exclusive scan of the (k-mer, task) block partials in place, one block.
 __global__ void __launch_bounds__(SCAN_BLOCK)
 k_prefix_partials_scan(uint64_t* __restrict__ partials, uint64_t nb) {
     __shared__ uint64_t ws[32];
     __shared__ uint64_t chunk_total;
-    uint64_t carry = 0;
-    for (uint64_t base = 0; base < nb; base += SCAN_BLOCK) {
-        uint64_t i = base + threadIdx.x;
-        uint64_t v = i < nb ? partials[i] : 0;
-        uint64_t s = block_inclusive_scan(v, ws);
-        if (i < nb) partials[i] = carry + s - v;
-        if (threadIdx.x == SCAN_BLOCK - 1) chunk_total = s;
-        __syncthreads();
-        carry += chunk_total;
-        __syncthreads();
+    for (int c = 0; c < 2; ++c) {
+        uint64_t carry = 0;
+        for (uint64_t base = 0; base < nb; base += SCAN_BLOCK) {
+            uint64_t i = base + threadIdx.x;
+            uint64_t v = i < nb ? partials[2 * i + c] : 0;
+            uint64_t s = block_inclusive_scan(v, ws);
+            if (i < nb) partials[2 * i + c] = carry + s - v;
+            if (threadIdx.x == SCAN_BLOCK - 1) chunk_total = s;
+            __syncthreads();
+            carry += chunk_total;
+            __syncthreads();
+        }
     }
 }
 
 __global__ void __launch_bounds__(SCAN_BLOCK)
 k_prefix_final(const uint64_t* __restrict__ off, uint64_t n, uint32_t K, uint64_t max_bases,
-               const uint64_t* __restrict__ partials, uint64_t* __restrict__ kofs, uint32_t* err) {
-    __shared__ uint64_t ws[32];
+               const uint64_t* __restrict__ partials, uint64_t* __restrict__ kofs,
+               uint64_t* __restrict__ tofs) {
+    __shared__ uint64_t ws[32], wt[32];
     uint64_t r = (uint64_t)blockIdx.x * SCAN_BLOCK + threadIdx.x;
-    (void)err;
-    uint64_t v = r < n ? read_kmers(off, r, K, max_bases, nullptr) : 0;
-    uint64_t s = block_inclusive_scan(v, ws) + partials[blockIdx.x];
+    ulonglong2 v = r < n ? read_counts(off, r, K, max_bases, nullptr) : make_ulonglong2(0, 0);
+    uint64_t s = block_inclusive_scan(v.x, ws) + partials[2 * blockIdx.x];
+    uint64_t t = block_inclusive_scan(v.y, wt) + partials[2 * blockIdx.x + 1];
     if (r < n) {
-        kofs[r] = s - v;
-        if (r == n - 1) kofs[n] = s;
+        kofs[r] = s - v.x;
+        tofs[r] = t - v.y;
+        if (r == n - 1) {
+            kofs[n] = s;
+            tofs[n] = t;
+        }
     }
 }
 
 cudaError_t launch_kmer_prefix(const uint64_t* offsets, uint64_t n_reads, uint32_t K,
                                uint64_t max_bases, uint64_t* partials, uint64_t* kofs,
-                               uint32_t* err, cudaStream_t st, int* launches) {
+                               uint64_t* tofs, uint32_t* err, cudaStream_t st, int* launches) {
     if (n_reads == 0) {
         *launches = 0;
+        cudaMemsetAsync(tofs, 0, sizeof(uint64_t), st);
         return cudaMemsetAsync(kofs, 0, sizeof(uint64_t), st);
     }
     uint64_t nb = (n_reads + SCAN_BLOCK - 1) / SCAN_BLOCK;
@@ -101,8 +120,23 @@ cudaError_t launch_kmer_prefix(const uint64_t* offsets, uint64_t n_reads, uint32
                                                            partials, err);
     k_prefix_partials_scan<<<1, SCAN_BLOCK, 0, st>>>(partials, nb);
     k_prefix_final<<<(unsigned)nb, SCAN_BLOCK, 0, st>>>(offsets, n_reads, K, max_bases, partials,
-                                                        kofs, err);
+                                                        kofs, tofs);
     *launches = 3;
+    return cudaGetLastError();
+}
+
+// task_read[t] = read of warp task t, for t < n_tasks_cap.
+__global__ void k_task_map(const uint64_t* __restrict__ tofs, uint64_t n, uint64_t cap,
+                           uint32_t* __restrict__ task_read) {
+    uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    for (uint64_t t = tofs[r], e = tofs[r + 1]; t < e && t < cap; ++t) task_read[t] = (uint32_t)r;
+}
+
+cudaError_t launch_task_map(const uint64_t* tofs, uint64_t n_reads, uint64_t cap,
+                            uint32_t* task_read, cudaStream_t st) {
+    if (n_reads == 0) return cudaSuccess;
+    k_task_map<<<(unsigned)((n_reads + 255) / 256), 256, 0, st>>>(tofs, n_reads, cap, task_read);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,16 @@ cudaError_t launch_insert_pass(int pass, const LaunchShape& s, uint64_t n_thread
                                const HashParams& hp, const TableParams& tp,
                                const WindowParams& w);
 
+struct PersistParams;
+
+// Persistent cooperative insert of a whole read batch (gdbg_persist.cuh).
+// max_tasks bounds the batch's warp tasks; *grid_used gets the block count.
+template <int STORAGE>
+cudaError_t launch_insert_persistent(const LaunchShape& s, uint64_t max_tasks, cudaStream_t st,
+                                     const BatchView& b, const HashParams& hp,
+                                     const TableParams& tp, const PersistParams& pp,
+                                     int* grid_used);
+
 template <int STORAGE>
 cudaError_t launch_query(const LaunchShape& s, uint64_t n_total, cudaStream_t st,
                          const BatchView& b, const uint64_t* hashes, const HashParams& hp,
@@ -38,10 +48,11 @@ cudaError_t launch_hashes(bool canonical, cudaStream_t st, const BatchView& b,
 // read counts as zero k-mers and sets GDBG_ERR_BAD_OFFSETS in *err.
 cudaError_t launch_kmer_prefix(const uint64_t* offsets, uint64_t n_reads, uint32_t K,
                                uint64_t max_bases, uint64_t* partials, uint64_t* kofs,
-                               uint32_t* err, cudaStream_t st, int* launches);
+                               uint64_t* tofs, uint32_t* err, cudaStream_t st, int* launches);
+// task_read[t] for every warp task t < cap (tasks: 32 k-mers of one read).
+cudaError_t launch_task_map(const uint64_t* tofs, uint64_t n_reads, uint64_t cap,
+                            uint32_t* task_read, cudaStream_t st);
 cudaError_t launch_tile_map(const uint64_t* kofs, uint64_t n_reads, uint64_t n_tiles,
                             uint32_t* tile_read, cudaStream_t st);
-
-constexpr uint32_t GDBG_ERR_BAD_OFFSETS = 8u;
 
 }  // namespace gdbg

@@ -3,6 +3,7 @@
 #pragma once
 #include "gdbg_kernels.cuh"
 #include "gdbg_launch.h"
+#include "gdbg_persist.cuh"
 
 namespace gdbg {
 
@@ -93,6 +94,45 @@ cudaError_t launch_masks(const LaunchShape& s, cudaStream_t st, const BatchView&
               : masks_one<ST, false, 0>(st, b, hp, tp, masks);
 }
 
+template <int ST, bool C, int NT>
+cudaError_t persist_one(uint64_t max_tasks, cudaStream_t st, const BatchView& b,
+                        const HashParams& hp, const TableParams& tp, const PersistParams& pp,
+                        int* grid_used) {
+    static int per_sm = -1, n_sm = 0;
+    auto kern = k_insert_persistent<ST, C, NT>;
+    if (per_sm < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PBLOCK, 0);
+        if (e != cudaSuccess) return e;
+    }
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    uint64_t want = (max_tasks * 32 + PBLOCK - 1) / PBLOCK;
+    uint64_t grid = (uint64_t)per_sm * n_sm;
+    if (want < grid) grid = want ? want : 1;
+    *grid_used = (int)grid;
+    BatchView b_ = b;
+    HashParams hp_ = hp;
+    TableParams tp_ = tp;
+    PersistParams pp_ = pp;
+    void* args[] = {&b_, &hp_, &tp_, &pp_};
+    return cudaLaunchCooperativeKernel((const void*)kern, dim3((unsigned)grid), dim3(PBLOCK), args,
+                                       0, st);
+}
+
+template <int ST>
+cudaError_t launch_insert_persistent(const LaunchShape& s, uint64_t max_tasks, cudaStream_t st,
+                                     const BatchView& b, const HashParams& hp,
+                                     const TableParams& tp, const PersistParams& pp,
+                                     int* grid_used) {
+    const bool t4 = s.n_tables == 4;
+    if (s.canonical) return t4 ? persist_one<ST, true, 4>(max_tasks, st, b, hp, tp, pp, grid_used)
+                               : persist_one<ST, true, 0>(max_tasks, st, b, hp, tp, pp, grid_used);
+    return t4 ? persist_one<ST, false, 4>(max_tasks, st, b, hp, tp, pp, grid_used)
+              : persist_one<ST, false, 0>(max_tasks, st, b, hp, tp, pp, grid_used);
+}
+
 #define GDBG_INSTANTIATE_LAUNCHERS(ST)                                                         \
     template cudaError_t launch_insert_pass<ST>(int, const LaunchShape&, uint64_t, cudaStream_t, \
                                                 const BatchView&, const uint64_t*,             \
@@ -102,6 +142,10 @@ cudaError_t launch_masks(const LaunchShape& s, cudaStream_t st, const BatchView&
                                           const BatchView&, const uint64_t*, const HashParams&, \
                                           const TableParams&, int16_t*, uint64_t*);            \
     template cudaError_t launch_masks<ST>(const LaunchShape&, cudaStream_t, const BatchView&,  \
-                                          const HashParams&, const TableParams&, uint8_t*);
+                                          const HashParams&, const TableParams&, uint8_t*);    \
+    template cudaError_t launch_insert_persistent<ST>(const LaunchShape&, uint64_t, cudaStream_t, \
+                                                      const BatchView&, const HashParams&,    \
+                                                      const TableParams&, const PersistParams&, \
+                                                      int*);
 
 }  // namespace gdbg

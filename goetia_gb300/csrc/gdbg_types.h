@@ -12,7 +12,8 @@ constexpr int MAX_TABLES = 32;
 enum : uint32_t {
     GDBG_ERR_CAS_LIMIT = 1u,      // a saturating compare-and-swap loop hit its cap
     GDBG_ERR_CLAIMS_FULL = 2u,    // the first-touch map overflowed
-    GDBG_ERR_BARRIER_TIMEOUT = 4u // a grid barrier wait hit its cap
+    GDBG_ERR_BARRIER_TIMEOUT = 4u,// a grid barrier wait hit its cap
+    GDBG_ERR_BAD_OFFSETS = 8u     // read offsets decrease or run past the packed stream
 };
 
 struct HashParams {
@@ -36,9 +37,13 @@ struct BatchView {
     uint64_t n_reads;
     uint64_t n_kmers;          // host copy of kofs[n_reads]
     uint64_t n_map_tiles;
+    const uint64_t* tofs;      // n_reads+1 exclusive prefix of per-read warp tasks
+    const uint32_t* task_read; // read of each warp task
+    uint64_t task_cap;         // entries of task_read that are valid to read
 };
 
 constexpr uint64_t MAP_TILE = 1024;  // k-mers per entry of tile_read
+constexpr uint32_t TASK_KMERS = 32;  // k-mers per warp task (one lane each)
 
 // One window of the insert: k-mers [start, end) of the batch.
 struct WindowParams {
@@ -51,6 +56,20 @@ struct WindowParams {
     unsigned long long* n_new;   // per read (may be null)
     unsigned long long* counters;// [0] n_unique, [1] n_occupied
     uint32_t* err;
+};
+
+// Persistent batch insert (gdbg_persist.cuh).
+struct PersistParams {
+    uint32_t window_tasks;        // warp tasks per window (<= 2^15)
+    uint32_t* fresh;              // per window ordinal: zero-cell bits
+    uint32_t* words;              // per window ordinal x table: word seen by the probe
+    uint64_t* claims;
+    uint32_t claims_mask;
+    uint32_t* epoch_state;        // last claims epoch used (device, persists across calls)
+    unsigned long long* n_new;    // per read, may be null
+    unsigned long long* counters; // [0] n_unique, [1] n_occupied
+    uint32_t* err;
+    unsigned int* bar;            // [0] arrivals, [1] generation
 };
 
 }  // namespace gdbg

@@ -532,6 +532,11 @@ class dBGBase:
     def set_insert_schedule(self, window_kmers=0, kmers_per_thread=0):
         _lib.call("gdbg_set_insert_schedule", self._h, int(window_kmers), int(kmers_per_thread))
 
+    def set_insert_path(self, persistent=True):
+        """One persistent cooperative launch per batch, or launches per window."""
+        _lib.call("gdbg_set_insert_path", self._h,
+                  _lib.PATH_PERSISTENT if persistent else _lib.PATH_WINDOWED)
+
     def insert_schedule(self):
         w, k = _lib.c_u32(), _lib.c_u32()
         _lib.call("gdbg_get_insert_schedule", self._h, _c.byref(w), _c.byref(k))

@@ -176,8 +176,15 @@ int gdbg_neighbor_masks_batch_device(gdbg_graph* g, const uint32_t* packed,
 /* ---- tuning and diagnostics ------------------------------------------- */
 
 /* Insert schedule: k-mers per window (<= 2^20; each window is a probe pass
- * then a commit pass) and k-mers per thread (1..16).  0 keeps a value. */
+ * then a commit pass) and k-mers per thread of the windowed path (4 or 8).
+ * 0 keeps a value. */
 int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmers_per_thread);
+/* Read-batch insert implementation: one persistent cooperative launch per
+ * batch (default), or one probe and one commit launch per window.  Both give
+ * identical results. */
+#define GDBG_PATH_PERSISTENT 0
+#define GDBG_PATH_WINDOWED 1
+int gdbg_set_insert_path(gdbg_graph* g, int path);
 int gdbg_get_insert_schedule(const gdbg_graph* g, uint32_t* window_kmers,
                              uint32_t* kmers_per_thread);
 /* Device status word (GDBG_ERR_* device bits); cleared by reading. */

@@ -91,3 +91,29 @@ def test_storage_params_mirror():
     assert s.get_tablesizes() == [4194301, 4194287, 4194277, 4194271]
     assert BitStorage.build().get_tablesizes() == oracle.primes(4, 1_000_000)
     assert ByteStorage.is_counting and NibbleStorage.is_counting and not BitStorage.is_counting
+
+
+def test_cpp_wrapper_compiles_and_links(lib, tmp_path):
+    """include/goetia_gb300.hpp (the reference-signature C++ front end) builds
+    and links against the library (not run: no GPU here)."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = tmp_path / "t.cc"
+    src.write_text(
+        '#include "goetia_gb300.hpp"\n'
+        "using namespace goetia_gb300;\n"
+        "int main() {\n"
+        "  auto g = GpuDBG<ByteStorage, CanLemireShifter>::build(100000, 4, 31);\n"
+        "  uint64_t n_new = 0;\n"
+        '  g->insert_sequence(std::string(40, \'A\'), n_new);\n'
+        '  auto c = g->query_sequence(std::string(40, \'A\'));\n'
+        "  return (int)c.size() + (int)n_new;\n"
+        "}\n")
+    libdir = os.path.join(ROOT, "goetia_gb300")
+    subprocess.check_call([gxx, "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src),
+                           "-o", str(tmp_path / "t"), "-L", libdir, "-l:libgoetia_gb300.so",
+                           "-Wl,-rpath-link,/usr/local/cuda/lib64",
+                           "-L/usr/local/cuda/lib64", "-lcudart"])

@@ -59,12 +59,15 @@ def test_golden_plain_per_read(cuda_ready, name):
 
 @pytest.mark.parametrize("name", names())
 @pytest.mark.parametrize("window,kpt", [(262144, 4), (64, 8), (5, 4)])
-def test_golden_batched(cuda_ready, name, window, kpt):
+@pytest.mark.parametrize("persistent", [True, False])
+def test_golden_batched(cuda_ready, name, window, kpt, persistent):
     """One packed batch; windows smaller than the batch exercise the
-    cross-window first-touch logic."""
+    cross-window first-touch logic (and, at 32 k-mers per window, the claims
+    epoch wrap after 127 windows)."""
     c = Case(name)
     g = graph_for(c.storage, c.canonical, c.K, c.sizes)
     g.set_insert_schedule(window, kpt)
+    g.set_insert_path(persistent)
     packed, off = c.packed()
     pr = G.PackedReads(packed, off)
     n_new = g.insert_packed(pr)
@@ -102,7 +105,8 @@ def _oracle_run(kind, canonical, K, sizes, pr):
     ("nibble", False, 21, 40009),
     ("bit", False, 25, 7919),
 ])
-def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table):
+@pytest.mark.parametrize("persistent", [True, False])
+def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table, persistent):
     """10,000 reads of 150 bp from a 100 kb genome, 1% substitutions."""
     gen = synth.genome(100_000, 1)
     rows = synth.sample_reads(gen, 10_000, 150, 0.01, 2)
@@ -111,6 +115,7 @@ def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table):
     st, n_new_ref = _oracle_run(kind, canonical, K, sizes, pr)
     g = graph_for(kind, canonical, K, sizes)
     g.set_insert_schedule(65536, 4)
+    g.set_insert_path(persistent)
     n_new = g.insert_packed(pr)
     assert np.array_equal(n_new, n_new_ref)
     check_tables(g, st.tables())
@@ -121,12 +126,15 @@ def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table):
 
 
 def test_batches_in_sequence_vs_oracle(cuda_ready):
-    """Several batches into one graph equal one sequential pass."""
+    """Several batches into one graph equal one sequential pass, switching
+    between the two insert paths (they share the claims map epochs)."""
     gen = synth.genome(30_000, 7)
     sizes = oracle.primes(4, 30011)
     st = oracle.Storage("byte", sizes)
     g = graph_for("byte", True, 31, sizes)
-    for b in range(4):
+    g.set_insert_schedule(2048, 4)
+    for b in range(6):
+        g.set_insert_path(b % 3 != 1)
         rows = synth.sample_reads(gen, 700, 150, 0.02, 100 + b)
         pr = synth.rows_to_packed(rows)
         _, ref = st.insert_reads(True, 31, pr.packed, pr.offsets)
