@@ -22,7 +22,7 @@ ERR_UNSUPPORTED = 8
 
 BIT, BYTE, NIBBLE = 0, 1, 2
 FWD_LEMIRE, CAN_LEMIRE = 0, 1
-PATH_PERSISTENT, PATH_WINDOWED = 0, 1
+PATH_PERSISTENT, PATH_WINDOWED, PATH_BUCKETED, PATH_AUTO = 0, 1, 2, 3
 
 c_u64 = ctypes.c_uint64
 c_u32 = ctypes.c_uint32
@@ -70,6 +70,7 @@ SIGNATURES = {
     "gdbg_set_insert_schedule": [c_vp, c_u32, c_u32],
     "gdbg_get_insert_schedule": [c_vp, u32p, u32p],
     "gdbg_set_insert_path": [c_vp, c_int],
+    "gdbg_set_bucket_bits": [c_vp, c_u32],
     "gdbg_device_status": [c_vp, u32p],
     "gdbg_launch_count": [c_vp, u64p],
 }

@@ -101,7 +101,12 @@ struct gdbg_graph {
     uint32_t claims_mask = 0, epoch = 0;
     // persistent insert: device-owned claims epoch and grid-barrier state
     uint32_t pwindow = 262144;
+    int path = GDBG_PATH_AUTO;
     bool persistent = true;
+    // bucketed insert
+    uint32_t bucket_fs = 0;   // 0 = default for the storage kind
+    DevBuf<uint64_t> rec_a, rec_b;
+    DevBuf<uint32_t> hist, hist_off, scan_parts, bstart, new_bits;
     uint32_t* d_epoch = nullptr;
     unsigned int* d_bar = nullptr;
     bool epoch_on_device = false;
@@ -297,6 +302,102 @@ int launch_pass(gdbg_graph* g, int pass, const LaunchShape& s, uint64_t n_thread
     return GDBG_OK;
 }
 
+uint32_t default_bucket_fs(int storage) {
+    // 64 KB of table per bucket
+    return storage == GDBG_BIT ? 19u : storage == GDBG_NIBBLE ? 17u : 16u;
+}
+
+// Can the bucketed path take this batch?  (tables <= 8, every global cell id
+// and every record index below 2^32)
+bool bucket_fits(const gdbg_graph* g, uint64_t n_kmers, uint32_t fs) {
+    const uint64_t n = g->sizes.size();
+    if (n > (uint64_t)BK_MAXNT || n_kmers == 0) return false;
+    if (n_kmers * n >= (1ull << 32)) return false;
+    uint64_t cells = 0;
+    for (auto p : g->sizes) cells += ((p + (1ull << fs) - 1) >> fs) << fs;
+    return cells <= (1ull << 32);
+}
+
+int set_error_launch(cudaError_t e, const char* what) {
+    return fail(GDBG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Bucketed insert of a read batch: partition the (cell, k-mer) records by
+// table region, then apply each region in shared memory.
+int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaStream_t st) {
+    const uint64_t nk = b.n_kmers, n = g->sizes.size();
+    if (nk == 0) {
+        if (n_new && b.n_reads) GDBG_CUDA(cudaMemsetAsync(n_new, 0, b.n_reads * sizeof(uint64_t), st));
+        return GDBG_OK;
+    }
+    const uint32_t fs = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
+    BucketParams bp{};
+    bp.fs = fs;
+    uint32_t nb = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        bp.bbase[i] = nb;
+        bp.tbase[i] = (uint64_t)nb << fs;
+        bp.twords[i] = (uint32_t)g->words[i];
+        nb += (uint32_t)((g->sizes[i] + (1ull << fs) - 1) >> fs);
+    }
+    bp.bbase[n] = nb;
+    bp.n_buckets = nb;
+    bp.n_tables = (uint32_t)n;
+    bp.total_kmers = b.kofs + b.n_reads;
+    const uint64_t nrec = nk * n;
+    bp.n_recs = nrec;
+    bp.kmer_cap = nk;
+    uint32_t bits = 0;
+    while ((1ull << bits) < nb) ++bits;
+    const uint32_t passes = bits <= 8 ? 1u : (bits + 7) / 8;
+
+    const uint64_t tile_recs = bucket_tile_records();
+    const uint64_t tiles = (nrec + tile_recs - 1) / tile_recs;
+    const uint64_t hmax = 256 * tiles;
+    GDBG_TRY(g->rec_a.ensure(nrec));
+    GDBG_TRY(g->rec_b.ensure(nrec));
+    GDBG_TRY(g->hist.ensure(hmax));
+    GDBG_TRY(g->hist_off.ensure(hmax));
+    GDBG_TRY(g->scan_parts.ensure(scan32_partials_needed(hmax) + 1));
+    GDBG_TRY(g->bstart.ensure(nb + 1));
+    GDBG_TRY(g->new_bits.ensure(nk / 32 + 2));
+    GDBG_CUDA(cudaMemsetAsync(g->new_bits.p, 0, (nk / 32 + 2) * sizeof(uint32_t), st));
+    GDBG_CUDA(cudaMemsetAsync(g->bstart.p, 0xFF, (nb + 1) * sizeof(uint32_t), st));
+    const bool canon = g->shifter == GDBG_CAN_LEMIRE;
+    cudaError_t e;
+    bp.rout = g->rec_a.p;
+    if ((e = launch_bucket_emit(canon, st, b, g->hp, g->tp, bp)) != cudaSuccess)
+        return set_error_launch(e, "bucket emit");
+    uint64_t* src = g->rec_a.p;
+    uint64_t* dst = g->rec_b.p;
+    bp.n_tiles = (uint32_t)tiles;
+    bp.hist = g->hist.p;
+    bp.offsets = g->hist_off.p;
+    for (uint32_t pass = 0; pass < passes; ++pass) {
+        bp.shift = 8 * pass;
+        bp.rin = src;
+        bp.rout = dst;
+        if ((e = launch_bucket_hist((uint32_t)tiles, st, bp)) != cudaSuccess)
+            return set_error_launch(e, "bucket histogram");
+        if ((e = launch_scan32(g->hist.p, g->hist_off.p, hmax, g->scan_parts.p, st)) != cudaSuccess)
+            return set_error_launch(e, "bucket scan");
+        if ((e = launch_bucket_scatter(pass + 1 == passes, (uint32_t)tiles, st, bp, g->bstart.p)) != cudaSuccess)
+            return set_error_launch(e, "bucket scatter");
+        std::swap(src, dst);
+        g->launches += 5;   // histogram, 3 scan kernels, scatter
+    }
+    if ((e = launch_bucket_starts_fix(st, bp, g->bstart.p)) != cudaSuccess)
+        return set_error_launch(e, "bucket starts");
+    g->launches += 2;
+    if ((e = launch_bucket_apply(g->storage, g->tp, bp, src, g->bstart.p, g->new_bits.p,
+                                 g->d_counters, st)) != cudaSuccess)
+        return set_error_launch(e, "bucket apply");
+    if ((e = launch_bucket_read_new(b.kofs, b.n_reads, g->new_bits.p, n_new, g->d_counters, st)) != cudaSuccess)
+        return set_error_launch(e, "bucket read counts");
+    g->launches += 3;
+    return GDBG_OK;
+}
+
 // Persistent cooperative insert of a read batch (one launch per batch).
 int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaStream_t st) {
     if (b.n_kmers == 0 || b.task_cap == 0) return GDBG_OK;
@@ -348,7 +449,17 @@ int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cu
 int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64_t n_total,
                uint64_t* n_new, cudaStream_t st) {
     if (n_total == 0) return GDBG_OK;
-    if (!hashes && g->persistent) return run_insert_persistent(g, b, n_new, st);
+    if (!hashes) {
+        const uint32_t fs = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
+        uint64_t table_bytes = 0;
+        for (auto w : g->words) table_bytes += 4 * w;
+        const bool fits = bucket_fits(g, n_total, fs);
+        if (g->path == GDBG_PATH_BUCKETED && fits) return run_insert_bucketed(g, b, n_new, st);
+        if (g->path == GDBG_PATH_AUTO && fits && table_bytes >= (256ull << 20) &&
+            n_total >= (1ull << 22))
+            return run_insert_bucketed(g, b, n_new, st);
+        if (g->path != GDBG_PATH_WINDOWED) return run_insert_persistent(g, b, n_new, st);
+    }
     GDBG_TRY(ensure_insert_scratch(g, st));
     if (g->epoch_on_device) {
         // the device owns the epoch counter: start the host-driven windows
@@ -544,6 +655,8 @@ int gdbg_destroy(gdbg_graph* g) {
     g->fresh.release(); g->words_seen.release(); g->claims.release();
     g->kofs.release(); g->tofs.release(); g->partials.release(); g->tile_read.release();
     g->task_read.release();
+    g->rec_a.release(); g->rec_b.release(); g->hist.release(); g->hist_off.release();
+    g->scan_parts.release(); g->bstart.release(); g->new_bits.release();
     g->st_packed.release(); g->st_offsets.release(); g->st_out64.release();
     g->st_out64b.release(); g->st_out64c.release(); g->st_counts.release(); g->st_u8.release();
     if (g->own_stream) cudaStreamDestroy(g->own_stream);
@@ -559,6 +672,8 @@ int gdbg_clone(const gdbg_graph* g, gdbg_graph** out) {
     (*out)->kpt = g->kpt;
     (*out)->pwindow = g->pwindow;
     (*out)->persistent = g->persistent;
+    (*out)->path = g->path;
+    (*out)->bucket_fs = g->bucket_fs;
     return GDBG_OK;
 }
 
@@ -912,9 +1027,23 @@ int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmer
 
 int gdbg_set_insert_path(gdbg_graph* g, int path) {
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
-    if (path != GDBG_PATH_PERSISTENT && path != GDBG_PATH_WINDOWED)
+    if (path < GDBG_PATH_PERSISTENT || path > GDBG_PATH_AUTO)
         return fail(GDBG_ERR_INVALID_ARG, "unknown insert path");
-    g->persistent = path == GDBG_PATH_PERSISTENT;
+    g->path = path;
+    return GDBG_OK;
+}
+
+int gdbg_set_bucket_bits(gdbg_graph* g, uint32_t log2_cells) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    const uint32_t min_fs = g->storage == GDBG_BIT ? 5u : g->storage == GDBG_NIBBLE ? 3u : 2u;
+    if (log2_cells && (log2_cells < min_fs || log2_cells > 20))
+        return fail(GDBG_ERR_INVALID_ARG, "bucket size must be 2^k cells, one word <= 2^k <= 2^20");
+    if (log2_cells) {
+        const uint32_t cpw = g->storage == GDBG_BIT ? 32u : g->storage == GDBG_NIBBLE ? 8u : 4u;
+        const uint64_t smem = ((1ull << log2_cells) / cpw) * 4 + 2 * BK_MAP * 4;
+        if (smem > 200 * 1024) return fail(GDBG_ERR_INVALID_ARG, "bucket does not fit shared memory");
+    }
+    g->bucket_fs = log2_cells;
     return GDBG_OK;
 }
 

@@ -1,0 +1,169 @@
+// Launchers for the bucketed insert path (kernels in gdbg_bucket.cuh).
+#include "gdbg_bucket.cuh"
+#include "gdbg_launch.h"
+
+namespace gdbg {
+
+cudaError_t launch_bucket_emit(bool canonical, cudaStream_t st, const BatchView& b,
+                               const HashParams& hp, const TableParams& tp, const BucketParams& bp) {
+    const uint64_t warps = b.task_cap;
+    uint64_t grid = (warps * 32 + BK_EMIT_BLOCK - 1) / BK_EMIT_BLOCK;
+    if (grid > 152 * 64) grid = 152 * 64;
+    if (grid == 0) return cudaSuccess;
+    if (canonical) k_bkt_emit<true><<<(unsigned)grid, BK_EMIT_BLOCK, 0, st>>>(b, hp, tp, bp);
+    else k_bkt_emit<false><<<(unsigned)grid, BK_EMIT_BLOCK, 0, st>>>(b, hp, tp, bp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_hist(uint32_t n_tiles, cudaStream_t st, const BucketParams& bp) {
+    if (n_tiles == 0) return cudaSuccess;
+    k_bkt_hist<<<n_tiles, BK_TB, 0, st>>>(bp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_scatter(bool last, uint32_t n_tiles, cudaStream_t st,
+                                  const BucketParams& bp, uint32_t* start) {
+    if (n_tiles == 0) return cudaSuccess;
+    const size_t smem = bk_scatter_smem();
+    cudaError_t e;
+    if (last) {
+        e = cudaFuncSetAttribute(k_bkt_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_bkt_scatter<true><<<n_tiles, BK_TB, smem, st>>>(bp, start);
+    } else {
+        e = cudaFuncSetAttribute(k_bkt_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_bkt_scatter<false><<<n_tiles, BK_TB, smem, st>>>(bp, start);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_starts_fix(cudaStream_t st, const BucketParams& bp, uint32_t* start) {
+    k_bkt_starts_fix<<<1, 1024, 0, st>>>(bp, start);
+    return cudaGetLastError();
+}
+
+uint64_t bucket_tile_records() { return BK_TILE; }
+
+template <int ST>
+static cudaError_t apply_one(const TableParams& tp, const BucketParams& bp, const uint64_t* recs,
+                             const uint32_t* start, uint32_t* new_bits,
+                             unsigned long long* counters, cudaStream_t st) {
+    const size_t smem = ((size_t)(1u << bp.fs) / cells_per_word<ST>()) * 4 + 2 * BK_MAP * 4;
+    cudaError_t e = cudaFuncSetAttribute(k_bkt_apply<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_bkt_apply<ST><<<bp.n_buckets, BK_BLOCK, smem, st>>>(tp, bp, recs, start, new_bits, counters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_apply(int storage, const TableParams& tp, const BucketParams& bp,
+                                const uint64_t* recs, const uint32_t* start, uint32_t* new_bits,
+                                unsigned long long* counters, cudaStream_t st) {
+    if (bp.n_buckets == 0) return cudaSuccess;
+    switch (storage) {
+    case GDBG_BIT: return apply_one<GDBG_BIT>(tp, bp, recs, start, new_bits, counters, st);
+    case GDBG_BYTE: return apply_one<GDBG_BYTE>(tp, bp, recs, start, new_bits, counters, st);
+    default: return apply_one<GDBG_NIBBLE>(tp, bp, recs, start, new_bits, counters, st);
+    }
+}
+
+cudaError_t launch_bucket_read_new(const uint64_t* kofs, uint64_t n_reads, const uint32_t* new_bits,
+                                   uint64_t* n_new, unsigned long long* counters, cudaStream_t st) {
+    if (n_reads == 0) return cudaSuccess;
+    k_bkt_read_new<<<(unsigned)((n_reads + 255) / 256), 256, 0, st>>>(
+        kofs, n_reads, new_bits, (unsigned long long*)n_new, counters);
+    return cudaGetLastError();
+}
+
+// ---- exclusive scan of uint32 (histograms) --------------------------------
+constexpr int SCAN32_BLOCK = 1024;
+constexpr int SCAN32_ITEMS = 4;   // per thread
+
+__device__ __forceinline__ uint32_t block_scan32(uint32_t v, uint32_t* ws) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) ws[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t s = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xFFFFFFFFu, s, o);
+            if (lane >= o) s += t;
+        }
+        ws[lane] = s;
+    }
+    __syncthreads();
+    if (wid > 0) v += ws[wid - 1];
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(SCAN32_BLOCK)
+k_scan32_partials(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ partials) {
+    __shared__ uint32_t ws[32];
+    const uint64_t base = ((uint64_t)blockIdx.x * SCAN32_BLOCK + threadIdx.x) * SCAN32_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN32_ITEMS; ++j)
+        if (base + j < n) s += in[base + j];
+    s = block_scan32(s, ws);
+    if (threadIdx.x == SCAN32_BLOCK - 1) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(SCAN32_BLOCK)
+k_scan32_partials_scan(uint32_t* __restrict__ partials, uint64_t nb) {
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t chunk_total;
+    uint32_t carry = 0;
+    for (uint64_t base = 0; base < nb; base += SCAN32_BLOCK) {
+        const uint64_t i = base + threadIdx.x;
+        const uint32_t v = i < nb ? partials[i] : 0;
+        const uint32_t s = block_scan32(v, ws);
+        if (i < nb) partials[i] = carry + s - v;
+        if (threadIdx.x == SCAN32_BLOCK - 1) chunk_total = s;
+        __syncthreads();
+        carry += chunk_total;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(SCAN32_BLOCK)
+k_scan32_final(const uint32_t* __restrict__ in, uint64_t n, const uint32_t* __restrict__ partials,
+               uint32_t* __restrict__ out) {
+    __shared__ uint32_t ws[32];
+    const uint64_t base = ((uint64_t)blockIdx.x * SCAN32_BLOCK + threadIdx.x) * SCAN32_ITEMS;
+    uint32_t v[SCAN32_ITEMS], s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN32_ITEMS; ++j) {
+        v[j] = base + j < n ? in[base + j] : 0;
+        s += v[j];
+    }
+    uint32_t run = block_scan32(s, ws) - s + partials[blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < SCAN32_ITEMS; ++j) {
+        if (base + j < n) out[base + j] = run;
+        run += v[j];
+    }
+}
+
+uint64_t scan32_partials_needed(uint64_t n) {
+    return (n + SCAN32_BLOCK * SCAN32_ITEMS - 1) / (SCAN32_BLOCK * SCAN32_ITEMS) + 1;
+}
+
+cudaError_t launch_scan32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* partials,
+                          cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    const uint64_t nb = (n + SCAN32_BLOCK * SCAN32_ITEMS - 1) / (SCAN32_BLOCK * SCAN32_ITEMS);
+    k_scan32_partials<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials);
+    k_scan32_partials_scan<<<1, SCAN32_BLOCK, 0, st>>>(partials, nb);
+    k_scan32_final<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials, out);
+    return cudaGetLastError();
+}
+
+}  // namespace gdbg

@@ -1,0 +1,425 @@
+// Bucketed insert for large batches on large tables.
+//
+// The per-k-mer insert touches 4 random table sectors per k-mer; once the
+// tables are far larger than L2 every touch is a DRAM round trip and the DRAM
+// traffic per k-mer is several times the algorithmic 256 bytes.  This path
+// turns the batch's random updates into streams:
+//
+//   1. every k-mer g yields one record per table: (global cell id << 32) | g,
+//      where the global cell id places table i at a base aligned to the
+//      bucket size, and bucket = global cell id >> fs;
+//   2. the records are stably partitioned by bucket with 8-bit digit passes
+//      (per-warp histograms, bin-major scan, per-warp ranked scatter), so
+//      inside a bucket they stay in ascending g;
+//   3. one CTA per bucket loads the bucket's slice of its table into shared
+//      memory, applies the records in chunks of the block size in g order and
+//      writes the slice back.  Within a chunk, a k-mer is new on this table
+//      when the cell is zero and no earlier record of the chunk touches the
+//      same cell (a shared-memory min map); earlier chunks are already
+//      applied.  That is the reference's sequential rule (bitstorage.hh:
+//      195-219, bytestorage.cc:60-113, nibblestorage.cc:60-100) cell by cell;
+//   4. new flags land in a per-k-mer bitmask; per-read counts are popcounts.
+#pragma once
+#include "gdbg_persist.cuh"
+
+namespace gdbg {
+
+// Records actually produced by the k-mer pass (device-side count, bounded by
+// the host's allocation).
+__device__ __forceinline__ uint64_t bk_records(const BucketParams& bp) {
+    const uint64_t r = __ldg(bp.total_kmers) * bp.n_tables;
+    return r < bp.n_recs ? r : bp.n_recs;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Lanes of the warp holding the same 8-bit digit (valid lanes only): one
+// ballot per digit bit (warp multi-split).
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d, bool valid) {
+    uint32_t m = __ballot_sync(0xFFFFFFFFu, valid);
+#pragma unroll
+    for (int bit = 0; bit < 8; ++bit) {
+        const uint32_t vb = __ballot_sync(0xFFFFFFFFu, (d >> bit) & 1u);
+        m &= ((d >> bit) & 1u) ? vb : ~vb;
+    }
+    return m;
+}
+
+// Add this warp's digits to its private histogram row.
+__device__ __forceinline__ void warp_count(uint32_t* row, uint32_t d, bool valid) {
+    const uint32_t peers = digit_peers(d, valid);
+    if (valid && (peers & lanemask_lt()) == 0) row[d] += __popc(peers);
+    __syncwarp();
+}
+
+// Position of this lane's record in the warp's running bin cursor, then
+// advance the cursor by the group size.
+__device__ __forceinline__ uint32_t warp_rank(uint32_t* row, uint32_t d, bool valid) {
+    const uint32_t peers = digit_peers(d, valid);
+    uint32_t pos = 0;
+    if (valid) pos = row[d] + __popc(peers & lanemask_lt());
+    __syncwarp();
+    if (valid && (peers & lanemask_lt()) == 0) row[d] += __popc(peers);
+    __syncwarp();
+    return pos;
+}
+
+constexpr int BK_TB = 512;                    // threads per CTA, partition kernels
+constexpr int BK_TW = BK_TB / 32;
+constexpr int BK_IPT = 8;                     // records per thread per tile
+constexpr int BK_TILE = BK_TB * BK_IPT;       // records per tile
+constexpr int BK_EMIT_BLOCK = 256;
+
+__device__ __forceinline__ uint32_t rec_digit(uint64_t rec, const BucketParams& bp) {
+    return (((uint32_t)(rec >> 32) >> bp.fs) >> bp.shift) & 255u;
+}
+__device__ __forceinline__ uint32_t rec_bucket(uint64_t rec, uint32_t fs) {
+    return (uint32_t)(rec >> 32) >> fs;
+}
+
+// Records in k-mer order: R0[g * n + i] = (global cell of table i << 32) | g.
+// Each warp stages its task's records in shared memory and writes them as one
+// contiguous run.
+template <bool CANON>
+__global__ void __launch_bounds__(BK_EMIT_BLOCK)
+k_bkt_emit(BatchView b, HashParams hp, TableParams tp, BucketParams bp) {
+    __shared__ uint64_t stage[BK_EMIT_BLOCK / 32][32 * BK_MAXNT];
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint64_t n_tasks = __ldg(b.tofs + b.n_reads);
+    if (n_tasks > b.task_cap) n_tasks = b.task_cap;
+    const uint32_t n = (uint32_t)tp.n;
+    const uint64_t warp0 = ((uint64_t)blockIdx.x * BK_EMIT_BLOCK + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * BK_EMIT_BLOCK) >> 5;
+    for (uint64_t t = warp0; t < n_tasks; t += n_warps) {
+        const TaskInfo ti = task_info(b, t, lane);
+        uint64_t fw, rc;
+        task_hash<CANON>(b.packed, ti.b0, hp, ti.valid, lane, fw, rc);
+        const uint32_t cnt = __popc(__ballot_sync(0xFFFFFFFFu, ti.valid));
+        if (ti.valid) {
+            const uint64_t h = hash_value<CANON>(fw, rc);
+#pragma unroll
+            for (int i = 0; i < BK_MAXNT; ++i) {
+                if (i < (int)n) {
+                    const uint64_t c = fastmod(h, tp.p[i], tp.m[i]);
+                    stage[w][lane * n + i] = ((bp.tbase[i] + c) << 32) | (uint32_t)ti.g;
+                }
+            }
+        }
+        __syncwarp();
+        const uint64_t g0 = __shfl_sync(0xFFFFFFFFu, ti.g, 0);
+        uint64_t* dst = bp.rout + g0 * n;
+        for (uint32_t k = lane; k < cnt * n; k += 32) dst[k] = stage[w][k];
+        __syncwarp();
+    }
+}
+
+// Per-tile digit histogram, bin-major: hist[bin * n_tiles + tile].
+__global__ void __launch_bounds__(BK_TB, 3)
+k_bkt_hist(BucketParams bp) {
+    __shared__ uint32_t cnt[256];
+    for (int k = threadIdx.x; k < 256; k += BK_TB) cnt[k] = 0;
+    __syncthreads();
+    const uint64_t n_recs = bk_records(bp);
+    const uint64_t base = (uint64_t)blockIdx.x * BK_TILE;
+    uint64_t rec[BK_IPT];
+#pragma unroll
+    for (int j = 0; j < BK_IPT; ++j) {
+        const uint64_t k = base + (uint64_t)j * BK_TB + threadIdx.x;
+        rec[j] = k < n_recs ? __ldcs(bp.rin + k) : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < BK_IPT; ++j) {
+        const uint64_t k = base + (uint64_t)j * BK_TB + threadIdx.x;
+        if (k < n_recs) atomicAdd(cnt + rec_digit(rec[j], bp), 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 256; k += BK_TB)
+        bp.hist[(uint64_t)k * bp.n_tiles + blockIdx.x] = cnt[k];
+}
+
+// Exclusive scan of 256 values in shared memory by the first 256 threads
+// (8 warps); all threads must call.
+__device__ __forceinline__ void scan256(const uint32_t* in, uint32_t* out, uint32_t* wsum) {
+    const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
+    uint32_t v = 0, s = 0;
+    if (t < 256) {
+        v = in[t];
+        s = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane == 31) wsum[w] = s;
+    }
+    __syncthreads();
+    if (t < 256) {
+        uint32_t add = 0;
+        for (uint32_t k = 0; k < w; ++k) add += wsum[k];
+        out[t] = add + s - v;
+    }
+    __syncthreads();
+}
+
+// Stable scatter of one tile by digit: rank in shared memory (per-warp
+// histograms keep warp order), then write each bin's run contiguously.  The
+// last pass also records, per bucket, the smallest output position of its
+// records (start[], pre-filled with 0xFFFFFFFF).
+template <bool LAST>
+__global__ void __launch_bounds__(BK_TB, 3)
+k_bkt_scatter(BucketParams bp, uint32_t* __restrict__ start) {
+    extern __shared__ uint64_t sh[];
+    uint64_t* stage = sh;                                           // BK_TILE
+    uint32_t(*whist)[256] = (uint32_t(*)[256])(sh + BK_TILE);       // BK_TW x 256
+    uint32_t* bin_cnt = (uint32_t*)(sh + BK_TILE) + BK_TW * 256;
+    uint32_t* bin_local = bin_cnt + 256;
+    uint32_t* bin_global = bin_local + 256;
+    uint32_t* wsum = bin_global + 256;
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = lane; k < 256; k += 32) whist[w][k] = 0;
+    __syncwarp();
+    const uint64_t n_recs = bk_records(bp);
+    const uint64_t tile_base = (uint64_t)blockIdx.x * BK_TILE;
+    const uint64_t wbase = tile_base + (uint64_t)w * 32 * BK_IPT;
+    uint64_t rec[BK_IPT];
+#pragma unroll
+    for (int j = 0; j < BK_IPT; ++j) {
+        const uint64_t k = wbase + (uint64_t)j * 32 + lane;
+        rec[j] = k < n_recs ? __ldcs(bp.rin + k) : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < BK_IPT; ++j) {
+        const uint64_t k = wbase + (uint64_t)j * 32 + lane;
+        warp_count(whist[w], rec_digit(rec[j], bp), k < n_recs);
+    }
+    __syncthreads();
+    if (threadIdx.x < 256) {
+        const uint32_t bin = threadIdx.x;
+        uint32_t run = 0;
+        for (int ww = 0; ww < BK_TW; ++ww) {
+            const uint32_t c = whist[ww][bin];
+            whist[ww][bin] = run;
+            run += c;
+        }
+        bin_cnt[bin] = run;
+        bin_global[bin] = bp.offsets[(uint64_t)bin * bp.n_tiles + blockIdx.x];
+    }
+    __syncthreads();
+    scan256(bin_cnt, bin_local, wsum);
+#pragma unroll
+    for (int j = 0; j < BK_IPT; ++j) {
+        const uint64_t k = wbase + (uint64_t)j * 32 + lane;
+        const bool v = k < n_recs;
+        const uint32_t d = rec_digit(rec[j], bp);
+        const uint32_t pos = warp_rank(whist[w], d, v);
+        if (v) stage[bin_local[d] + pos] = rec[j];
+    }
+    __syncthreads();
+    const uint64_t left = n_recs > tile_base ? n_recs - tile_base : 0;
+    const uint32_t n_tile = left < (uint64_t)BK_TILE ? (uint32_t)left : (uint32_t)BK_TILE;
+    for (uint32_t k = threadIdx.x; k < n_tile; k += BK_TB) {
+        const uint64_t r = stage[k];
+        const uint32_t d = rec_digit(r, bp);
+        const uint32_t gpos = bin_global[d] + (k - bin_local[d]);
+        bp.rout[gpos] = r;
+        if (LAST) {
+            const uint32_t bk = rec_bucket(r, bp.fs);
+            if (k == 0 || rec_bucket(stage[k - 1], bp.fs) != bk) atomicMin(start + bk, gpos);
+        }
+    }
+}
+
+constexpr size_t bk_scatter_smem() {
+    return (size_t)BK_TILE * 8 + (size_t)BK_TW * 256 * 4 + 3 * 256 * 4 + 8 * 4;
+}
+
+// start[n_buckets] = record count; empty buckets take the next bucket's start.
+__global__ void __launch_bounds__(1024)
+k_bkt_starts_fix(BucketParams bp, uint32_t* __restrict__ start) {
+    __shared__ uint32_t carry_s;
+    const uint32_t nb = bp.n_buckets;
+    if (threadIdx.x == 0) {
+        start[nb] = (uint32_t)bk_records(bp);
+        carry_s = start[nb];
+    }
+    __syncthreads();
+    // reverse inclusive min-scan, 1024 entries at a time from the end
+    for (int64_t hi = (int64_t)nb - 1; hi >= 0; hi -= 1024) {
+        const int64_t i = hi - threadIdx.x;
+        uint32_t v = i >= 0 ? start[i] : 0xFFFFFFFFu;
+        const uint32_t lane = threadIdx.x & 31;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+            if (lane >= o) v = min(v, y);
+        }
+        __shared__ uint32_t wmin[32];
+        if (lane == 31) wmin[threadIdx.x >> 5] = v;
+        __syncthreads();
+        uint32_t pre = carry_s;
+        for (uint32_t k = 0; k < (threadIdx.x >> 5); ++k) pre = min(pre, wmin[k]);
+        v = min(v, pre);
+        if (i >= 0) start[i] = v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry_s = v;
+        __syncthreads();
+    }
+}
+
+// Region-relative cell address in shared memory words.
+template <int STORAGE>
+__device__ __forceinline__ void region_cell(uint32_t co, uint32_t& word, uint32_t& shift) {
+    if (STORAGE == GDBG_BIT) {
+        word = co >> 5;
+        shift = co & 31u;
+    } else if (STORAGE == GDBG_BYTE) {
+        word = co >> 2;
+        shift = (co & 3u) << 3;
+    } else {
+        const uint32_t byte = co >> 1;
+        word = byte >> 2;
+        shift = ((byte & 3u) << 3) + ((co & 1u) ? 0u : 4u);
+    }
+}
+
+template <int STORAGE>
+__host__ __device__ constexpr uint32_t cells_per_word() {
+    return STORAGE == GDBG_BIT ? 32u : STORAGE == GDBG_BYTE ? 4u : 8u;
+}
+
+// One CTA per bucket.  Dynamic shared memory: the bucket's table words, then
+// the chunk map (keys, then minimum chunk ranks).
+template <int STORAGE>
+__global__ void __launch_bounds__(BK_BLOCK)
+k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
+            const uint32_t* __restrict__ start, uint32_t* __restrict__ new_bits,
+            unsigned long long* counters) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t bk = blockIdx.x;
+    const uint32_t rs = start[bk], re = start[bk + 1];
+    if (rs == re) return;
+    int ti = 0;
+    while (ti + 1 < tp.n && bp.bbase[ti + 1] <= bk) ++ti;
+    const uint32_t region_cells = 1u << bp.fs;
+    const uint32_t region_words = region_cells / cells_per_word<STORAGE>();
+    const uint64_t c0 = (uint64_t)(bk - bp.bbase[ti]) << bp.fs;
+    const uint64_t w0 = c0 / cells_per_word<STORAGE>();
+    uint32_t nw = region_words;
+    if (w0 + nw > bp.twords[ti]) nw = (uint32_t)(bp.twords[ti] - w0);
+    uint32_t* region = smem;
+    uint32_t* mkey = smem + region_words;
+    uint32_t* mval = mkey + BK_MAP;
+    const uint32_t* gsrc = tp.words[ti] + w0;
+    const bool vec = ((w0 & 3u) == 0) && ((nw & 3u) == 0);
+    if (vec) {
+        const uint4* s4 = reinterpret_cast<const uint4*>(gsrc);
+        uint4* d4 = reinterpret_cast<uint4*>(region);
+        const uint32_t n4 = nw >> 2;
+        constexpr int V = 4;   // loads in flight per thread
+        for (uint32_t k0 = threadIdx.x; k0 < n4; k0 += BK_BLOCK * V) {
+            uint4 v[V];
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+                if (k0 + j * BK_BLOCK < n4) v[j] = __ldcs(s4 + k0 + j * BK_BLOCK);
+#pragma unroll
+            for (int j = 0; j < V; ++j)
+                if (k0 + j * BK_BLOCK < n4) d4[k0 + j * BK_BLOCK] = v[j];
+        }
+    } else {
+        for (uint32_t k = threadIdx.x; k < nw; k += BK_BLOCK) region[k] = __ldcs(gsrc + k);
+    }
+    for (uint32_t k = threadIdx.x; k < BK_MAP; k += BK_BLOCK) mkey[k] = 0;
+    __syncthreads();
+    const uint32_t co_mask = region_cells - 1;
+    unsigned long long occ = 0;
+    uint64_t next = rs + threadIdx.x < re ? __ldcs(recs + rs + threadIdx.x) : 0;
+    for (uint32_t base = rs; base < re; base += BK_BLOCK) {
+        const uint32_t k = base + threadIdx.x;
+        const bool active = k < re;
+        const uint64_t r = next;
+        if (k + BK_BLOCK < re) next = __ldcs(recs + k + BK_BLOCK);
+        uint32_t co = 0, g = 0, word = 0, shift = 0, slot = 0;
+        bool fresh = false;
+        if (active) {
+            co = (uint32_t)(r >> 32) & co_mask;
+            g = (uint32_t)r;
+            region_cell<STORAGE>(co, word, shift);
+            fresh = cell_value<STORAGE>(region[word], shift) == 0;
+        }
+        if (fresh) {
+            // claim the smallest chunk rank for this cell (rank order = g order)
+            slot = (co * 0x9E3779B1u) >> (32 - 11);
+            for (int it = 0; it < BK_MAP; ++it) {
+                const uint32_t prev = atomicCAS(mkey + slot, 0u, co + 1u);
+                if (prev == 0u) {
+                    mval[slot] = threadIdx.x;   // first writer; the min is taken below
+                    break;
+                }
+                if (prev == co + 1u) break;
+                slot = (slot + 1) & (BK_MAP - 1);
+            }
+        }
+        __syncthreads();
+        if (fresh) atomicMin(mval + slot, threadIdx.x);
+        __syncthreads();
+        const bool isnew = fresh && mval[slot] == threadIdx.x;
+        if (active) {
+            if (STORAGE == GDBG_BIT) {
+                if (fresh) atomicOr(region + word, 1u << shift);
+            } else {
+                uint32_t cur = region[word];
+                for (int it = 0; it < BK_BLOCK + 1; ++it) {
+                    if (cell_value<STORAGE>(cur, shift) >= cell_max<STORAGE>()) break;
+                    const uint32_t prev = atomicCAS(region + word, cur, cur + (1u << shift));
+                    if (prev == cur) break;
+                    cur = prev;
+                }
+            }
+        }
+        if (isnew && g < bp.kmer_cap) {
+            atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
+            if (ti == 0) ++occ;
+        }
+        __syncthreads();
+        if (fresh) mkey[slot] = 0;
+        __syncthreads();
+    }
+    uint32_t* gdst = tp.words[ti] + w0;
+    if (vec) {
+        uint4* g4 = reinterpret_cast<uint4*>(gdst);
+        const uint4* s4 = reinterpret_cast<const uint4*>(region);
+        for (uint32_t k = threadIdx.x; k < (nw >> 2); k += BK_BLOCK) g4[k] = s4[k];
+    } else {
+        for (uint32_t k = threadIdx.x; k < nw; k += BK_BLOCK) gdst[k] = region[k];
+    }
+    occ = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)occ);
+    if ((threadIdx.x & 31) == 0 && occ) atomicAdd(counters + 1, occ);
+}
+
+// Per-read new counts from the new-k-mer bitmask, plus the batch total.
+__global__ void k_bkt_read_new(const uint64_t* __restrict__ kofs, uint64_t n_reads,
+                               const uint32_t* __restrict__ new_bits,
+                               unsigned long long* __restrict__ n_new,
+                               unsigned long long* counters) {
+    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t cnt = 0;
+    if (r < n_reads) {
+        const uint64_t a = kofs[r], e = kofs[r + 1];
+        for (uint64_t wd = a >> 5; (wd << 5) < e; ++wd) {
+            uint32_t v = __ldg(new_bits + wd);
+            const uint64_t lo = wd << 5;
+            if (a > lo) v &= ~0u << (a - lo);
+            if (e < lo + 32) v &= (1u << (e - lo)) - 1u;
+            cnt += __popc(v);
+        }
+        if (n_new) n_new[r] = cnt;
+    }
+    const uint32_t s = __reduce_add_sync(0xFFFFFFFFu, cnt);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(counters + 0, (unsigned long long)s);
+}
+
+}  // namespace gdbg

@@ -43,6 +43,24 @@ cudaError_t launch_masks(const LaunchShape& s, cudaStream_t st, const BatchView&
 cudaError_t launch_hashes(bool canonical, cudaStream_t st, const BatchView& b,
                           const HashParams& hp, uint64_t* values, uint64_t* fw, uint64_t* rc);
 
+// Bucketed insert (gdbg_bucket.cu / gdbg_bucket.cuh).
+struct BucketParams;
+cudaError_t launch_bucket_emit(bool canonical, cudaStream_t st, const BatchView& b,
+                               const HashParams& hp, const TableParams& tp, const BucketParams& bp);
+cudaError_t launch_bucket_hist(uint32_t n_tiles, cudaStream_t st, const BucketParams& bp);
+cudaError_t launch_bucket_scatter(bool last, uint32_t n_tiles, cudaStream_t st,
+                                  const BucketParams& bp, uint32_t* start);
+cudaError_t launch_bucket_starts_fix(cudaStream_t st, const BucketParams& bp, uint32_t* start);
+uint64_t bucket_tile_records();
+cudaError_t launch_bucket_apply(int storage, const TableParams& tp, const BucketParams& bp,
+                                const uint64_t* recs, const uint32_t* start, uint32_t* new_bits,
+                                unsigned long long* counters, cudaStream_t st);
+cudaError_t launch_bucket_read_new(const uint64_t* kofs, uint64_t n_reads, const uint32_t* new_bits,
+                                   uint64_t* n_new, unsigned long long* counters, cudaStream_t st);
+uint64_t scan32_partials_needed(uint64_t n);
+cudaError_t launch_scan32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* partials,
+                          cudaStream_t st);
+
 // Batch preparation (gdbg_batch.cu): per-read k-mer prefix and tile map.
 // Validates offsets (non-decreasing, within max_bases) on the device; a bad
 // read counts as zero k-mers and sets GDBG_ERR_BAD_OFFSETS in *err.

@@ -58,6 +58,32 @@ struct WindowParams {
     uint32_t* err;
 };
 
+// Bucketed batch insert (gdbg_bucket.cuh).
+constexpr int BK_BLOCK = 1024;        // threads per CTA in the bucket kernels
+constexpr int BK_WARPS = BK_BLOCK / 32;
+constexpr int BK_TPW = 2;             // warp tasks per warp per tile (k-mer passes)
+constexpr int BK_RPW = 8;             // records per lane per tile (record passes)
+constexpr int BK_MAXNT = 8;           // tables supported by the bucketed path
+constexpr int BK_MAP = 2048;          // first-touch map slots per chunk (2 x block)
+
+struct BucketParams {
+    uint32_t fs;                      // log2(cells per bucket)
+    uint32_t n_buckets;
+    uint32_t shift;                   // digit position (in bucket-id bits) of this pass
+    uint32_t n_tiles;
+    uint64_t tbase[BK_MAXNT];         // aligned global cell base of each table
+    uint32_t bbase[BK_MAXNT + 1];     // first bucket of each table
+    uint32_t twords[BK_MAXNT];        // padded word count of each table
+    const uint32_t* offsets;          // scatter: exclusive scan of hist (bin-major)
+    uint32_t* hist;                   // histogram output (bin-major: bin * n_tiles + tile)
+    const uint64_t* rin;
+    uint64_t* rout;
+    uint64_t n_recs;                  // host bound on the record count
+    const uint64_t* total_kmers;      // device: the batch's k-mer count (kofs[n_reads])
+    uint32_t n_tables;
+    uint64_t kmer_cap;                // k-mers the new-k-mer bitmask can hold
+};
+
 // Persistent batch insert (gdbg_persist.cuh).
 struct PersistParams {
     uint32_t window_tasks;        // warp tasks per window (<= 2^15)

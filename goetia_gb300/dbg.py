@@ -532,10 +532,18 @@ class dBGBase:
     def set_insert_schedule(self, window_kmers=0, kmers_per_thread=0):
         _lib.call("gdbg_set_insert_schedule", self._h, int(window_kmers), int(kmers_per_thread))
 
-    def set_insert_path(self, persistent=True):
-        """One persistent cooperative launch per batch, or launches per window."""
-        _lib.call("gdbg_set_insert_path", self._h,
-                  _lib.PATH_PERSISTENT if persistent else _lib.PATH_WINDOWED)
+    PATHS = {"persistent": _lib.PATH_PERSISTENT, "windowed": _lib.PATH_WINDOWED,
+             "bucketed": _lib.PATH_BUCKETED, "auto": _lib.PATH_AUTO,
+             True: _lib.PATH_PERSISTENT, False: _lib.PATH_WINDOWED}
+
+    def set_insert_path(self, path="auto"):
+        """Batch insert implementation: "persistent", "windowed", "bucketed" or
+        "auto" (True / False mean persistent / windowed)."""
+        _lib.call("gdbg_set_insert_path", self._h, self.PATHS[path])
+
+    def set_bucket_bits(self, log2_cells=0):
+        """Cells per bucket (log2) of the bucketed path; 0 = 64 KB of table."""
+        _lib.call("gdbg_set_bucket_bits", self._h, int(log2_cells))
 
     def insert_schedule(self):
         w, k = _lib.c_u32(), _lib.c_u32()

@@ -179,12 +179,21 @@ int gdbg_neighbor_masks_batch_device(gdbg_graph* g, const uint32_t* packed,
  * then a commit pass) and k-mers per thread of the windowed path (4 or 8).
  * 0 keeps a value. */
 int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmers_per_thread);
-/* Read-batch insert implementation: one persistent cooperative launch per
- * batch (default), or one probe and one commit launch per window.  Both give
- * identical results. */
+/* Read-batch insert implementation; all give identical results.
+ *   PERSISTENT  one cooperative launch per batch, per-k-mer table access
+ *   WINDOWED    one probe and one commit launch per window
+ *   BUCKETED    records partitioned by table region, each region applied in
+ *               shared memory (large batches on tables far beyond L2)
+ *   AUTO        BUCKETED for batches of >= 4M k-mers on >= 256 MB of tables,
+ *               else PERSISTENT (default) */
 #define GDBG_PATH_PERSISTENT 0
 #define GDBG_PATH_WINDOWED 1
+#define GDBG_PATH_BUCKETED 2
+#define GDBG_PATH_AUTO 3
 int gdbg_set_insert_path(gdbg_graph* g, int path);
+/* Cells per bucket of the bucketed path as log2 (0 = default: 64 KB of table
+ * per bucket). */
+int gdbg_set_bucket_bits(gdbg_graph* g, uint32_t log2_cells);
 int gdbg_get_insert_schedule(const gdbg_graph* g, uint32_t* window_kmers,
                              uint32_t* kmers_per_thread);
 /* Device status word (GDBG_ERR_* device bits); cleared by reading. */

@@ -57,17 +57,26 @@ def test_golden_plain_per_read(cuda_ready, name):
         k += n
 
 
+# insert path, window, k-mers per thread, log2 cells per bucket (0 = default)
+PATHS = [("persistent", 262144, 4, 0), ("persistent", 64, 8, 0), ("persistent", 5, 4, 0),
+         ("windowed", 262144, 4, 0), ("windowed", 64, 8, 0), ("windowed", 5, 4, 0),
+         ("bucketed", 0, 0, 0), ("bucketed", 0, 0, 5), ("bucketed", 0, 0, 7)]
+
+
 @pytest.mark.parametrize("name", names())
-@pytest.mark.parametrize("window,kpt", [(262144, 4), (64, 8), (5, 4)])
-@pytest.mark.parametrize("persistent", [True, False])
-def test_golden_batched(cuda_ready, name, window, kpt, persistent):
-    """One packed batch; windows smaller than the batch exercise the
-    cross-window first-touch logic (and, at 32 k-mers per window, the claims
-    epoch wrap after 127 windows)."""
+@pytest.mark.parametrize("path,window,kpt,fs", PATHS)
+def test_golden_batched(cuda_ready, name, path, window, kpt, fs):
+    """One packed batch through each insert path.  Windows smaller than the
+    batch exercise the cross-window first-touch logic (and, at 32 k-mers per
+    window, the claims epoch wrap after 127 windows); default buckets hold
+    several 1024-record chunks, tiny buckets give many buckets and two digit
+    passes."""
     c = Case(name)
     g = graph_for(c.storage, c.canonical, c.K, c.sizes)
     g.set_insert_schedule(window, kpt)
-    g.set_insert_path(persistent)
+    g.set_insert_path(path)
+    if fs:
+        g.set_bucket_bits(max(fs, 5) if c.storage == "bit" else fs)
     packed, off = c.packed()
     pr = G.PackedReads(packed, off)
     n_new = g.insert_packed(pr)
@@ -105,8 +114,9 @@ def _oracle_run(kind, canonical, K, sizes, pr):
     ("nibble", False, 21, 40009),
     ("bit", False, 25, 7919),
 ])
-@pytest.mark.parametrize("persistent", [True, False])
-def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table, persistent):
+@pytest.mark.parametrize("path,fs", [("persistent", 0), ("windowed", 0), ("bucketed", 0),
+                                     ("bucketed", 5)])
+def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table, path, fs):
     """10,000 reads of 150 bp from a 100 kb genome, 1% substitutions."""
     gen = synth.genome(100_000, 1)
     rows = synth.sample_reads(gen, 10_000, 150, 0.01, 2)
@@ -115,7 +125,9 @@ def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table, pers
     st, n_new_ref = _oracle_run(kind, canonical, K, sizes, pr)
     g = graph_for(kind, canonical, K, sizes)
     g.set_insert_schedule(65536, 4)
-    g.set_insert_path(persistent)
+    g.set_insert_path(path)
+    if fs:
+        g.set_bucket_bits(fs)
     n_new = g.insert_packed(pr)
     assert np.array_equal(n_new, n_new_ref)
     check_tables(g, st.tables())
@@ -133,8 +145,9 @@ def test_batches_in_sequence_vs_oracle(cuda_ready):
     st = oracle.Storage("byte", sizes)
     g = graph_for("byte", True, 31, sizes)
     g.set_insert_schedule(2048, 4)
+    g.set_bucket_bits(6)
     for b in range(6):
-        g.set_insert_path(b % 3 != 1)
+        g.set_insert_path(["persistent", "windowed", "bucketed"][b % 3])
         rows = synth.sample_reads(gen, 700, 150, 0.02, 100 + b)
         pr = synth.rows_to_packed(rows)
         _, ref = st.insert_reads(True, 31, pr.packed, pr.offsets)
@@ -150,11 +163,14 @@ def test_uneven_reads_vs_oracle(cuda_ready):
     pr = synth.list_to_packed(rs)
     sizes = oracle.primes(4, 60013)
     st, ref = _oracle_run("nibble", False, 21, sizes, pr)
-    g = graph_for("nibble", False, 21, sizes)
-    g.set_insert_schedule(4096, 8)
-    assert np.array_equal(g.insert_packed(pr), ref)
-    check_tables(g, st.tables())
-    assert (g.n_unique(), g.n_occupied()) == st.stats()
+    for path in ("persistent", "bucketed"):
+        g = graph_for("nibble", False, 21, sizes)
+        g.set_insert_schedule(4096, 8)
+        g.set_insert_path(path)
+        g.set_bucket_bits(9)
+        assert np.array_equal(g.insert_packed(pr), ref)
+        check_tables(g, st.tables())
+        assert (g.n_unique(), g.n_occupied()) == st.stats()
 
 
 def test_hash_array_insert_query_vs_oracle(cuda_ready):
