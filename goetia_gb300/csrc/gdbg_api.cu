@@ -82,6 +82,8 @@ uint32_t next_pow2(uint64_t x) {
 
 }  // namespace
 
+int gdbg::report_error(int code, const std::string& msg) { return fail(code, msg); }
+
 struct gdbg_graph {
     int storage = 0, shifter = 0;
     uint16_t K = 0;

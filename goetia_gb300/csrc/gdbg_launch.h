@@ -6,7 +6,12 @@
 
 #include "gdbg_types.h"
 
+#include <string>
+
 namespace gdbg {
+
+// Record the message behind a failing status for gdbg_last_error(); returns code.
+int report_error(int code, const std::string& msg);
 
 struct LaunchShape {
     bool canonical;

@@ -201,6 +201,43 @@ int gdbg_device_status(gdbg_graph* g, uint32_t* status);
 /* Kernel launches issued by this handle since creation. */
 int gdbg_launch_count(const gdbg_graph* g, uint64_t* launches);
 
+/* ---- insert without device allocation -------------------------------- */
+
+/* Limits of gdbg_insert_batch_noalloc (sizes of its static scratch). */
+#define GDBG_NOALLOC_MAX_READS 131072u
+#define GDBG_NOALLOC_MAX_TASKS 1048576u   /* packed_words/2 + n_reads must not exceed it */
+#define GDBG_NOALLOC_MAX_TABLES 8u
+#define GDBG_NOALLOC_SCRATCH_BYTES 17825792u
+
+/* Word offset of each table (and the total, entry n_tables) in the table
+ * buffer gdbg_insert_batch_noalloc works on: table i holds the reference's
+ * bytes (size/8+1, size or size/2+1) padded to a multiple of 256 bytes. */
+int gdbg_noalloc_table_layout(int storage, const uint64_t* sizes, uint16_t n_tables,
+                              uint64_t* word_offsets);
+
+/* No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory -- a framework that hands out all GPU memory from
+ * its own fixed pool, or a latency-critical loop that must not pay the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  Inserts one packed
+ * batch (device pointers, as gdbg_insert_batch_device) into caller-owned
+ * tables (`tables`, device, laid out by gdbg_noalloc_table_layout, zeroed
+ * by the caller before first use) with the same exact results, and calls no
+ * cudaMalloc, cudaFree or allocating library routine.  Its scratch is a
+ * static device array of GDBG_NOALLOC_SCRATCH_BYTES that every GPU loading
+ * this library holds until exit; batches beyond GDBG_NOALLOC_MAX_READS reads
+ * or GDBG_NOALLOC_MAX_TASKS warp tasks, or with more than
+ * GDBG_NOALLOC_MAX_TABLES tables, are rejected with GDBG_ERR_INVALID_ARG.
+ * The first call on a device looks the array up and clears it: make that
+ * call before any stream capture.  Calls share the array; calls that overlap
+ * on the GPU race and must be serialised by the caller.  n_new (device, one
+ * uint64 per read) may be NULL.  stats (device, 3 x uint64) may be NULL; it
+ * receives the call's n_unique and n_occupied increments and the device
+ * status bits (non-zero = a device-side check failed). */
+int gdbg_insert_batch_noalloc(int storage, int shifter, uint16_t K, const uint64_t* sizes,
+                              uint16_t n_tables, uint32_t* tables, const uint32_t* packed,
+                              uint64_t packed_words, const uint64_t* offsets, uint64_t n_reads,
+                              uint64_t* n_new, uint64_t* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
