@@ -80,7 +80,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -234,11 +234,14 @@ def run_gpu(args):
         d_batches.append((d_packed, d_off, d_new, pr.n_reads, pr.n_kmers(K)))
     torch.cuda.synchronize(dev)
 
-    def step(i):
+    def step_on(graph, i):
         d_packed, d_off, d_new, n_reads, nk = d_batches[i]
-        g.insert_device(d_packed.data_ptr(), d_packed.numel(), d_off.data_ptr(), n_reads,
-                        n_kmers=nk, n_new_ptr=d_new.data_ptr(), stream=stream.cuda_stream)
+        graph.insert_device(d_packed.data_ptr(), d_packed.numel(), d_off.data_ptr(), n_reads,
+                            n_kmers=nk, n_new_ptr=d_new.data_ptr(), stream=stream.cuda_stream)
         return nk
+
+    def step(i):
+        return step_on(g, i)
 
     for i in range(args.warmup):
         step(i)
@@ -246,19 +249,36 @@ def run_gpu(args):
     if world > 1:
         dist.barrier()
 
+    g.stage_times()   # reset the stage totals
     launches0 = g.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     kmers = 0
     with ClockSampler(local) as clocks:
+        time.sleep(0.3)
         torch.cuda.synchronize(dev)
         e0.record(stream)
         for i in range(args.warmup, n_batches):
             kmers += step(i)
         e1.record(stream)
         torch.cuda.synchronize(dev)
+        time.sleep(0.1)
     launches = g.launch_count() - launches0
     g.synchronize()   # raises if a device-side check fired
     dt = e0.elapsed_time(e1) / 1000.0
+    # per-stage times of the same steps, measured with CUDA events on the
+    # launching stream in a second timed pass over the same batches on a clone
+    g_prof = g.clone()
+    g_prof.set_stream(stream.cuda_stream)
+    g_prof.set_profiling(True)
+    for i in range(args.warmup):
+        step_on(g_prof, i)
+    torch.cuda.synchronize(dev)
+    g_prof.stage_times()
+    for i in range(args.warmup, n_batches):
+        step_on(g_prof, i)
+    torch.cuda.synchronize(dev)
+    stages = g_prof.stage_times()
+    del g_prof
     if world > 1:
         t = torch.tensor([dt], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -335,14 +355,19 @@ def run_gpu(args):
     peak, peak_kind = measured_peak()
     achieved = value / world * BYTES_PER_KMER / 1e9
     tpk = profile_traffic_per_kmer()
-    per_launch_kmers = kmers / max(args.steps, 1)
+    per_step_kmers = kmers / max(args.steps, 1)
+    stage_total = sum(ms for ms, _ in stages.values()) or 1.0
+    dom_name, (dom_ms, dom_n) = max(stages.items(), key=lambda kv: kv[1][0]) if stages else ("", (0.0, 1))
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-        "frac": achieved / peak, "peak_source": peak_kind,
-        "kernel": "insert (probe + commit passes per window)",
+        "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+        "kernel": "batch insert step: the k-mer insert pipeline of one batch",
         "algorithmic_bytes_per_kmer": BYTES_PER_KMER,
-        "traffic": (tpk * per_launch_kmers) if tpk else None,
-        "traffic_unit": "DRAM bytes per step (ncu, scaled by k-mers)" if tpk else None,
+        "traffic": (tpk * per_step_kmers) if tpk else None,
+        "traffic_unit": "DRAM bytes per step (ncu capture, scaled by k-mers)" if tpk else None,
+        "dominant_kernel": {"name": dom_name, "share": dom_ms / stage_total,
+                            "ms_per_launch": dom_ms / max(dom_n, 1), "launches": dom_n},
+        "stages_ms_per_step": {k: v[0] / max(args.steps, 1) for k, v in stages.items()},
     }
 
     line = None
@@ -365,7 +390,7 @@ def run_gpu(args):
                        "reads_per_step": int(batches[0].n_reads), "read_len": READ_LEN,
                        "genome_bp": GENOME_LEN, "substitution_rate": SUB_RATE,
                        "n_reads_dropped_per_step": int(batches[0].n_skipped),
-                       "insert_schedule": list(g.insert_schedule()),
+                       "insert_path": "bucketed" if "k_bkt_apply" in stages else "persistent",
                        "l2": "inputs larger than L2: 4 GiB of tables, random cells",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "k-mers/s", "h2d_bytes_per_step": h2d // args.steps,
@@ -386,7 +411,7 @@ def run_gpu(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--reads-per-step", type=int, default=1_000_000)

@@ -76,6 +76,8 @@ SIGNATURES = {
     "gdbg_insert_batch_noalloc": [c_int, c_int, c_u16, u64p, c_u16, c_vp, c_vp, c_u64, c_vp,
                                   c_u64, c_vp, c_vp, c_vp],
     "gdbg_launch_count": [c_vp, u64p],
+    "gdbg_set_profiling": [c_vp, c_int],
+    "gdbg_stage_times": [c_vp, c_cp, c_u64, P(ctypes.c_double), u64p, c_u32, u32p],
 }
 
 _lib = None

@@ -122,7 +122,12 @@ struct gdbg_graph {
     DevBuf<int16_t> st_counts;
     DevBuf<uint8_t> st_u8;
     uint64_t launches = 0;
-    bool live_hint_valid = false;
+    // optional per-stage timing (CUDA events around each stage, on its stream)
+    bool profiling = false;
+    struct Pending { const char* name; cudaEvent_t a, b; };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> free_events;
+    std::vector<std::pair<std::string, std::pair<double, uint64_t>>> stage_acc;
 
     LaunchShape shape(int kpt_) const {
         return LaunchShape{shifter == GDBG_CAN_LEMIRE, kpt_, (int)sizes.size()};
@@ -130,6 +135,58 @@ struct gdbg_graph {
 };
 
 namespace {
+
+cudaEvent_t take_event(gdbg_graph* g) {
+    if (!g->free_events.empty()) {
+        cudaEvent_t e = g->free_events.back();
+        g->free_events.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Records a CUDA event pair around one stage when profiling is on.
+struct Stage {
+    gdbg_graph* g;
+    const char* name;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    Stage(gdbg_graph* g_, const char* n, cudaStream_t s) : g(g_), name(n), st(s) {
+        if (g->profiling) {
+            a = take_event(g);
+            cudaEventRecord(a, st);
+        }
+    }
+    ~Stage() {
+        if (a) {
+            cudaEvent_t b = take_event(g);
+            cudaEventRecord(b, st);
+            g->pending.push_back({name, a, b});
+        }
+    }
+};
+
+// Resolve recorded stage events into the per-stage totals.
+void collect_stages(gdbg_graph* g) {
+    for (auto& p : g->pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            bool found = false;
+            for (auto& acc : g->stage_acc)
+                if (acc.first == p.name) {
+                    acc.second.first += ms;
+                    acc.second.second += 1;
+                    found = true;
+                }
+            if (!found) g->stage_acc.push_back({p.name, {ms, 1}});
+        }
+        g->free_events.push_back(p.a);
+        g->free_events.push_back(p.b);
+    }
+    g->pending.clear();
+}
 
 int set_device(const gdbg_graph* g) {
     GDBG_CUDA(cudaSetDevice(g->device));
@@ -228,6 +285,7 @@ int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
     GDBG_TRY(g->tofs.ensure(n_reads + 1));
     GDBG_TRY(g->partials.ensure(2 * (n_reads / 1024 + 2)));
     int nl = 0;
+    Stage stage_prep(g, "prepare", st);
     GDBG_CUDA(launch_kmer_prefix(offsets, n_reads, g->K, packed_words * 16ull, g->partials.p,
                                  g->kofs.p, g->tofs.p, g->d_err, st, &nl));
     g->launches += nl;
@@ -368,8 +426,11 @@ int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cuda
     const bool canon = g->shifter == GDBG_CAN_LEMIRE;
     cudaError_t e;
     bp.rout = g->rec_a.p;
-    if ((e = launch_bucket_emit(canon, st, b, g->hp, g->tp, bp)) != cudaSuccess)
-        return set_error_launch(e, "bucket emit");
+    {
+        Stage sg(g, "k_bkt_emit", st);
+        if ((e = launch_bucket_emit(canon, st, b, g->hp, g->tp, bp)) != cudaSuccess)
+            return set_error_launch(e, "bucket emit");
+    }
     uint64_t* src = g->rec_a.p;
     uint64_t* dst = g->rec_b.p;
     bp.n_tiles = (uint32_t)tiles;
@@ -379,18 +440,28 @@ int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cuda
         bp.shift = 8 * pass;
         bp.rin = src;
         bp.rout = dst;
-        if ((e = launch_bucket_hist((uint32_t)tiles, st, bp)) != cudaSuccess)
-            return set_error_launch(e, "bucket histogram");
-        if ((e = launch_scan32(g->hist.p, g->hist_off.p, hmax, g->scan_parts.p, st)) != cudaSuccess)
-            return set_error_launch(e, "bucket scan");
-        if ((e = launch_bucket_scatter(pass + 1 == passes, (uint32_t)tiles, st, bp, g->bstart.p)) != cudaSuccess)
-            return set_error_launch(e, "bucket scatter");
+        {
+            Stage sg(g, "k_bkt_hist", st);
+            if ((e = launch_bucket_hist((uint32_t)tiles, st, bp)) != cudaSuccess)
+                return set_error_launch(e, "bucket histogram");
+        }
+        {
+            Stage sg(g, "k_scan32", st);
+            if ((e = launch_scan32(g->hist.p, g->hist_off.p, hmax, g->scan_parts.p, st)) != cudaSuccess)
+                return set_error_launch(e, "bucket scan");
+        }
+        {
+            Stage sg(g, "k_bkt_scatter", st);
+            if ((e = launch_bucket_scatter(pass + 1 == passes, (uint32_t)tiles, st, bp, g->bstart.p)) != cudaSuccess)
+                return set_error_launch(e, "bucket scatter");
+        }
         std::swap(src, dst);
         g->launches += 5;   // histogram, 3 scan kernels, scatter
     }
     if ((e = launch_bucket_starts_fix(st, bp, g->bstart.p)) != cudaSuccess)
         return set_error_launch(e, "bucket starts");
     g->launches += 2;
+    Stage sg_apply(g, "k_bkt_apply", st);
     if ((e = launch_bucket_apply(g->storage, g->tp, bp, src, g->bstart.p, g->new_bits.p,
                                  g->d_counters, st)) != cudaSuccess)
         return set_error_launch(e, "bucket apply");
@@ -436,6 +507,7 @@ int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cu
     LaunchShape s = g->shape(4);
     int grid = 0;
     cudaError_t e;
+    Stage sg(g, "k_insert_persistent", st);
     switch (g->storage) {
     case GDBG_BIT: e = launch_insert_persistent<GDBG_BIT>(s, b.task_cap, st, b, g->hp, g->tp, pp, &grid); break;
     case GDBG_BYTE: e = launch_insert_persistent<GDBG_BYTE>(s, b.task_cap, st, b, g->hp, g->tp, pp, &grid); break;
@@ -661,6 +733,11 @@ int gdbg_destroy(gdbg_graph* g) {
     g->scan_parts.release(); g->bstart.release(); g->new_bits.release();
     g->st_packed.release(); g->st_offsets.release(); g->st_out64.release();
     g->st_out64b.release(); g->st_out64c.release(); g->st_counts.release(); g->st_u8.release();
+    for (auto& p : g->pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : g->free_events) cudaEventDestroy(e);
     if (g->own_stream) cudaStreamDestroy(g->own_stream);
     delete g;
     return GDBG_OK;
@@ -1062,6 +1139,37 @@ int gdbg_device_status(gdbg_graph* g, uint32_t* status) {
     GDBG_CUDA(cudaMemcpyAsync(status, g->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
     GDBG_CUDA(cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream));
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    return GDBG_OK;
+}
+
+int gdbg_set_profiling(gdbg_graph* g, int on) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    g->profiling = on != 0;
+    return GDBG_OK;
+}
+
+int gdbg_stage_times(gdbg_graph* g, char* names, uint64_t names_len, double* total_ms,
+                     uint64_t* launches, uint32_t max_stages, uint32_t* n_stages) {
+    if (!g || !n_stages) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    collect_stages(g);
+    std::string joined;
+    uint32_t n = 0;
+    for (auto& acc : g->stage_acc) {
+        if (n < max_stages) {
+            if (total_ms) total_ms[n] = acc.second.first;
+            if (launches) launches[n] = acc.second.second;
+        }
+        if (!joined.empty()) joined += ",";
+        joined += acc.first;
+        ++n;
+    }
+    if (names && names_len) {
+        std::strncpy(names, joined.c_str(), names_len - 1);
+        names[names_len - 1] = 0;
+    }
+    *n_stages = n;
+    g->stage_acc.clear();
     return GDBG_OK;
 }
 

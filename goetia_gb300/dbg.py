@@ -555,6 +555,20 @@ class dBGBase:
         _lib.call("gdbg_device_status", self._h, _c.byref(s))
         return int(s.value)
 
+    def set_profiling(self, on=True):
+        """Bracket each insert stage with CUDA events (see stage_times)."""
+        _lib.call("gdbg_set_profiling", self._h, 1 if on else 0)
+
+    def stage_times(self):
+        """{stage: (total_ms, launches)} since the last call (synchronises)."""
+        names = _c.create_string_buffer(4096)
+        ms = (_c.c_double * 64)()
+        cnt = (_c.c_uint64 * 64)()
+        n = _lib.c_u32()
+        _lib.call("gdbg_stage_times", self._h, names, 4096, ms, cnt, 64, _c.byref(n))
+        keys = names.value.decode().split(",") if n.value else []
+        return {k: (ms[i], int(cnt[i])) for i, k in enumerate(keys[:64])}
+
     def launch_count(self):
         n = _lib.c_u64()
         _lib.call("gdbg_launch_count", self._h, _c.byref(n))

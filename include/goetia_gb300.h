@@ -198,6 +198,13 @@ int gdbg_get_insert_schedule(const gdbg_graph* g, uint32_t* window_kmers,
                              uint32_t* kmers_per_thread);
 /* Device status word (GDBG_ERR_* device bits); cleared by reading. */
 int gdbg_device_status(gdbg_graph* g, uint32_t* status);
+/* Per-stage timing: when on, every stage of a batch insert is bracketed by
+ * CUDA events on its stream.  gdbg_stage_times synchronises, returns the
+ * accumulated milliseconds and launch counts per stage (names comma-separated
+ * in `names`) and resets the totals. */
+int gdbg_set_profiling(gdbg_graph* g, int on);
+int gdbg_stage_times(gdbg_graph* g, char* names, uint64_t names_len, double* total_ms,
+                     uint64_t* launches, uint32_t max_stages, uint32_t* n_stages);
 /* Kernel launches issued by this handle since creation. */
 int gdbg_launch_count(const gdbg_graph* g, uint64_t* launches);
 
