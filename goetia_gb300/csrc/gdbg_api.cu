@@ -1119,7 +1119,7 @@ int gdbg_set_bucket_bits(gdbg_graph* g, uint32_t log2_cells) {
         return fail(GDBG_ERR_INVALID_ARG, "bucket size must be 2^k cells, one word <= 2^k <= 2^20");
     if (log2_cells) {
         const uint32_t cpw = g->storage == GDBG_BIT ? 32u : g->storage == GDBG_NIBBLE ? 8u : 4u;
-        const uint64_t smem = ((1ull << log2_cells) / cpw) * 4 + 2 * BK_MAP * 4;
+        const uint64_t smem = ((1ull << log2_cells) / cpw) * 4 + 2 * 2 * 2048 * 4 + 1024;
         if (smem > 200 * 1024) return fail(GDBG_ERR_INVALID_ARG, "bucket does not fit shared memory");
     }
     g->bucket_fs = log2_cells;

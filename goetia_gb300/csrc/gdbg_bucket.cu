@@ -49,7 +49,7 @@ template <int ST>
 static cudaError_t apply_one(const TableParams& tp, const BucketParams& bp, const uint64_t* recs,
                              const uint32_t* start, uint32_t* new_bits,
                              unsigned long long* counters, cudaStream_t st) {
-    const size_t smem = ((size_t)(1u << bp.fs) / cells_per_word<ST>()) * 4 + 2 * BK_MAP * 4;
+    const size_t smem = bk_apply_smem((1u << bp.fs) / cells_per_word<ST>());
     cudaError_t e = cudaFuncSetAttribute(k_bkt_apply<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;

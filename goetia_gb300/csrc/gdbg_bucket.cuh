@@ -49,13 +49,6 @@ __device__ __forceinline__ uint32_t digit_peers(uint32_t d, bool valid) {
     return m;
 }
 
-// Add this warp's digits to its private histogram row.
-__device__ __forceinline__ void warp_count(uint32_t* row, uint32_t d, bool valid) {
-    const uint32_t peers = digit_peers(d, valid);
-    if (valid && (peers & lanemask_lt()) == 0) row[d] += __popc(peers);
-    __syncwarp();
-}
-
 // Position of this lane's record in the warp's running bin cursor, then
 // advance the cursor by the group size.
 __device__ __forceinline__ uint32_t warp_rank(uint32_t* row, uint32_t d, bool valid) {
@@ -191,10 +184,11 @@ k_bkt_scatter(BucketParams bp, uint32_t* __restrict__ start) {
         const uint64_t k = wbase + (uint64_t)j * 32 + lane;
         rec[j] = k < n_recs ? __ldcs(bp.rin + k) : 0;
     }
+    // per-warp counts: one shared-memory atomic per record (ranks come later)
 #pragma unroll
     for (int j = 0; j < BK_IPT; ++j) {
         const uint64_t k = wbase + (uint64_t)j * 32 + lane;
-        warp_count(whist[w], rec_digit(rec[j], bp), k < n_recs);
+        if (k < n_recs) atomicAdd(&whist[w][rec_digit(rec[j], bp)], 1u);
     }
     __syncthreads();
     if (threadIdx.x < 256) {
@@ -291,8 +285,14 @@ __host__ __device__ constexpr uint32_t cells_per_word() {
     return STORAGE == GDBG_BIT ? 32u : STORAGE == GDBG_BYTE ? 4u : 8u;
 }
 
-// One CTA per bucket.  Dynamic shared memory: the bucket's table words, then
-// the chunk map (keys, then minimum chunk ranks).
+constexpr int BK_RPT = 2;                         // records per thread per chunk
+constexpr int BK_CHUNK = BK_BLOCK * BK_RPT;       // records per chunk
+constexpr int BK_AMAP = 2 * BK_CHUNK;             // chunk map slots
+
+// One CTA per bucket.  Dynamic shared memory: the bucket's table words, the
+// chunk map (keys, then minimum chunk ranks) and a dirty bit per 32-byte
+// sector of the slice.  Records are applied in chunks of BK_CHUNK in g order;
+// only dirty sectors are written back.
 template <int STORAGE>
 __global__ void __launch_bounds__(BK_BLOCK)
 k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
@@ -306,13 +306,15 @@ k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
     while (ti + 1 < tp.n && bp.bbase[ti + 1] <= bk) ++ti;
     const uint32_t region_cells = 1u << bp.fs;
     const uint32_t region_words = region_cells / cells_per_word<STORAGE>();
+    const uint32_t region_sectors = (region_words + 7) / 8;
     const uint64_t c0 = (uint64_t)(bk - bp.bbase[ti]) << bp.fs;
     const uint64_t w0 = c0 / cells_per_word<STORAGE>();
     uint32_t nw = region_words;
     if (w0 + nw > bp.twords[ti]) nw = (uint32_t)(bp.twords[ti] - w0);
     uint32_t* region = smem;
     uint32_t* mkey = smem + region_words;
-    uint32_t* mval = mkey + BK_MAP;
+    uint32_t* mval = mkey + BK_AMAP;
+    uint32_t* dirty = mval + BK_AMAP;
     const uint32_t* gsrc = tp.words[ti] + w0;
     const bool vec = ((w0 & 3u) == 0) && ((nw & 3u) == 0);
     if (vec) {
@@ -332,72 +334,110 @@ k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
     } else {
         for (uint32_t k = threadIdx.x; k < nw; k += BK_BLOCK) region[k] = __ldcs(gsrc + k);
     }
-    for (uint32_t k = threadIdx.x; k < BK_MAP; k += BK_BLOCK) mkey[k] = 0;
+    for (uint32_t k = threadIdx.x; k < BK_AMAP; k += BK_BLOCK) mkey[k] = 0;
+    for (uint32_t k = threadIdx.x; k < (region_sectors + 31) / 32; k += BK_BLOCK) dirty[k] = 0;
     __syncthreads();
     const uint32_t co_mask = region_cells - 1;
     unsigned long long occ = 0;
-    uint64_t next = rs + threadIdx.x < re ? __ldcs(recs + rs + threadIdx.x) : 0;
-    for (uint32_t base = rs; base < re; base += BK_BLOCK) {
-        const uint32_t k = base + threadIdx.x;
-        const bool active = k < re;
-        const uint64_t r = next;
-        if (k + BK_BLOCK < re) next = __ldcs(recs + k + BK_BLOCK);
-        uint32_t co = 0, g = 0, word = 0, shift = 0, slot = 0;
-        bool fresh = false;
-        if (active) {
-            co = (uint32_t)(r >> 32) & co_mask;
-            g = (uint32_t)r;
-            region_cell<STORAGE>(co, word, shift);
-            fresh = cell_value<STORAGE>(region[word], shift) == 0;
-        }
-        if (fresh) {
-            // claim the smallest chunk rank for this cell (rank order = g order)
-            slot = (co * 0x9E3779B1u) >> (32 - 11);
-            for (int it = 0; it < BK_MAP; ++it) {
-                const uint32_t prev = atomicCAS(mkey + slot, 0u, co + 1u);
-                if (prev == 0u) {
-                    mval[slot] = threadIdx.x;   // first writer; the min is taken below
-                    break;
+    uint64_t next[BK_RPT];
+#pragma unroll
+    for (int r = 0; r < BK_RPT; ++r) {
+        const uint32_t k = rs + r * BK_BLOCK + threadIdx.x;
+        next[r] = k < re ? __ldcs(recs + k) : 0;
+    }
+    for (uint32_t base = rs; base < re; base += BK_CHUNK) {
+        uint32_t co[BK_RPT], g[BK_RPT], word[BK_RPT], shift[BK_RPT], slot[BK_RPT];
+        bool active[BK_RPT], fresh[BK_RPT];
+#pragma unroll
+        for (int r = 0; r < BK_RPT; ++r) {
+            const uint32_t idx = r * BK_BLOCK + threadIdx.x;
+            const uint32_t k = base + idx;
+            active[r] = k < re;
+            const uint64_t rec = next[r];
+            if (k + BK_CHUNK < re) next[r] = __ldcs(recs + k + BK_CHUNK);
+            co[r] = (uint32_t)(rec >> 32) & co_mask;
+            g[r] = (uint32_t)rec;
+            region_cell<STORAGE>(co[r], word[r], shift[r]);
+            fresh[r] = active[r] && cell_value<STORAGE>(region[word[r]], shift[r]) == 0;
+            slot[r] = 0;
+            if (fresh[r]) {
+                // register the cell in the chunk map (rank order = g order)
+                uint32_t sl = (co[r] * 0x9E3779B1u) >> (32 - 12);
+                for (int it = 0; it < BK_AMAP; ++it) {
+                    const uint32_t prev = atomicCAS(mkey + sl, 0u, co[r] + 1u);
+                    if (prev == 0u) {
+                        mval[sl] = 0xFFFFFFFFu;
+                        break;
+                    }
+                    if (prev == co[r] + 1u) break;
+                    sl = (sl + 1) & (BK_AMAP - 1);
                 }
-                if (prev == co + 1u) break;
-                slot = (slot + 1) & (BK_MAP - 1);
+                slot[r] = sl;
             }
         }
         __syncthreads();
-        if (fresh) atomicMin(mval + slot, threadIdx.x);
+#pragma unroll
+        for (int r = 0; r < BK_RPT; ++r)
+            if (fresh[r]) atomicMin(mval + slot[r], r * BK_BLOCK + threadIdx.x);
         __syncthreads();
-        const bool isnew = fresh && mval[slot] == threadIdx.x;
-        if (active) {
-            if (STORAGE == GDBG_BIT) {
-                if (fresh) atomicOr(region + word, 1u << shift);
-            } else {
-                uint32_t cur = region[word];
-                for (int it = 0; it < BK_BLOCK + 1; ++it) {
-                    if (cell_value<STORAGE>(cur, shift) >= cell_max<STORAGE>()) break;
-                    const uint32_t prev = atomicCAS(region + word, cur, cur + (1u << shift));
-                    if (prev == cur) break;
-                    cur = prev;
+#pragma unroll
+        for (int r = 0; r < BK_RPT; ++r) {
+            const bool isnew = fresh[r] && mval[slot[r]] == r * BK_BLOCK + threadIdx.x;
+            if (active[r]) {
+                bool changed = false;
+                if (STORAGE == GDBG_BIT) {
+                    if (fresh[r]) {
+                        atomicOr(region + word[r], 1u << shift[r]);
+                        changed = true;
+                    }
+                } else {
+                    uint32_t cur = region[word[r]];
+                    for (int it = 0; it < BK_CHUNK + 1; ++it) {
+                        if (cell_value<STORAGE>(cur, shift[r]) >= cell_max<STORAGE>()) break;
+                        const uint32_t prev = atomicCAS(region + word[r], cur, cur + (1u << shift[r]));
+                        if (prev == cur) {
+                            changed = true;
+                            break;
+                        }
+                        cur = prev;
+                    }
+                }
+                if (changed) {
+                    const uint32_t sec = word[r] >> 3;
+                    atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
                 }
             }
-        }
-        if (isnew && g < bp.kmer_cap) {
-            atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
-            if (ti == 0) ++occ;
+            if (isnew && g[r] < bp.kmer_cap) {
+                atomicOr(new_bits + (g[r] >> 5), 1u << (g[r] & 31u));
+                if (ti == 0) ++occ;
+            }
         }
         __syncthreads();
-        if (fresh) mkey[slot] = 0;
+#pragma unroll
+        for (int r = 0; r < BK_RPT; ++r)
+            if (fresh[r]) mkey[slot[r]] = 0;
         __syncthreads();
     }
+    // write back the dirty 32-byte sectors (8 words each)
     uint32_t* gdst = tp.words[ti] + w0;
-    if (vec) {
-        uint4* g4 = reinterpret_cast<uint4*>(gdst);
-        const uint4* s4 = reinterpret_cast<const uint4*>(region);
-        for (uint32_t k = threadIdx.x; k < (nw >> 2); k += BK_BLOCK) g4[k] = s4[k];
-    } else {
-        for (uint32_t k = threadIdx.x; k < nw; k += BK_BLOCK) gdst[k] = region[k];
+    for (uint32_t sec = threadIdx.x; sec < region_sectors; sec += BK_BLOCK) {
+        if (!((dirty[sec >> 5] >> (sec & 31u)) & 1u)) continue;
+        const uint32_t wb = sec * 8;
+        if (vec && wb + 8 <= nw) {
+            uint4* g4 = reinterpret_cast<uint4*>(gdst + wb);
+            const uint4* s4 = reinterpret_cast<const uint4*>(region + wb);
+            g4[0] = s4[0];
+            g4[1] = s4[1];
+        } else {
+            for (uint32_t k = wb; k < wb + 8 && k < nw; ++k) gdst[k] = region[k];
+        }
     }
     occ = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)occ);
     if ((threadIdx.x & 31) == 0 && occ) atomicAdd(counters + 1, occ);
+}
+
+__host__ __device__ constexpr size_t bk_apply_smem(uint32_t region_words) {
+    return (size_t)region_words * 4 + 2 * BK_AMAP * 4 + ((region_words + 7) / 8 + 31) / 32 * 4;
 }
 
 // Per-read new counts from the new-k-mer bitmask, plus the batch total.
