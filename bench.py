@@ -164,6 +164,45 @@ def cpu_baseline_port(batches, sample_reads, threads):
     return total / dt, total, dt
 
 
+def run_serving(args, check_streams=3):
+    """Config 5 shape: 64 streams, each its own dBG<BitStorage, CanLemireShifter>
+    (K=31, 4 tables of 2^24-2^28 bits, log-uniform per stream), 150 bp reads
+    with 1% errors arriving as 8-4096-read chunks on Poisson timing.  Stream
+    sizes are the configuration's 10k-5M reads scaled by args.serve_scale to
+    bound the run.  Per-chunk new counts of a few streams are checked against
+    a sequential replay."""
+    import numpy as np
+    import goetia_gb300 as G
+    from goetia_gb300 import serving
+    sc = args.serve_scale
+    specs = serving.make_streams(args.serve_streams, 17, reads_lo=max(8, int(10_000 * sc)),
+                                 reads_hi=max(16, int(5_000_000 * sc)), chunk_lo=8, chunk_hi=4096,
+                                 table_lo_bits=24, table_hi_bits=28, mean_gap_s=args.serve_gap,
+                                 genome_len=2_000_000)
+    srv = serving.Server(G.BitStorage, G.CanLemireShifter, K=31, n_tables=4,
+                         hbm_budget=int(args.serve_budget_gb * (1 << 30)), depth=4)
+    results, stats = srv.run(specs)
+    exact = True
+    for spec in specs[:check_streams]:
+        want = serving.replay(spec)
+        exact &= all(np.array_equal(r.n_new, w) for r, w in zip(results[spec.sid], want))
+    offered = sum(s.n_kmers(31) for s in specs)
+    return {
+        "streams": len(specs), "chunks": stats["chunks"],
+        "p50_chunk_latency_ms": stats["p50_ms"], "p99_chunk_latency_ms": stats["p99_ms"],
+        "max_chunk_latency_ms": stats["max_ms"],
+        "kmers_per_s": stats["kmers_per_s"], "kmers": stats["kmers"],
+        "wall_s": stats["wall_s"], "offered_kmers": offered,
+        "peak_hbm_GB": stats["peak_hbm_bytes"] / (1 << 30),
+        "admission_waits": stats["admission_waits"],
+        "hbm_budget_GB": args.serve_budget_gb,
+        "exact_vs_sequential_replay": bool(exact), "replay_checked_streams": check_streams,
+        "workload": (f"64 streams, reads 10k-5M x {sc} log-uniform, chunks 8-4096 reads, "
+                     f"Poisson mean gap {args.serve_gap * 1e3:.1f} ms per stream, "
+                     "Bit 4 x 2^24-2^28 bits per stream"),
+    }
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -370,6 +409,12 @@ def run_gpu(args):
         "stages_ms_per_step": {k: v[0] / max(args.steps, 1) for k, v in stages.items()},
     }
 
+    serving_stats = None
+    if not args.no_serving:
+        del g, g2, g3
+        torch.cuda.empty_cache()
+        serving_stats = run_serving(args)
+
     line = None
     if rank == 0:
         cpu = None
@@ -398,6 +443,7 @@ def run_gpu(args):
             "plain": {"value": plain_value, "unit": "k-mers/s",
                       "sample": f"{n_plain - 20} reads, one insert_sequence call each"},
             "gpu_launches": int(launches),
+            "serving": serving_stats,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
@@ -421,6 +467,11 @@ def main():
     ap.add_argument("--cpu-sample-reads", type=int, default=300_000)
     ap.add_argument("--reference-sample-reads", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-streams", type=int, default=64)
+    ap.add_argument("--serve-scale", type=float, default=0.02)
+    ap.add_argument("--serve-gap", type=float, default=0.002)
+    ap.add_argument("--serve-budget-gb", type=float, default=32.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -532,7 +532,10 @@ int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64
         if (g->path == GDBG_PATH_AUTO && fits && table_bytes >= (256ull << 20) &&
             n_total >= (1ull << 22))
             return run_insert_bucketed(g, b, n_new, st);
-        if (g->path != GDBG_PATH_WINDOWED) return run_insert_persistent(g, b, n_new, st);
+        // the cooperative kernel only on request: AUTO stays with kernels that
+        // never wait on other blocks, so graphs on concurrent streams cannot
+        // hold each other's blocks off the GPU
+        if (g->path == GDBG_PATH_PERSISTENT) return run_insert_persistent(g, b, n_new, st);
     }
     GDBG_TRY(ensure_insert_scratch(g, st));
     if (g->epoch_on_device) {

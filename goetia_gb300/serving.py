@@ -1,0 +1,274 @@
+"""Serving loop: many concurrent sample streams, each with its own dBG resident
+in HBM, fed with read chunks as they arrive.
+
+The reference's streaming driver (goetia/processors.py:39-498,
+AsyncSequenceProcessor) consumes one sample at a time in a worker thread and
+reports progress per interval of k-mers.  Here one process serves many
+samples at once on one GPU:
+
+* admission: a stream is admitted when its tables and scratch fit in the HBM
+  budget; otherwise it waits until a finished stream releases its memory;
+* continuous batching: every admitted stream has its own CUDA stream; a chunk
+  is dispatched as soon as it arrives (host pinned staging -> H2D copy ->
+  insert -> D2H copy of the per-read new-k-mer counts -> event), up to
+  `depth` chunks of a stream in flight, so chunks of different streams overlap
+  on the device while each stream's chunks apply in arrival order;
+* completion: events are polled; a chunk's latency is completion time minus
+  arrival time.
+
+Per-chunk new counts equal a sequential replay of each stream, whatever the
+mix (tests/test_gpu_serving.py).
+"""
+import collections
+import dataclasses
+import time
+
+import numpy as np
+
+from . import dbg as D
+from .reads import PackedReads
+
+
+@dataclasses.dataclass
+class StreamSpec:
+    """One sample: its table size and its chunks with arrival times (seconds
+    from the start of the run)."""
+    sid: int
+    max_table: int
+    chunks: list            # list of PackedReads
+    arrivals: list          # seconds, non-decreasing
+
+    def n_kmers(self, K):
+        return sum(c.n_kmers(K) for c in self.chunks)
+
+
+@dataclasses.dataclass
+class ChunkResult:
+    sid: int
+    index: int
+    n_reads: int
+    n_kmers: int
+    n_new: np.ndarray
+    arrival: float
+    done: float
+
+    @property
+    def latency(self):
+        return self.done - self.arrival
+
+
+class _Slot:
+    def __init__(self, torch, dev, max_words, max_reads):
+        self.d_packed = torch.empty(max_words, dtype=torch.int32, device=dev)
+        self.d_off = torch.empty(max_reads + 1, dtype=torch.int64, device=dev)
+        self.d_new = torch.empty(max_reads, dtype=torch.int64, device=dev)
+        self.h_packed = torch.empty(max_words, dtype=torch.int32).pin_memory()
+        self.h_off = torch.empty(max_reads + 1, dtype=torch.int64).pin_memory()
+        self.h_new = torch.empty(max_reads, dtype=torch.int64).pin_memory()
+        self.nbytes = (max_words * 4 + (2 * max_reads + 1) * 8)
+
+
+class _Stream:
+    def __init__(self, spec, server):
+        torch = server.torch
+        self.spec = spec
+        storage = server.storage_type.build(spec.max_table, server.n_tables)
+        self.graph = D.dBG[server.storage_type, server.shifter_type].build(storage, server.K)
+        self.graph.set_insert_path("windowed")
+        self.graph.set_insert_schedule(server.window, 4)
+        self.cuda = torch.cuda.Stream(server.dev)
+        self.graph.set_stream(self.cuda.cuda_stream)
+        max_reads = max(c.n_reads for c in spec.chunks)
+        max_words = max(c.packed.size for c in spec.chunks)
+        self.slots = [_Slot(torch, server.dev, max_words, max_reads) for _ in range(server.depth)]
+        self.free = collections.deque(range(server.depth))
+        self.inflight = collections.deque()      # (event, slot, index)
+        self.next_chunk = 0                      # next chunk to dispatch
+        self.done_chunks = 0
+        self.results = []
+        # grow the graph's scratch to the largest chunk now, so no device
+        # allocation (and its device-wide synchronisation) happens while
+        # serving; the tables are zeroed again afterwards
+        big = max(spec.chunks, key=lambda c: c.n_kmers(server.K))
+        self.graph.insert_packed(big)
+        self.graph.reset()
+
+    def table_bytes(self):
+        return sum(self.graph.table_bytes())
+
+
+def stream_footprint(storage_type, max_table, n_tables, window, n_tables_scratch=None):
+    """HBM bytes a stream holds: tables plus the windowed insert's scratch."""
+    sizes = storage_type.build(max_table, n_tables).get_tablesizes()
+    per = {D.BitStorage: lambda p: p // 8 + 1, D.ByteStorage: lambda p: p,
+           D.NibbleStorage: lambda p: p // 2 + 1}[storage_type]
+    tables = sum((per(p) + 255) // 256 * 256 for p in sizes)
+    slots = 1
+    while slots < 2 * window * n_tables:
+        slots *= 2
+    scratch = slots * 8 * 5 // 4 + window * 4 * (1 + n_tables)
+    return tables + scratch
+
+
+class Server:
+    """Continuous-batching server for many dBG streams on one GPU."""
+
+    def __init__(self, storage_type=D.BitStorage, shifter_type=D.CanLemireShifter, K=31,
+                 n_tables=4, hbm_budget=16 << 30, depth=2, window=262144, device=0):
+        import torch
+        self.torch = torch
+        self.dev = torch.device("cuda", device)
+        self.storage_type = storage_type
+        self.shifter_type = shifter_type
+        self.K = K
+        self.n_tables = n_tables
+        self.budget = hbm_budget
+        self.depth = depth
+        self.window = window
+
+    def footprint(self, spec):
+        return stream_footprint(self.storage_type, spec.max_table, self.n_tables, self.window) + \
+            self.depth * (max(c.packed.size for c in spec.chunks) * 4 +
+                          (2 * max(c.n_reads for c in spec.chunks) + 1) * 8)
+
+    def run(self, specs, time_scale=1.0, max_seconds=600.0):
+        """Serve every stream's chunks at their arrival times.  Returns
+        (results, stats): results per stream id (list of ChunkResult in chunk
+        order), stats with latency percentiles, throughput and admission."""
+        torch = self.torch
+        order = sorted(specs, key=lambda s: s.arrivals[0])
+        waiting = collections.deque(order)       # not yet admitted
+        active = {}
+        used = 0
+        peak_used = 0
+        results = {}
+        admitted_at = {}
+        waited = set()
+        total_kmers = 0
+        lat = []
+        t0 = time.perf_counter()
+        first_dispatch = None
+        last_done = None
+        while waiting or active:
+            now = (time.perf_counter() - t0) / time_scale
+            if now > max_seconds:
+                raise TimeoutError("serving run exceeded its time limit")
+            # admission: streams whose first chunk has arrived, in arrival order
+            while waiting and waiting[0].arrivals[0] <= now:
+                spec = waiting[0]
+                need = self.footprint(spec)
+                if need > self.budget:
+                    raise MemoryError(f"stream {spec.sid} needs {need} bytes, over the budget")
+                if used + need > self.budget:
+                    waited.add(spec.sid)
+                    break
+                waiting.popleft()
+                st = _Stream(spec, self)
+                st.need = need
+                used += need
+                peak_used = max(peak_used, used)
+                active[spec.sid] = st
+                admitted_at[spec.sid] = now
+            # dispatch arrived chunks
+            for st in active.values():
+                spec = st.spec
+                while (st.free and st.next_chunk < len(spec.chunks)
+                       and spec.arrivals[st.next_chunk] <= now):
+                    i = st.next_chunk
+                    c = spec.chunks[i]
+                    slot = st.slots[st.free.popleft()]
+                    nw, nr = c.packed.size, c.n_reads
+                    slot.h_packed[:nw].numpy()[:] = c.packed.view(np.int32)
+                    slot.h_off[:nr + 1].numpy()[:] = c.offsets.view(np.int64)
+                    with torch.cuda.stream(st.cuda):
+                        slot.d_packed[:nw].copy_(slot.h_packed[:nw], non_blocking=True)
+                        slot.d_off[:nr + 1].copy_(slot.h_off[:nr + 1], non_blocking=True)
+                    nk = c.n_kmers(self.K)
+                    st.graph.insert_device(slot.d_packed.data_ptr(), nw, slot.d_off.data_ptr(),
+                                           nr, n_kmers=nk, n_new_ptr=slot.d_new.data_ptr(),
+                                           stream=st.cuda.cuda_stream)
+                    with torch.cuda.stream(st.cuda):
+                        slot.h_new[:nr].copy_(slot.d_new[:nr], non_blocking=True)
+                        ev = torch.cuda.Event()
+                        ev.record(st.cuda)
+                    st.inflight.append((ev, st.slots.index(slot), i))
+                    st.next_chunk += 1
+                    if first_dispatch is None:
+                        first_dispatch = time.perf_counter()
+            # completions (in order per stream)
+            finished = []
+            for sid, st in active.items():
+                while st.inflight and st.inflight[0][0].query():
+                    ev, si, i = st.inflight.popleft()
+                    done = (time.perf_counter() - t0) / time_scale
+                    c = st.spec.chunks[i]
+                    slot = st.slots[si]
+                    r = ChunkResult(sid, i, c.n_reads, c.n_kmers(self.K),
+                                    slot.h_new[:c.n_reads].numpy().view(np.uint64).copy(),
+                                    st.spec.arrivals[i], done)
+                    st.results.append(r)
+                    lat.append(r.latency)
+                    total_kmers += r.n_kmers
+                    st.free.append(si)
+                    last_done = time.perf_counter()
+                if st.next_chunk == len(st.spec.chunks) and not st.inflight:
+                    finished.append(sid)
+            for sid in finished:
+                st = active.pop(sid)
+                st.graph.synchronize()
+                results[sid] = st.results
+                used -= st.need
+                del st
+        lat_ms = np.array(lat) * 1000.0 * time_scale
+        span = (last_done - first_dispatch) if first_dispatch and last_done else 0.0
+        stats = {
+            "chunks": len(lat),
+            "kmers": total_kmers,
+            "kmers_per_s": total_kmers / span if span > 0 else 0.0,
+            "p50_ms": float(np.percentile(lat_ms, 50)) if len(lat_ms) else 0.0,
+            "p99_ms": float(np.percentile(lat_ms, 99)) if len(lat_ms) else 0.0,
+            "max_ms": float(lat_ms.max()) if len(lat_ms) else 0.0,
+            "peak_hbm_bytes": peak_used,
+            "admission_waits": len(waited),
+            "wall_s": span,
+        }
+        return results, stats
+
+
+def replay(spec, storage_type=D.BitStorage, shifter_type=D.CanLemireShifter, K=31, n_tables=4):
+    """Sequential replay of one stream: its chunks inserted one after another
+    into a fresh graph (the reference's order).  Returns per-chunk n_new."""
+    storage = storage_type.build(spec.max_table, n_tables)
+    g = D.dBG[storage_type, shifter_type].build(storage, K)
+    g.set_insert_path("windowed")
+    return [g.insert_packed(c) for c in spec.chunks]
+
+
+def make_streams(n_streams, seed, reads_lo, reads_hi, chunk_lo, chunk_hi, table_lo_bits,
+                 table_hi_bits, mean_gap_s, genome_len=2_000_000, read_len=150, sub_rate=0.01,
+                 start_spread_s=1.0):
+    """Seeded serving workload: stream sizes log-uniform in [reads_lo, reads_hi],
+    chunk sizes log-uniform in [chunk_lo, chunk_hi], table sizes log-uniform
+    in [2^table_lo_bits, 2^table_hi_bits] per table, Poisson chunk arrivals
+    with mean gap mean_gap_s, stream starts uniform over start_spread_s."""
+    from . import synth
+    rng = np.random.default_rng(seed)
+    specs = []
+    for s in range(n_streams):
+        g = synth.genome(genome_len, seed * 1000 + s)
+        n_reads = int(np.exp(rng.uniform(np.log(reads_lo), np.log(reads_hi))))
+        bits = rng.uniform(table_lo_bits, table_hi_bits)
+        max_table = int(2 ** bits)
+        rows = synth.sample_reads(g, n_reads, read_len, sub_rate, seed * 7919 + s)
+        chunks, arrivals = [], []
+        t = rng.uniform(0.0, start_spread_s)
+        pos = 0
+        while pos < n_reads:
+            n = int(np.exp(rng.uniform(np.log(chunk_lo), np.log(chunk_hi))))
+            n = max(1, min(n, n_reads - pos))
+            chunks.append(synth.rows_to_packed(rows[pos:pos + n]))
+            arrivals.append(t)
+            t += rng.exponential(mean_gap_s)
+            pos += n
+        specs.append(StreamSpec(s, max_table, chunks, arrivals))
+    return specs

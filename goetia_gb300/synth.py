@@ -97,3 +97,42 @@ def list_to_packed(reads):
     if reads:
         offsets[1:] = np.cumsum([len(r) for r in reads], dtype=np.uint64)
     return PackedReads(pack_codes(flat), offsets, 0)
+
+
+def uneven_batch(genomes, abundances, n_reads, median, sigma, lo, hi, sub, ins, dele, seed):
+    """Vectorised uneven_reads: returns PackedReads directly.
+
+    Read lengths are log-normal (median, sigma) clipped to [lo, hi]; each read
+    comes from genome i with probability proportional to abundances[i], from
+    either strand; every base is independently deleted (dele), substituted
+    (sub) or followed by an inserted random base (ins)."""
+    rng = np.random.default_rng(seed)
+    w = np.asarray(abundances, float)
+    src = rng.choice(len(genomes), n_reads, p=w / w.sum())
+    lens = np.clip(np.exp(rng.normal(np.log(median), sigma, n_reads)), lo, hi).astype(np.int64)
+    glen = np.array([len(g) for g in genomes], np.int64)
+    lens = np.minimum(lens, glen[src])
+    starts = (rng.random(n_reads) * (glen[src] - lens + 1)).astype(np.int64)
+    cat = np.concatenate(genomes)
+    gbase = np.concatenate([[0], np.cumsum(glen)[:-1]])
+    total = int(lens.sum())
+    read_of = np.repeat(np.arange(n_reads), lens)
+    pos_in = np.arange(total) - np.repeat(np.cumsum(lens) - lens, lens)
+    flip = rng.random(n_reads) < 0.5
+    fr = flip[read_of]
+    src_pos = gbase[src][read_of] + starts[read_of] + np.where(fr, lens[read_of] - 1 - pos_in, pos_in)
+    bases = cat[src_pos]
+    bases = np.where(fr, 3 - bases, bases).astype(np.uint8)
+    u = rng.random(total, dtype=np.float32)
+    subm = (u >= dele) & (u < dele + sub)
+    bases[subm] = (bases[subm] + rng.integers(1, 4, int(subm.sum()), dtype=np.uint8)) & 3
+    reps = np.where(u < dele, 0, np.where(u < dele + sub + ins, np.where(u >= dele + sub, 2, 1), 1))
+    out = np.repeat(bases, reps)
+    # the second copy of each inserted base becomes a random base
+    ins_at = np.cumsum(reps)[reps == 2] - 1
+    out[ins_at] = rng.integers(0, 4, len(ins_at), dtype=np.uint8)
+    new_lens = np.add.reduceat(reps, np.cumsum(lens) - lens) if n_reads else np.zeros(0, np.int64)
+    new_lens = np.where(lens > 0, new_lens, 0)
+    offsets = np.zeros(n_reads + 1, np.uint64)
+    offsets[1:] = np.cumsum(new_lens, dtype=np.uint64)
+    return PackedReads(pack_codes(out), offsets, 0)

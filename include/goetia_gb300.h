@@ -180,12 +180,14 @@ int gdbg_neighbor_masks_batch_device(gdbg_graph* g, const uint32_t* packed,
  * 0 keeps a value. */
 int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmers_per_thread);
 /* Read-batch insert implementation; all give identical results.
- *   PERSISTENT  one cooperative launch per batch, per-k-mer table access
+ *   PERSISTENT  one cooperative launch per batch, per-k-mer table access;
+ *               its blocks wait on each other at grid barriers (bounded), so
+ *               do not run two such inserts concurrently on different streams
  *   WINDOWED    one probe and one commit launch per window
  *   BUCKETED    records partitioned by table region, each region applied in
  *               shared memory (large batches on tables far beyond L2)
  *   AUTO        BUCKETED for batches of >= 4M k-mers on >= 256 MB of tables,
- *               else PERSISTENT (default) */
+ *               else WINDOWED (default) */
 #define GDBG_PATH_PERSISTENT 0
 #define GDBG_PATH_WINDOWED 1
 #define GDBG_PATH_BUCKETED 2
