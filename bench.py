@@ -203,6 +203,67 @@ def run_serving(args, check_streams=3):
     }
 
 
+def run_masks(args, check_reads=2000):
+    """Config 4 shape: decision-node masks against a resident BitStorage, K=31.
+    Tables (4 x ~2^28 bits) are built from a 20 Mbp genome with 2,000 inserted
+    1-5 kb repeats and a 0.1% SNP haplotype; every k-mer of the query reads
+    (150 bp, sampled from both haplotypes) gets its 8-bit neighbour mask.
+    args.mask_reads query reads (the configuration's 5M by default)."""
+    import numpy as np
+    import torch
+    import goetia_gb300 as G
+    import oracle
+    from goetia_gb300 import synth
+    K = 31
+    a, b = synth.repeat_genome(20_000_000, 2000, 1000, 5000, 0.001, 11)
+    storage = G.BitStorage.build(1 << 28, 4)
+    g = G.dBG[G.BitStorage, G.CanLemireShifter].build(storage, K)
+    for hap in (a, b):
+        g.insert_packed(synth.tiles_of(hap, 100_000, K))
+    n = args.mask_reads
+    half = n // 2
+    q = np.concatenate([synth.sample_reads(a, half, 150, 0.0, 12),
+                        synth.sample_reads(b, n - half, 150, 0.0, 13)])
+    pr = synth.rows_to_packed(q)
+    nk = pr.n_kmers(K)
+    dev = torch.device("cuda", 0)
+    s = torch.cuda.Stream(dev)
+    g.set_stream(s.cuda_stream)
+    d_p = torch.from_numpy(pr.packed.view(np.int32)).to(dev)
+    d_o = torch.from_numpy(pr.offsets.view(np.int64)).to(dev)
+    d_m = torch.empty(nk, dtype=torch.uint8, device=dev)
+    for _ in range(2):
+        g.neighbor_masks_device(d_p.data_ptr(), d_p.numel(), d_o.data_ptr(), pr.n_reads,
+                                d_m.data_ptr(), n_kmers=nk, stream=s.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record(s)
+    for _ in range(reps):
+        g.neighbor_masks_device(d_p.data_ptr(), d_p.numel(), d_o.data_ptr(), pr.n_reads,
+                                d_m.data_ptr(), n_kmers=nk, stream=s.cuda_stream)
+    e1.record(s)
+    s.synchronize()
+    g.synchronize()
+    dt = e0.elapsed_time(e1) / 1000.0 / reps
+    masks = d_m.cpu().numpy()
+    lo = np.unpackbits((masks & 15)[:, None], axis=1).sum(1)
+    hi = np.unpackbits((masks >> 4)[:, None], axis=1).sum(1)
+    # bit-exact check of a sample against the oracle's walker on the same tables
+    ref = oracle.Storage("bit", storage.get_tablesizes())
+    sub_off = pr.offsets[:check_reads + 1].copy()
+    for hap in (a, b):
+        t = synth.tiles_of(hap, 100_000, K)
+        ref.insert_reads(True, K, t.packed, t.offsets)
+    want = ref.decision_masks(True, K, pr.packed, sub_off)
+    exact = bool(np.array_equal(masks[:len(want)], want))
+    return {"kmers_per_s": nk / dt, "ms_per_pass": dt * 1e3, "kmers": nk,
+            "decision_kmers": int(((lo > 1) | (hi > 1)).sum()),
+            "probe_bytes_per_kmer": 1024, "achieved_GBs_at_1024B": nk / dt * 1024 / 1e9,
+            "exact_vs_oracle_sample": exact, "oracle_sample_reads": check_reads,
+            "workload": f"{n} reads x 150 bp vs Bit 4 x ~2^28 bits built from a 20 Mbp "
+                        "genome + 2,000 1-5 kb repeats + 0.1% SNP haplotype"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -409,6 +470,9 @@ def run_gpu(args):
         "stages_ms_per_step": {k: v[0] / max(args.steps, 1) for k, v in stages.items()},
     }
 
+    mask_stats = None
+    if not args.no_masks:
+        mask_stats = run_masks(args)
     serving_stats = None
     if not args.no_serving:
         del g, g2, g3
@@ -444,6 +508,7 @@ def run_gpu(args):
                       "sample": f"{n_plain - 20} reads, one insert_sequence call each"},
             "gpu_launches": int(launches),
             "serving": serving_stats,
+            "decision_masks": mask_stats,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
@@ -468,6 +533,8 @@ def main():
     ap.add_argument("--reference-sample-reads", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-masks", action="store_true")
+    ap.add_argument("--mask-reads", type=int, default=5_000_000)
     ap.add_argument("--serve-streams", type=int, default=64)
     ap.add_argument("--serve-scale", type=float, default=0.02)
     ap.add_argument("--serve-gap", type=float, default=0.002)

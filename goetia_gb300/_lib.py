@@ -77,6 +77,7 @@ SIGNATURES = {
                                   c_u64, c_vp, c_vp, c_vp],
     "gdbg_launch_count": [c_vp, u64p],
     "gdbg_set_profiling": [c_vp, c_int],
+    "gdbg_reserve": [c_vp, c_u64, c_u64],
     "gdbg_stage_times": [c_vp, c_cp, c_u64, P(ctypes.c_double), u64p, c_u32, u32p],
 }
 

@@ -278,9 +278,11 @@ int check_device_status(gdbg_graph* g) {
 }
 
 // Per-read k-mer prefix + tile map for a device-resident batch.
+enum MapNeed { MAP_TILES = 1, MAP_TASKS = 2 };
+
 int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                   const uint64_t* offsets, uint64_t n_reads, uint64_t hint, cudaStream_t st,
-                  BatchView* view) {
+                  BatchView* view, int maps = MAP_TILES | MAP_TASKS) {
     GDBG_TRY(g->kofs.ensure(n_reads + 1));
     GDBG_TRY(g->tofs.ensure(n_reads + 1));
     GDBG_TRY(g->partials.ensure(2 * (n_reads / 1024 + 2)));
@@ -307,9 +309,14 @@ int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
     GDBG_TRY(g->tile_read.ensure(tiles + 1));
     GDBG_TRY(g->task_read.ensure(tasks + 1));
     if (total) {
-        GDBG_CUDA(launch_tile_map(g->kofs.p, n_reads, tiles, g->tile_read.p, st));
-        GDBG_CUDA(launch_task_map(g->tofs.p, n_reads, tasks, g->task_read.p, st));
-        g->launches += 2;
+        if (maps & MAP_TILES) {
+            GDBG_CUDA(launch_tile_map(g->kofs.p, n_reads, tiles, g->tile_read.p, st));
+            g->launches += 1;
+        }
+        if (maps & MAP_TASKS) {
+            GDBG_CUDA(launch_task_map(g->tofs.p, n_reads, tasks, g->task_read.p, st));
+            g->launches += 1;
+        }
     }
     view->packed = packed;
     view->offsets = offsets;
@@ -376,6 +383,21 @@ bool bucket_fits(const gdbg_graph* g, uint64_t n_kmers, uint32_t fs) {
     uint64_t cells = 0;
     for (auto p : g->sizes) cells += ((p + (1ull << fs) - 1) >> fs) << fs;
     return cells <= (1ull << 32);
+}
+
+// Read maps the batch insert will use: the windowed path walks k-mer runs
+// (tile map), the persistent and bucketed paths walk warp tasks (task map).
+int insert_maps(const gdbg_graph* g, uint64_t n_total) {
+    if (n_total == UINT64_MAX) return MAP_TILES | MAP_TASKS;
+    const uint32_t fs = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
+    uint64_t table_bytes = 0;
+    for (auto w : g->words) table_bytes += 4 * w;
+    const bool fits = bucket_fits(g, n_total, fs);
+    if (g->path == GDBG_PATH_BUCKETED && fits) return MAP_TASKS;
+    if (g->path == GDBG_PATH_AUTO && fits && table_bytes >= (256ull << 20) && n_total >= (1ull << 22))
+        return MAP_TASKS;
+    if (g->path == GDBG_PATH_PERSISTENT) return MAP_TASKS;
+    return MAP_TILES;
 }
 
 int set_error_launch(cudaError_t e, const char* what) {
@@ -620,8 +642,11 @@ int check_host_batch(const gdbg_graph* g, const uint32_t* packed, uint64_t n_wor
 }
 
 // Copy a host batch into the handle's staging buffers and prepare it.
+int insert_maps(const gdbg_graph* g, uint64_t n_total);
+
 int stage_host_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
-                     const uint64_t* offsets, uint64_t n_reads, BatchView* view) {
+                     const uint64_t* offsets, uint64_t n_reads, BatchView* view,
+                     bool for_insert = false) {
     uint64_t total = 0;
     GDBG_TRY(check_host_batch(g, packed, n_words, offsets, n_reads, &total));
     GDBG_TRY(g->st_packed.ensure(n_words + 1));
@@ -632,7 +657,7 @@ int stage_host_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
     GDBG_CUDA(cudaMemcpyAsync(g->st_offsets.p, offsets, (n_reads + 1) * sizeof(uint64_t),
                               cudaMemcpyHostToDevice, g->stream));
     return prepare_batch(g, g->st_packed.p, n_words, g->st_offsets.p, n_reads, total, g->stream,
-                         view);
+                         view, for_insert ? insert_maps(g, total) : (MAP_TILES | MAP_TASKS));
 }
 
 // Validate a string against DNA_SIMPLE and pack it as a one-read batch.
@@ -655,12 +680,13 @@ int pack_string(const char* seq, uint64_t len, std::vector<uint32_t>& packed) {
     return GDBG_OK;
 }
 
-int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view) {
+int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view,
+                 bool for_insert = false) {
     if (len < g->K) return fail(GDBG_ERR_SEQUENCE_LENGTH, "Sequence must have length >= K");
     std::vector<uint32_t> packed;
     GDBG_TRY(pack_string(seq, len, packed));
     uint64_t off[2] = {0, len};
-    return stage_host_batch(g, packed.data(), packed.size(), off, 1, view);
+    return stage_host_batch(g, packed.data(), packed.size(), off, 1, view, for_insert);
 }
 
 }  // namespace
@@ -874,7 +900,7 @@ int gdbg_insert_sequence(gdbg_graph* g, const char* seq, uint64_t len, uint64_t*
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
     GDBG_TRY(set_device(g));
     BatchView b;
-    GDBG_TRY(stage_string(g, seq, len, &b));
+    GDBG_TRY(stage_string(g, seq, len, &b, true));
     GDBG_TRY(g->st_out64.ensure(1));
     GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, sizeof(uint64_t), g->stream));
     GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, g->st_out64.p, g->stream));
@@ -980,7 +1006,7 @@ int gdbg_insert_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
     GDBG_TRY(set_device(g));
     BatchView b;
-    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b));
+    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b, true));
     GDBG_TRY(g->st_out64.ensure(n_reads + 1));
     if (n_new) GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, n_reads * sizeof(uint64_t), g->stream));
     GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, n_new ? g->st_out64.p : nullptr, g->stream));
@@ -1051,7 +1077,8 @@ int gdbg_insert_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t pac
     GDBG_TRY(set_device(g));
     cudaStream_t st = pick_stream(g, stream);
     BatchView b;
-    GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b));
+    GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b,
+                           insert_maps(g, n_kmers_hint)));
     if (n_new && n_reads) GDBG_CUDA(cudaMemsetAsync(n_new, 0, n_reads * sizeof(uint64_t), st));
     return run_insert(g, b, nullptr, b.n_kmers, n_new, st);
 }
@@ -1141,6 +1168,20 @@ int gdbg_device_status(gdbg_graph* g, uint32_t* status) {
     GDBG_TRY(set_device(g));
     GDBG_CUDA(cudaMemcpyAsync(status, g->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
     GDBG_CUDA(cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    return GDBG_OK;
+}
+
+int gdbg_reserve(gdbg_graph* g, uint64_t max_reads, uint64_t max_kmers) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    const uint64_t tasks = max_kmers / TASK_KMERS + std::min(max_reads, max_kmers);
+    GDBG_TRY(g->kofs.ensure(max_reads + 1));
+    GDBG_TRY(g->tofs.ensure(max_reads + 1));
+    GDBG_TRY(g->partials.ensure(2 * (max_reads / 1024 + 2)));
+    GDBG_TRY(g->tile_read.ensure((max_kmers + MAP_TILE - 1) / MAP_TILE + 1));
+    GDBG_TRY(g->task_read.ensure(tasks + 1));
+    GDBG_TRY(ensure_insert_scratch(g, g->stream));
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
     return GDBG_OK;
 }

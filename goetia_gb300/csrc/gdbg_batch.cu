@@ -107,6 +107,25 @@ k_prefix_final(const uint64_t* __restrict__ off, uint64_t n, uint32_t K, uint64_
     }
 }
 
+// One block does the whole prefix when the batch has at most SCAN_BLOCK reads.
+__global__ void __launch_bounds__(SCAN_BLOCK)
+k_prefix_small(const uint64_t* __restrict__ off, uint64_t n, uint32_t K, uint64_t max_bases,
+               uint64_t* __restrict__ kofs, uint64_t* __restrict__ tofs, uint32_t* err) {
+    __shared__ uint64_t ws[32], wt[32];
+    const uint64_t r = threadIdx.x;
+    ulonglong2 v = r < n ? read_counts(off, r, K, max_bases, err) : make_ulonglong2(0, 0);
+    const uint64_t s = block_inclusive_scan(v.x, ws);
+    const uint64_t t = block_inclusive_scan(v.y, wt);
+    if (r < n) {
+        kofs[r] = s - v.x;
+        tofs[r] = t - v.y;
+        if (r == n - 1) {
+            kofs[n] = s;
+            tofs[n] = t;
+        }
+    }
+}
+
 cudaError_t launch_kmer_prefix(const uint64_t* offsets, uint64_t n_reads, uint32_t K,
                                uint64_t max_bases, uint64_t* partials, uint64_t* kofs,
                                uint64_t* tofs, uint32_t* err, cudaStream_t st, int* launches) {
@@ -114,6 +133,11 @@ cudaError_t launch_kmer_prefix(const uint64_t* offsets, uint64_t n_reads, uint32
         *launches = 0;
         cudaMemsetAsync(tofs, 0, sizeof(uint64_t), st);
         return cudaMemsetAsync(kofs, 0, sizeof(uint64_t), st);
+    }
+    if (n_reads <= SCAN_BLOCK) {
+        k_prefix_small<<<1, SCAN_BLOCK, 0, st>>>(offsets, n_reads, K, max_bases, kofs, tofs, err);
+        *launches = 1;
+        return cudaGetLastError();
     }
     uint64_t nb = (n_reads + SCAN_BLOCK - 1) / SCAN_BLOCK;
     k_prefix_partials<<<(unsigned)nb, SCAN_BLOCK, 0, st>>>(offsets, n_reads, K, max_bases,

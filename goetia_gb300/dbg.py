@@ -555,6 +555,10 @@ class dBGBase:
         _lib.call("gdbg_device_status", self._h, _c.byref(s))
         return int(s.value)
 
+    def reserve(self, max_reads, max_kmers):
+        """Grow the insert scratch for batches up to this size now."""
+        _lib.call("gdbg_reserve", self._h, int(max_reads), int(max_kmers))
+
     def set_profiling(self, on=True):
         """Bracket each insert stage with CUDA events (see stage_times)."""
         _lib.call("gdbg_set_profiling", self._h, 1 if on else 0)

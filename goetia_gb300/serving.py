@@ -88,10 +88,8 @@ class _Stream:
         self.results = []
         # grow the graph's scratch to the largest chunk now, so no device
         # allocation (and its device-wide synchronisation) happens while
-        # serving; the tables are zeroed again afterwards
-        big = max(spec.chunks, key=lambda c: c.n_kmers(server.K))
-        self.graph.insert_packed(big)
-        self.graph.reset()
+        # serving
+        self.graph.reserve(max_reads, max(c.n_kmers(server.K) for c in spec.chunks))
 
     def table_bytes(self):
         return sum(self.graph.table_bytes())

@@ -136,3 +136,31 @@ def uneven_batch(genomes, abundances, n_reads, median, sigma, lo, hi, sub, ins, 
     offsets = np.zeros(n_reads + 1, np.uint64)
     offsets[1:] = np.cumsum(new_lens, dtype=np.uint64)
     return PackedReads(pack_codes(out), offsets, 0)
+
+
+def repeat_genome(n, n_repeats, rep_lo, rep_hi, snp_rate, seed):
+    """A genome with inserted repeats plus a SNP haplotype (decision-node
+    workload): n random bases, n_repeats copies of random 1-5 kb segments
+    pasted at random positions, and a second haplotype with i.i.d. SNPs at
+    snp_rate.  Returns (haplotype_a, haplotype_b) as code arrays."""
+    rng = np.random.default_rng(seed)
+    g = rng.integers(0, 4, n, dtype=np.uint8)
+    for _ in range(n_repeats):
+        L = int(rng.integers(rep_lo, rep_hi + 1))
+        src = int(rng.integers(0, n - L))
+        dst = int(rng.integers(0, n - L))
+        g[dst:dst + L] = g[src:src + L].copy()
+    h = g.copy()
+    k = rng.binomial(n, snp_rate)
+    idx = rng.integers(0, n, k)
+    h[idx] = (h[idx] + rng.integers(1, 4, k, dtype=np.uint8)) & 3
+    return g, h
+
+
+def tiles_of(seq, tile, K):
+    """Cut a long sequence into reads of `tile` bases overlapping by K-1, so
+    every k-mer of seq is in exactly one read."""
+    step = tile - (K - 1)
+    starts = np.arange(0, max(len(seq) - K + 1, 1), step)
+    reads = [seq[s:s + tile] for s in starts]
+    return list_to_packed(reads)

@@ -200,6 +200,10 @@ int gdbg_get_insert_schedule(const gdbg_graph* g, uint32_t* window_kmers,
                              uint32_t* kmers_per_thread);
 /* Device status word (GDBG_ERR_* device bits); cleared by reading. */
 int gdbg_device_status(gdbg_graph* g, uint32_t* status);
+/* Grow the graph's batch and windowed-insert scratch for batches of up to
+ * max_reads reads and max_kmers k-mers now, so later inserts within that
+ * size allocate nothing. */
+int gdbg_reserve(gdbg_graph* g, uint64_t max_reads, uint64_t max_kmers);
 /* Per-stage timing: when on, every stage of a batch insert is bracketed by
  * CUDA events on its stream.  gdbg_stage_times synchronises, returns the
  * accumulated milliseconds and launch counts per stage (names comma-separated
