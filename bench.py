@@ -264,6 +264,72 @@ def run_masks(args, check_reads=2000):
                         "genome + 2,000 1-5 kb repeats + 0.1% SNP haplotype"}
 
 
+def run_batched(args, check_reads=300):
+    """Config 3 shape: uneven-length batched insert into
+    dBG<NibbleStorage, FwdLemireShifter>, K=21, 4 tables of ~2^28 cells.
+    Reads: log-normal lengths (median 4 kb, clipped 200 bp-60 kb) from 5
+    random 10 Mbp genomes at abundances 1:2:4:8:16, 4% substitutions, 2%
+    insertions, 2% deletions; args.batched_reads of the configuration's 2M
+    reads.  Batches are replayed through a CUDA graph with the autotuned
+    capacity and schedule; the plain per-read call is timed on a sample of
+    the same reads."""
+    import numpy as np
+    import goetia_gb300 as G
+    import oracle
+    from goetia_gb300 import batched, synth
+    K = 21
+    gens = [synth.genome(10_000_000, 5 + i) for i in range(5)]
+    parts = []
+    per = 8000
+    for i in range(0, args.batched_reads, per):
+        parts.append(synth.uneven_batch(gens, [1, 2, 4, 8, 16], min(per, args.batched_reads - i),
+                                        4000, 1.0, 200, 60_000, 0.04, 0.02, 0.02, 10 + i))
+    from goetia_gb300.reads import concat
+    reads = concat(parts)
+    nk = reads.n_kmers(K)
+    storage = G.NibbleStorage.build(1 << 28, 4)
+    g = G.dBG[G.NibbleStorage, G.FwdLemireShifter].build(storage, K)
+    caps = [(2048, 16 << 20), (8192, 64 << 20), (16384, 128 << 20)]
+    cap, tuned = batched.autotune_capacity(g, reads, caps)
+    ins = batched.BatchedInserter(g, cap[0], cap[1], use_graph=True).prepare()
+    bat = batched.split_batches(reads, cap[0], cap[1])
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n_new = np.zeros(reads.n_reads, np.uint64)
+    for r0, b in bat:
+        n_new[r0:r0 + b.n_reads] = ins.insert(b)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    # exactness: the first reads against the oracle from empty tables
+    first = bat[0][1]
+    sub = G.PackedReads(first.packed, first.offsets[:min(check_reads, first.n_reads) + 1].copy())
+    ref = oracle.Storage("nibble", storage.get_tablesizes())
+    _, want = ref.insert_reads(False, K, sub.packed, sub.offsets)
+    exact = bool(np.array_equal(n_new[:sub.n_reads], want))
+    # plain: one insert_sequence call per read on a fresh graph
+    gp = G.dBG[G.NibbleStorage, G.FwdLemireShifter].build(storage, K)
+    from goetia_gb300.reads import codes_to_str
+    sample = []
+    j_all = np.arange(int(first.offsets[min(40, first.n_reads)]))
+    codes = ((first.packed[j_all >> 4] >> (2 * (j_all & 15)).astype(np.uint32)) & 3).astype(np.uint8)
+    for r in range(min(40, first.n_reads)):
+        sample.append(codes_to_str(codes[int(first.offsets[r]):int(first.offsets[r + 1])]).encode())
+    gp.insert_sequence(sample[0])
+    t0 = time.perf_counter()
+    pk = 0
+    for sq in sample[1:]:
+        pk += gp.insert_sequence(sq)
+    plain = pk / (time.perf_counter() - t0)
+    return {"kmers_per_s": nk / dt, "kmers": nk, "reads": reads.n_reads, "seconds": dt,
+            "batches": len(bat), "capacity_reads_bases": list(cap),
+            "schedule": tuned["schedule"], "cuda_graph": ins.cuda_graph is not None,
+            "plain_kmers_per_s": plain, "batched_over_plain": (nk / dt) / plain,
+            "exact_vs_oracle_first_reads": exact, "oracle_checked_reads": sub.n_reads,
+            "workload": f"{reads.n_reads} of the 2M uneven reads (median 4 kb, 200 bp-60 kb), "
+                        "5 x 10 Mbp genomes 1:2:4:8:16, 8% errors; Nibble 4 x ~2^28 cells, K=21"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -470,6 +536,9 @@ def run_gpu(args):
         "stages_ms_per_step": {k: v[0] / max(args.steps, 1) for k, v in stages.items()},
     }
 
+    batched_stats = None
+    if not args.no_batched:
+        batched_stats = run_batched(args)
     mask_stats = None
     if not args.no_masks:
         mask_stats = run_masks(args)
@@ -509,6 +578,7 @@ def run_gpu(args):
             "gpu_launches": int(launches),
             "serving": serving_stats,
             "decision_masks": mask_stats,
+            "batched_uneven": batched_stats,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
@@ -534,6 +604,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-masks", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-reads", type=int, default=32_000)
     ap.add_argument("--mask-reads", type=int, default=5_000_000)
     ap.add_argument("--serve-streams", type=int, default=64)
     ap.add_argument("--serve-scale", type=float, default=0.02)

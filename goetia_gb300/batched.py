@@ -254,3 +254,24 @@ def autotune(graph, sample, max_reads, max_bases, repeats=2, use_cache=True, ver
             json.dump(cache, f, indent=1)
         os.replace(tmp, path)
     return best
+
+
+def autotune_capacity(graph, reads, capacities, use_graph=True, verbose=False):
+    """Pick the batch capacity (reads, bases) -- the chunk size -- and, for it,
+    the schedule, by timing the insert of the first batch of `reads` at each
+    capacity on scratch clones.  Returns (capacity, best)."""
+    best = None
+    for cap in capacities:
+        parts = split_batches(reads, cap[0], cap[1])
+        if not parts:
+            continue
+        sample = parts[0][1]
+        res = autotune(graph.clone(), sample, cap[0], cap[1], use_cache=False, verbose=verbose,
+                       use_graph=use_graph)
+        rate = sample.n_kmers(graph.K) / res["seconds"]
+        if verbose:
+            print("capacity", cap, f"{rate / 1e9:.2f} G k-mers/s")
+        if best is None or rate > best[2]:
+            best = (cap, res, rate)
+    apply_schedule(graph, best[1]["schedule"])
+    return best[0], best[1]

@@ -84,3 +84,26 @@ def codes_to_str(codes):
 def str_to_codes(s):
     t = {"A": 0, "C": 1, "G": 2, "T": 3}
     return np.array([t[c] for c in s], np.uint8)
+
+
+def concat(parts):
+    """One contiguous PackedReads from several (bases re-aligned by shifting
+    each part's words to where the previous part ended)."""
+    total = sum(int(p.offsets[-1]) for p in parts)
+    out = np.zeros(total // 16 + 2, np.uint64)
+    offs = [np.zeros(1, np.uint64)]
+    B = 0
+    for p in parts:
+        nb = int(p.offsets[-1])
+        nw = (nb + 15) // 16
+        if nw:
+            words = p.packed[:nw].astype(np.uint64)
+            if nb % 16:   # clear bits past the part's last base
+                words[-1] &= np.uint64((1 << (2 * (nb % 16))) - 1)
+            w, sh = B // 16, 2 * (B % 16)
+            out[w:w + nw] |= (words << np.uint64(sh)) & np.uint64(0xFFFFFFFF)
+            if sh:
+                out[w + 1:w + 1 + nw] |= words >> np.uint64(32 - sh)
+        offs.append(p.offsets[1:].astype(np.uint64) + np.uint64(B))
+        B += nb
+    return PackedReads(out.astype(np.uint32), np.concatenate(offs))
