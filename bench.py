@@ -195,6 +195,9 @@ def run_serving(args, check_streams=3):
         "wall_s": stats["wall_s"], "offered_kmers": offered,
         "peak_hbm_GB": stats["peak_hbm_bytes"] / (1 << 30),
         "admission_waits": stats["admission_waits"],
+        "lazy_frees": stats["lazy_frees"],
+        "host": {k: stats[k] for k in ("admit_ms_max", "admit_ms_total", "dispatch_ms_p99",
+                                       "dispatch_delay_ms_p99")},
         "hbm_budget_GB": args.serve_budget_gb,
         "exact_vs_sequential_replay": bool(exact), "replay_checked_streams": check_streams,
         "workload": (f"64 streams, reads 10k-5M x {sc} log-uniform, chunks 8-4096 reads, "
@@ -308,7 +311,7 @@ def run_batched(args, check_reads=300):
     _, want = ref.insert_reads(False, K, sub.packed, sub.offsets)
     exact = bool(np.array_equal(n_new[:sub.n_reads], want))
     # plain: one insert_sequence call per read on a fresh graph
-    gp = G.dBG[G.NibbleStorage, G.FwdLemireShifter].build(storage, K)
+    gp = g.clone()
     from goetia_gb300.reads import codes_to_str
     sample = []
     j_all = np.arange(int(first.offsets[min(40, first.n_reads)]))
@@ -457,7 +460,7 @@ def run_gpu(args):
     value = total_kmers / dt
 
     # e2e: host-buffer C-ABI call on a fresh graph, copies inside the timed region
-    g2 = Graph.build(storage, K)
+    g2 = g.clone()
     if args.window:
         g2.set_insert_schedule(args.window, args.kpt)
     pinned = []
@@ -502,7 +505,7 @@ def run_gpu(args):
 
     # plain drop-in: one insert_sequence call per read
     from goetia_gb300.reads import codes_to_str
-    g3 = Graph.build(storage, K)
+    g3 = g.clone()
     pr0 = batches[0]
     n_plain = min(args.plain_reads, pr0.n_reads)
     j = np.arange(int(pr0.offsets[n_plain]))

@@ -41,6 +41,7 @@ SIGNATURES = {
     "gdbg_create_sized": [c_int, c_int, c_u16, u64p, c_u16, P(c_vp)],
     "gdbg_destroy": [c_vp],
     "gdbg_clone": [c_vp, P(c_vp)],
+    "gdbg_share_storage": [c_vp, c_int, c_u16, P(c_vp)],
     "gdbg_reset": [c_vp],
     "gdbg_info": [c_vp, intp, intp, u16p, u16p],
     "gdbg_get_tablesizes": [c_vp, u64p],
@@ -48,11 +49,15 @@ SIGNATURES = {
     "gdbg_get_tables": [c_vp, u8p, c_u64],
     "gdbg_set_tables": [c_vp, u8p, c_u64],
     "gdbg_stats": [c_vp, u64p, u64p],
+    "gdbg_save": [c_vp, c_cp],
+    "gdbg_load": [c_vp, c_cp, u16p],
+    "gdbg_update_from": [c_vp, c_vp],
     "gdbg_set_stream": [c_vp, c_vp],
     "gdbg_synchronize": [c_vp],
     "gdbg_hash": [c_vp, c_cp, c_u64, u64p, u64p, u64p],
     "gdbg_insert_sequence": [c_vp, c_cp, c_u64, u64p, u64p],
     "gdbg_query_sequence": [c_vp, c_cp, c_u64, i16p, u64p],
+    "gdbg_insert_and_query_sequence": [c_vp, c_cp, c_u64, i16p, u64p],
     "gdbg_hashes": [c_vp, c_cp, c_u64, u64p, u64p, u64p],
     "gdbg_insert_hashes": [c_vp, u64p, c_u64, u8p],
     "gdbg_query_hashes": [c_vp, u64p, c_u64, i16p],
@@ -61,10 +66,13 @@ SIGNATURES = {
     "gdbg_pack_codes": [u8p, c_u64, u32p],
     "gdbg_insert_batch": [c_vp, u32p, c_u64, u64p, c_u64, u64p, u64p],
     "gdbg_query_batch": [c_vp, u32p, c_u64, u64p, c_u64, i16p],
+    "gdbg_insert_and_query_batch": [c_vp, u32p, c_u64, u64p, c_u64, i16p, u64p],
     "gdbg_hashes_batch": [c_vp, u32p, c_u64, u64p, c_u64, u64p, u64p, u64p],
     "gdbg_neighbor_masks_batch": [c_vp, u32p, c_u64, u64p, c_u64, u8p],
     "gdbg_insert_batch_device": [c_vp, c_vp, c_u64, c_vp, c_u64, c_u64, c_vp, c_vp],
     "gdbg_query_batch_device": [c_vp, c_vp, c_u64, c_vp, c_u64, c_u64, c_vp, c_vp],
+    "gdbg_insert_and_query_batch_device": [c_vp, c_vp, c_u64, c_vp, c_u64, c_u64, c_vp, c_vp,
+                                           c_vp],
     "gdbg_hashes_batch_device": [c_vp, c_vp, c_u64, c_vp, c_u64, c_u64, c_vp, c_vp, c_vp, c_vp],
     "gdbg_neighbor_masks_batch_device": [c_vp, c_vp, c_u64, c_vp, c_u64, c_u64, c_vp, c_vp],
     "gdbg_set_insert_schedule": [c_vp, c_u32, c_u32],
@@ -100,6 +108,11 @@ class InvalidSequenceException(GoetiaError, ValueError):
     """Symbol outside DNA_SIMPLE, or a k-mer shorter than K (alphabets.hh:41-56)."""
 
 
+class GoetiaFileException(GoetiaError, OSError):
+    """Table file missing, truncated or of the wrong kind (goetia.hh
+    GoetiaFileException, raised by Storage::load, bitstorage.cc:188-307)."""
+
+
 def load():
     """Load the in-tree shared library (build it with goetia_gb300.build first)."""
     global _lib
@@ -131,6 +144,8 @@ def check(rc):
         raise InvalidSequenceException(rc, msg)
     if rc == ERR_OOM:
         raise MemoryError(msg)
+    if rc == ERR_IO:
+        raise GoetiaFileException(rc, msg)
     raise GoetiaError(rc, msg)
 
 

@@ -6,8 +6,10 @@
 // staging buffers for the host-pointer entry points.  All device work of a
 // handle runs on its stream in submission order.
 #include <algorithm>
+#include <cerrno>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -84,17 +86,32 @@ uint32_t next_pow2(uint64_t x) {
 
 int gdbg::report_error(int code, const std::string& msg) { return fail(code, msg); }
 
-struct gdbg_graph {
-    int storage = 0, shifter = 0;
-    uint16_t K = 0;
+// The storage proper: one device allocation holding every table (each padded
+// to 256 bytes), the table sizes, the kernel-side table parameters and the
+// n_unique / n_occupied counters.  Handles made by gdbg_share_storage point to
+// the same store, the way dBGs built on one Storage share its shared_ptr
+// (dbg.hh:97-101); it is freed with the last handle.
+struct TableStore {
     int device = 0;
     std::vector<uint64_t> sizes, bytes, word_off, words;
     uint32_t* d_tables = nullptr;
     uint64_t total_words = 0;
     TableParams tp{};
+    unsigned long long* d_counters = nullptr;  // [0] n_unique, [1] n_occupied
+    ~TableStore() {
+        cudaSetDevice(device);
+        if (d_tables) cudaFree(d_tables);
+        if (d_counters) cudaFree(d_counters);
+    }
+};
+
+struct gdbg_graph {
+    int storage = 0, shifter = 0;
+    uint16_t K = 0;
+    int device = 0;
+    std::shared_ptr<TableStore> ts;   // tables and counters, shared by gdbg_share_storage
     HashParams hp{};
     cudaStream_t own_stream = nullptr, stream = nullptr;
-    unsigned long long* d_counters = nullptr;  // [0] n_unique, [1] n_occupied
     uint32_t* d_err = nullptr;
     // insert scratch
     uint32_t window = 262144, kpt = 4;
@@ -109,6 +126,7 @@ struct gdbg_graph {
     uint32_t bucket_fs = 0;   // 0 = default for the storage kind
     DevBuf<uint64_t> rec_a, rec_b;
     DevBuf<uint32_t> hist, hist_off, scan_parts, bstart, new_bits;
+    DevBuf<uint8_t> iq_vals;    // insert_and_query: post-insert value per table and k-mer
     uint32_t* d_epoch = nullptr;
     unsigned int* d_bar = nullptr;
     bool epoch_on_device = false;
@@ -130,7 +148,7 @@ struct gdbg_graph {
     std::vector<std::pair<std::string, std::pair<double, uint64_t>>> stage_acc;
 
     LaunchShape shape(int kpt_) const {
-        return LaunchShape{shifter == GDBG_CAN_LEMIRE, kpt_, (int)sizes.size()};
+        return LaunchShape{shifter == GDBG_CAN_LEMIRE, kpt_, (int)ts->sizes.size()};
     }
 };
 
@@ -197,15 +215,73 @@ cudaStream_t pick_stream(gdbg_graph* g, void* s) {
     return s ? (cudaStream_t)s : g->stream;
 }
 
-int make_graph(int storage, int shifter, uint16_t K, const uint64_t* sizes, uint16_t n,
-               gdbg_graph** out) {
-    if (!out) return fail(GDBG_ERR_INVALID_ARG, "out is NULL");
-    *out = nullptr;
+// Table layout in the single device allocation: table i holds its reference
+// byte length (size/8+1, size, size/2+1 for Bit, Byte, Nibble) padded up to
+// 256 bytes, at word offset word_off[i].  Returns the total in 32-bit words.
+uint64_t table_layout(int storage, const uint64_t* sizes, uint16_t n, std::vector<uint64_t>& sz,
+                      std::vector<uint64_t>& bytes, std::vector<uint64_t>& words,
+                      std::vector<uint64_t>& word_off) {
+    sz.clear(); bytes.clear(); words.clear(); word_off.clear();
+    uint64_t off = 0;
+    for (uint16_t i = 0; i < n; ++i) {
+        uint64_t p = sizes[i];
+        uint64_t b = storage == GDBG_BIT ? p / 8 + 1 : storage == GDBG_NIBBLE ? p / 2 + 1 : p;
+        uint64_t w = ((b + 3) / 4 + 63) / 64 * 64;
+        sz.push_back(p);
+        bytes.push_back(b);
+        words.push_back(w);
+        word_off.push_back(off);
+        off += w;
+    }
+    return off;
+}
+
+// Kernel-side table parameters (base pointers, sizes, fastmod magics).
+void set_table_params(gdbg_graph* g) {
+    const size_t n = g->ts->sizes.size();
+    for (size_t i = 0; i < n; ++i) {
+        g->ts->tp.words[i] = g->ts->d_tables + g->ts->word_off[i];
+        g->ts->tp.p[i] = g->ts->sizes[i];
+        g->ts->tp.m[i] = ~0ull / g->ts->sizes[i];
+    }
+    g->ts->tp.n = (int)n;
+}
+
+// Per-handle state: stream, status word, claims epoch, grid barrier and the
+// hash constants for K.  The tables come from g->ts.
+int init_handle(gdbg_graph* g, int storage, int shifter, uint16_t K) {
+    g->storage = storage;
+    g->shifter = shifter;
+    g->K = K;
+    if (cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(GDBG_ERR_CUDA, "cudaStreamCreate failed");
+    g->stream = g->own_stream;
+    if (cudaMalloc((void**)&g->d_err, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&g->d_epoch, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&g->d_bar, 2 * sizeof(unsigned int)) != cudaSuccess)
+        return fail(GDBG_ERR_OOM, "counter allocation failed");
+    cudaMemsetAsync(g->d_epoch, 0, sizeof(uint32_t), g->stream);
+    cudaMemsetAsync(g->d_bar, 0, 2 * sizeof(unsigned int), g->stream);
+    cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
+    g->hp.K = K;
+    for (int c = 0; c < 4; ++c) g->hp.tk[c] = host_rotl(HSYM[c], K % 64u);
+    return GDBG_OK;
+}
+
+int check_kinds(int storage, int shifter, uint16_t K) {
     if (storage < GDBG_BIT || storage > GDBG_NIBBLE)
         return fail(GDBG_ERR_INVALID_ARG, "unknown storage kind");
     if (shifter != GDBG_FWD_LEMIRE && shifter != GDBG_CAN_LEMIRE)
         return fail(GDBG_ERR_INVALID_ARG, "unknown shifter kind");
     if (K == 0) return fail(GDBG_ERR_INVALID_ARG, "K must be positive");
+    return GDBG_OK;
+}
+
+int make_graph(int storage, int shifter, uint16_t K, const uint64_t* sizes, uint16_t n,
+               gdbg_graph** out) {
+    if (!out) return fail(GDBG_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    GDBG_TRY(check_kinds(storage, shifter, K));
     if (n == 0 || n > MAX_TABLES)
         return fail(GDBG_ERR_INVALID_ARG, "n_tables must be in 1..32");
     for (uint16_t i = 0; i < n; ++i)
@@ -213,49 +289,24 @@ int make_graph(int storage, int shifter, uint16_t K, const uint64_t* sizes, uint
             return fail(GDBG_ERR_INVALID_ARG, "table sizes must be in 1..2^32-1 cells");
 
     gdbg_graph* g = new gdbg_graph();
-    g->storage = storage;
-    g->shifter = shifter;
-    g->K = K;
     cudaGetDevice(&g->device);
-    uint64_t off = 0;
-    for (uint16_t i = 0; i < n; ++i) {
-        uint64_t p = sizes[i];
-        uint64_t b = storage == GDBG_BIT ? p / 8 + 1 : storage == GDBG_NIBBLE ? p / 2 + 1 : p;
-        uint64_t w = ((b + 3) / 4 + 63) / 64 * 64;  // 256-byte padded
-        g->sizes.push_back(p);
-        g->bytes.push_back(b);
-        g->words.push_back(w);
-        g->word_off.push_back(off);
-        off += w;
-    }
-    g->total_words = off;
+    g->ts = std::make_shared<TableStore>();
+    g->ts->device = g->device;
     auto cleanup = [&](int rc) { gdbg_destroy(g); return rc; };
-    cudaError_t e = cudaMalloc((void**)&g->d_tables, off * sizeof(uint32_t));
+    const int rc = init_handle(g, storage, shifter, K);
+    if (rc != GDBG_OK) return cleanup(rc);
+    const uint64_t off = table_layout(storage, sizes, n, g->ts->sizes, g->ts->bytes, g->ts->words, g->ts->word_off);
+    g->ts->total_words = off;
+    cudaError_t e = cudaMalloc((void**)&g->ts->d_tables, off * sizeof(uint32_t));
     if (e != cudaSuccess) {
-        g->d_tables = nullptr;
+        g->ts->d_tables = nullptr;
         return cleanup(fail(GDBG_ERR_OOM, std::string("table allocation: ") + cudaGetErrorString(e)));
     }
-    if (cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking) != cudaSuccess)
-        return cleanup(fail(GDBG_ERR_CUDA, "cudaStreamCreate failed"));
-    g->stream = g->own_stream;
-    if (cudaMalloc((void**)&g->d_counters, 2 * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMalloc((void**)&g->d_err, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc((void**)&g->d_epoch, sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc((void**)&g->d_bar, 2 * sizeof(unsigned int)) != cudaSuccess)
+    if (cudaMalloc((void**)&g->ts->d_counters, 2 * sizeof(unsigned long long)) != cudaSuccess)
         return cleanup(fail(GDBG_ERR_OOM, "counter allocation failed"));
-    cudaMemsetAsync(g->d_epoch, 0, sizeof(uint32_t), g->stream);
-    cudaMemsetAsync(g->d_bar, 0, 2 * sizeof(unsigned int), g->stream);
-    cudaMemsetAsync(g->d_tables, 0, off * sizeof(uint32_t), g->stream);
-    cudaMemsetAsync(g->d_counters, 0, 2 * sizeof(unsigned long long), g->stream);
-    cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
-    for (uint16_t i = 0; i < n; ++i) {
-        g->tp.words[i] = g->d_tables + g->word_off[i];
-        g->tp.p[i] = sizes[i];
-        g->tp.m[i] = ~0ull / sizes[i];
-    }
-    g->tp.n = n;
-    g->hp.K = K;
-    for (int c = 0; c < 4; ++c) g->hp.tk[c] = host_rotl(HSYM[c], K % 64u);
+    cudaMemsetAsync(g->ts->d_tables, 0, off * sizeof(uint32_t), g->stream);
+    cudaMemsetAsync(g->ts->d_counters, 0, 2 * sizeof(unsigned long long), g->stream);
+    set_table_params(g);
     e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) return cleanup(fail(GDBG_ERR_CUDA, cudaGetErrorString(e)));
     *out = g;
@@ -332,7 +383,7 @@ int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
 }
 
 int ensure_insert_scratch(gdbg_graph* g, cudaStream_t st) {
-    const uint64_t W = g->window, n = g->sizes.size();
+    const uint64_t W = g->window, n = g->ts->sizes.size();
     GDBG_TRY(g->fresh.ensure(W));
     if (g->storage != GDBG_BIT) GDBG_TRY(g->words_seen.ensure(W * n));
     uint32_t slots = next_pow2(2 * W * n);
@@ -360,9 +411,9 @@ int launch_pass(gdbg_graph* g, int pass, const LaunchShape& s, uint64_t n_thread
                 const BatchView& b, const uint64_t* hashes, const WindowParams& w) {
     cudaError_t e;
     switch (g->storage) {
-    case GDBG_BIT: e = launch_insert_pass<GDBG_BIT>(pass, s, n_threads, st, b, hashes, g->hp, g->tp, w); break;
-    case GDBG_BYTE: e = launch_insert_pass<GDBG_BYTE>(pass, s, n_threads, st, b, hashes, g->hp, g->tp, w); break;
-    default: e = launch_insert_pass<GDBG_NIBBLE>(pass, s, n_threads, st, b, hashes, g->hp, g->tp, w); break;
+    case GDBG_BIT: e = launch_insert_pass<GDBG_BIT>(pass, s, n_threads, st, b, hashes, g->hp, g->ts->tp, w); break;
+    case GDBG_BYTE: e = launch_insert_pass<GDBG_BYTE>(pass, s, n_threads, st, b, hashes, g->hp, g->ts->tp, w); break;
+    default: e = launch_insert_pass<GDBG_NIBBLE>(pass, s, n_threads, st, b, hashes, g->hp, g->ts->tp, w); break;
     }
     if (e != cudaSuccess) return fail(GDBG_ERR_CUDA, std::string("insert launch: ") + cudaGetErrorString(e));
     g->launches += 1;
@@ -377,11 +428,11 @@ uint32_t default_bucket_fs(int storage) {
 // Can the bucketed path take this batch?  (tables <= 8, every global cell id
 // and every record index below 2^32)
 bool bucket_fits(const gdbg_graph* g, uint64_t n_kmers, uint32_t fs) {
-    const uint64_t n = g->sizes.size();
+    const uint64_t n = g->ts->sizes.size();
     if (n > (uint64_t)BK_MAXNT || n_kmers == 0) return false;
     if (n_kmers * n >= (1ull << 32)) return false;
     uint64_t cells = 0;
-    for (auto p : g->sizes) cells += ((p + (1ull << fs) - 1) >> fs) << fs;
+    for (auto p : g->ts->sizes) cells += ((p + (1ull << fs) - 1) >> fs) << fs;
     return cells <= (1ull << 32);
 }
 
@@ -391,7 +442,7 @@ int insert_maps(const gdbg_graph* g, uint64_t n_total) {
     if (n_total == UINT64_MAX) return MAP_TILES | MAP_TASKS;
     const uint32_t fs = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
     uint64_t table_bytes = 0;
-    for (auto w : g->words) table_bytes += 4 * w;
+    for (auto w : g->ts->words) table_bytes += 4 * w;
     const bool fits = bucket_fits(g, n_total, fs);
     if (g->path == GDBG_PATH_BUCKETED && fits) return MAP_TASKS;
     if (g->path == GDBG_PATH_AUTO && fits && table_bytes >= (256ull << 20) && n_total >= (1ull << 22))
@@ -406,8 +457,11 @@ int set_error_launch(cudaError_t e, const char* what) {
 
 // Bucketed insert of a read batch: partition the (cell, k-mer) records by
 // table region, then apply each region in shared memory.
-int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaStream_t st) {
-    const uint64_t nk = b.n_kmers, n = g->sizes.size();
+// counts != nullptr: also the insert_and_query count of every k-mer
+// (Byte/Nibble; Bit callers fill ones themselves).
+int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaStream_t st,
+                        int16_t* counts = nullptr) {
+    const uint64_t nk = b.n_kmers, n = g->ts->sizes.size();
     if (nk == 0) {
         if (n_new && b.n_reads) GDBG_CUDA(cudaMemsetAsync(n_new, 0, b.n_reads * sizeof(uint64_t), st));
         return GDBG_OK;
@@ -419,8 +473,8 @@ int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cuda
     for (uint64_t i = 0; i < n; ++i) {
         bp.bbase[i] = nb;
         bp.tbase[i] = (uint64_t)nb << fs;
-        bp.twords[i] = (uint32_t)g->words[i];
-        nb += (uint32_t)((g->sizes[i] + (1ull << fs) - 1) >> fs);
+        bp.twords[i] = (uint32_t)g->ts->words[i];
+        nb += (uint32_t)((g->ts->sizes[i] + (1ull << fs) - 1) >> fs);
     }
     bp.bbase[n] = nb;
     bp.n_buckets = nb;
@@ -450,7 +504,7 @@ int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cuda
     bp.rout = g->rec_a.p;
     {
         Stage sg(g, "k_bkt_emit", st);
-        if ((e = launch_bucket_emit(canon, st, b, g->hp, g->tp, bp)) != cudaSuccess)
+        if ((e = launch_bucket_emit(canon, st, b, g->hp, g->ts->tp, bp)) != cudaSuccess)
             return set_error_launch(e, "bucket emit");
     }
     uint64_t* src = g->rec_a.p;
@@ -483,11 +537,22 @@ int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cuda
     if ((e = launch_bucket_starts_fix(st, bp, g->bstart.p)) != cudaSuccess)
         return set_error_launch(e, "bucket starts");
     g->launches += 2;
+    uint8_t* vals = nullptr;
+    if (counts && g->storage != GDBG_BIT) {
+        GDBG_TRY(g->iq_vals.ensure(n * nk));
+        vals = g->iq_vals.p;
+    }
     Stage sg_apply(g, "k_bkt_apply", st);
-    if ((e = launch_bucket_apply(g->storage, g->tp, bp, src, g->bstart.p, g->new_bits.p,
-                                 g->d_counters, st)) != cudaSuccess)
+    if ((e = launch_bucket_apply(g->storage, g->ts->tp, bp, src, g->bstart.p, g->new_bits.p,
+                                 g->ts->d_counters, vals, st)) != cudaSuccess)
         return set_error_launch(e, "bucket apply");
-    if ((e = launch_bucket_read_new(b.kofs, b.n_reads, g->new_bits.p, n_new, g->d_counters, st)) != cudaSuccess)
+    if (vals) {
+        if ((e = launch_iq_counts(vals, nk, (uint32_t)n, g->new_bits.p, bp.total_kmers, counts,
+                                  false, st)) != cudaSuccess)
+            return set_error_launch(e, "insert_and_query counts");
+        g->launches += 1;
+    }
+    if ((e = launch_bucket_read_new(b.kofs, b.n_reads, g->new_bits.p, n_new, g->ts->d_counters, st)) != cudaSuccess)
         return set_error_launch(e, "bucket read counts");
     g->launches += 3;
     return GDBG_OK;
@@ -496,7 +561,7 @@ int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cuda
 // Persistent cooperative insert of a read batch (one launch per batch).
 int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaStream_t st) {
     if (b.n_kmers == 0 || b.task_cap == 0) return GDBG_OK;
-    const uint64_t W = g->pwindow, n = g->sizes.size();
+    const uint64_t W = g->pwindow, n = g->ts->sizes.size();
     GDBG_TRY(g->fresh.ensure(W));
     if (g->storage != GDBG_BIT) GDBG_TRY(g->words_seen.ensure(W * n));
     const uint32_t slots = next_pow2(W * n + W * n / 4);
@@ -523,7 +588,7 @@ int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cu
     pp.claims_mask = slots - 1;
     pp.epoch_state = g->d_epoch;
     pp.n_new = (unsigned long long*)n_new;
-    pp.counters = g->d_counters;
+    pp.counters = g->ts->d_counters;
     pp.err = g->d_err;
     pp.bar = g->d_bar;
     LaunchShape s = g->shape(4);
@@ -531,9 +596,9 @@ int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cu
     cudaError_t e;
     Stage sg(g, "k_insert_persistent", st);
     switch (g->storage) {
-    case GDBG_BIT: e = launch_insert_persistent<GDBG_BIT>(s, b.task_cap, st, b, g->hp, g->tp, pp, &grid); break;
-    case GDBG_BYTE: e = launch_insert_persistent<GDBG_BYTE>(s, b.task_cap, st, b, g->hp, g->tp, pp, &grid); break;
-    default: e = launch_insert_persistent<GDBG_NIBBLE>(s, b.task_cap, st, b, g->hp, g->tp, pp, &grid); break;
+    case GDBG_BIT: e = launch_insert_persistent<GDBG_BIT>(s, b.task_cap, st, b, g->hp, g->ts->tp, pp, &grid); break;
+    case GDBG_BYTE: e = launch_insert_persistent<GDBG_BYTE>(s, b.task_cap, st, b, g->hp, g->ts->tp, pp, &grid); break;
+    default: e = launch_insert_persistent<GDBG_NIBBLE>(s, b.task_cap, st, b, g->hp, g->ts->tp, pp, &grid); break;
     }
     if (e != cudaSuccess)
         return fail(GDBG_ERR_CUDA, std::string("persistent insert launch: ") + cudaGetErrorString(e));
@@ -548,7 +613,7 @@ int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64
     if (!hashes) {
         const uint32_t fs = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
         uint64_t table_bytes = 0;
-        for (auto w : g->words) table_bytes += 4 * w;
+        for (auto w : g->ts->words) table_bytes += 4 * w;
         const bool fits = bucket_fits(g, n_total, fs);
         if (g->path == GDBG_PATH_BUCKETED && fits) return run_insert_bucketed(g, b, n_new, st);
         if (g->path == GDBG_PATH_AUTO && fits && table_bytes >= (256ull << 20) &&
@@ -581,7 +646,7 @@ int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64
         w.claims_mask = g->claims_mask;
         w.epoch = g->epoch;
         w.n_new = (unsigned long long*)n_new;
-        w.counters = g->d_counters;
+        w.counters = g->ts->d_counters;
         w.err = g->d_err;
         uint64_t n_threads = (end - start + kpt - 1) / kpt;
         GDBG_TRY(launch_pass(g, 0, s, n_threads, st, b, hashes, w));
@@ -590,15 +655,39 @@ int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64
     return GDBG_OK;
 }
 
+// Insert a batch and return every k-mer's insert_and_query count in batch
+// order (dbg.hh:327-340 / 249-265 per read).  Needs the bucketed layout,
+// where each table region's records are applied in k-mer order.
+int run_insert_query(gdbg_graph* g, const BatchView& b, int16_t* counts, uint64_t* n_new,
+                     cudaStream_t st) {
+    if (b.n_kmers == 0) {
+        if (n_new && b.n_reads) GDBG_CUDA(cudaMemsetAsync(n_new, 0, b.n_reads * sizeof(uint64_t), st));
+        return GDBG_OK;
+    }
+    const uint32_t fs = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
+    if (!bucket_fits(g, b.n_kmers, fs))
+        return fail(GDBG_ERR_UNSUPPORTED,
+                    "insert_and_query batches need at most 8 tables, 2^32 cells and 2^32 records");
+    if (g->storage == GDBG_BIT) {
+        GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, n_new, st));
+        cudaError_t e = launch_iq_counts(nullptr, b.n_kmers, 0, nullptr, b.kofs + b.n_reads, counts,
+                                         true, st);
+        if (e != cudaSuccess) return set_error_launch(e, "insert_and_query counts");
+        g->launches += 1;
+        return GDBG_OK;
+    }
+    return run_insert_bucketed(g, b, n_new, st, counts);
+}
+
 int run_query(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64_t n_total,
               int16_t* counts, uint64_t* values, cudaStream_t st) {
     if (n_total == 0) return GDBG_OK;
     LaunchShape s = g->shape(4);
     cudaError_t e;
     switch (g->storage) {
-    case GDBG_BIT: e = launch_query<GDBG_BIT>(s, n_total, st, b, hashes, g->hp, g->tp, counts, values); break;
-    case GDBG_BYTE: e = launch_query<GDBG_BYTE>(s, n_total, st, b, hashes, g->hp, g->tp, counts, values); break;
-    default: e = launch_query<GDBG_NIBBLE>(s, n_total, st, b, hashes, g->hp, g->tp, counts, values); break;
+    case GDBG_BIT: e = launch_query<GDBG_BIT>(s, n_total, st, b, hashes, g->hp, g->ts->tp, counts, values); break;
+    case GDBG_BYTE: e = launch_query<GDBG_BYTE>(s, n_total, st, b, hashes, g->hp, g->ts->tp, counts, values); break;
+    default: e = launch_query<GDBG_NIBBLE>(s, n_total, st, b, hashes, g->hp, g->ts->tp, counts, values); break;
     }
     if (e != cudaSuccess) return fail(GDBG_ERR_CUDA, std::string("query launch: ") + cudaGetErrorString(e));
     g->launches += 1;
@@ -610,9 +699,9 @@ int run_masks(gdbg_graph* g, const BatchView& b, uint8_t* masks, cudaStream_t st
     LaunchShape s = g->shape(2);
     cudaError_t e;
     switch (g->storage) {
-    case GDBG_BIT: e = launch_masks<GDBG_BIT>(s, st, b, g->hp, g->tp, masks); break;
-    case GDBG_BYTE: e = launch_masks<GDBG_BYTE>(s, st, b, g->hp, g->tp, masks); break;
-    default: e = launch_masks<GDBG_NIBBLE>(s, st, b, g->hp, g->tp, masks); break;
+    case GDBG_BIT: e = launch_masks<GDBG_BIT>(s, st, b, g->hp, g->ts->tp, masks); break;
+    case GDBG_BYTE: e = launch_masks<GDBG_BYTE>(s, st, b, g->hp, g->ts->tp, masks); break;
+    default: e = launch_masks<GDBG_NIBBLE>(s, st, b, g->hp, g->ts->tp, masks); break;
     }
     if (e != cudaSuccess) return fail(GDBG_ERR_CUDA, std::string("mask launch: ") + cudaGetErrorString(e));
     g->launches += 1;
@@ -750,8 +839,7 @@ int gdbg_destroy(gdbg_graph* g) {
     cudaSetDevice(g->device);
     if (g->own_stream) cudaStreamSynchronize(g->own_stream);
     if (g->stream && g->stream != g->own_stream) cudaStreamSynchronize(g->stream);
-    if (g->d_tables) cudaFree(g->d_tables);
-    if (g->d_counters) cudaFree(g->d_counters);
+    g->ts.reset();   // frees the tables with the last handle on them
     if (g->d_err) cudaFree(g->d_err);
     if (g->d_epoch) cudaFree(g->d_epoch);
     if (g->d_bar) cudaFree(g->d_bar);
@@ -759,7 +847,7 @@ int gdbg_destroy(gdbg_graph* g) {
     g->kofs.release(); g->tofs.release(); g->partials.release(); g->tile_read.release();
     g->task_read.release();
     g->rec_a.release(); g->rec_b.release(); g->hist.release(); g->hist_off.release();
-    g->scan_parts.release(); g->bstart.release(); g->new_bits.release();
+    g->scan_parts.release(); g->bstart.release(); g->new_bits.release(); g->iq_vals.release();
     g->st_packed.release(); g->st_offsets.release(); g->st_out64.release();
     g->st_out64b.release(); g->st_out64c.release(); g->st_counts.release(); g->st_u8.release();
     for (auto& p : g->pending) {
@@ -775,7 +863,7 @@ int gdbg_destroy(gdbg_graph* g) {
 int gdbg_clone(const gdbg_graph* g, gdbg_graph** out) {
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
     GDBG_TRY(set_device(g));
-    GDBG_TRY(make_graph(g->storage, g->shifter, g->K, g->sizes.data(), (uint16_t)g->sizes.size(), out));
+    GDBG_TRY(make_graph(g->storage, g->shifter, g->K, g->ts->sizes.data(), (uint16_t)g->ts->sizes.size(), out));
     (*out)->window = g->window;
     (*out)->kpt = g->kpt;
     (*out)->pwindow = g->pwindow;
@@ -785,10 +873,39 @@ int gdbg_clone(const gdbg_graph* g, gdbg_graph** out) {
     return GDBG_OK;
 }
 
+int gdbg_share_storage(const gdbg_graph* g, int shifter, uint16_t K, gdbg_graph** out) {
+    if (!g || !out) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    GDBG_TRY(check_kinds(g->storage, shifter, K));
+    GDBG_TRY(set_device(g));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    gdbg_graph* h = new gdbg_graph();
+    h->device = g->device;
+    h->ts = g->ts;
+    const int rc = init_handle(h, g->storage, shifter, K);
+    if (rc != GDBG_OK) {
+        gdbg_destroy(h);
+        return rc;
+    }
+    h->window = g->window;
+    h->kpt = g->kpt;
+    h->pwindow = g->pwindow;
+    h->persistent = g->persistent;
+    h->path = g->path;
+    h->bucket_fs = g->bucket_fs;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        gdbg_destroy(h);
+        return fail(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *out = h;
+    return GDBG_OK;
+}
+
 int gdbg_reset(gdbg_graph* g) {
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
     GDBG_TRY(set_device(g));
-    GDBG_CUDA(cudaMemsetAsync(g->d_tables, 0, g->total_words * sizeof(uint32_t), g->stream));
+    GDBG_CUDA(cudaMemsetAsync(g->ts->d_tables, 0, g->ts->total_words * sizeof(uint32_t), g->stream));
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
     return GDBG_OK;
 }
@@ -798,33 +915,33 @@ int gdbg_info(const gdbg_graph* g, int* storage, int* shifter, uint16_t* K, uint
     if (storage) *storage = g->storage;
     if (shifter) *shifter = g->shifter;
     if (K) *K = g->K;
-    if (n_tables) *n_tables = (uint16_t)g->sizes.size();
+    if (n_tables) *n_tables = (uint16_t)g->ts->sizes.size();
     return GDBG_OK;
 }
 
 int gdbg_get_tablesizes(const gdbg_graph* g, uint64_t* out) {
     if (!g || !out) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
-    std::copy(g->sizes.begin(), g->sizes.end(), out);
+    std::copy(g->ts->sizes.begin(), g->ts->sizes.end(), out);
     return GDBG_OK;
 }
 
 int gdbg_table_bytes(const gdbg_graph* g, uint64_t* out) {
     if (!g || !out) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
-    std::copy(g->bytes.begin(), g->bytes.end(), out);
+    std::copy(g->ts->bytes.begin(), g->ts->bytes.end(), out);
     return GDBG_OK;
 }
 
 int gdbg_get_tables(gdbg_graph* g, uint8_t* out, uint64_t out_len) {
     if (!g || !out) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
     uint64_t need = 0;
-    for (auto b : g->bytes) need += b;
+    for (auto b : g->ts->bytes) need += b;
     if (out_len < need) return fail(GDBG_ERR_INVALID_ARG, "output buffer too small");
     GDBG_TRY(set_device(g));
     uint64_t pos = 0;
-    for (size_t i = 0; i < g->sizes.size(); ++i) {
-        GDBG_CUDA(cudaMemcpyAsync(out + pos, g->d_tables + g->word_off[i], g->bytes[i],
+    for (size_t i = 0; i < g->ts->sizes.size(); ++i) {
+        GDBG_CUDA(cudaMemcpyAsync(out + pos, g->ts->d_tables + g->ts->word_off[i], g->ts->bytes[i],
                                   cudaMemcpyDeviceToHost, g->stream));
-        pos += g->bytes[i];
+        pos += g->ts->bytes[i];
     }
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
     return GDBG_OK;
@@ -833,14 +950,14 @@ int gdbg_get_tables(gdbg_graph* g, uint8_t* out, uint64_t out_len) {
 int gdbg_set_tables(gdbg_graph* g, const uint8_t* in, uint64_t in_len) {
     if (!g || !in) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
     uint64_t need = 0;
-    for (auto b : g->bytes) need += b;
+    for (auto b : g->ts->bytes) need += b;
     if (in_len != need) return fail(GDBG_ERR_INVALID_ARG, "input length does not match the tables");
     GDBG_TRY(set_device(g));
     uint64_t pos = 0;
-    for (size_t i = 0; i < g->sizes.size(); ++i) {
-        GDBG_CUDA(cudaMemcpyAsync(g->d_tables + g->word_off[i], in + pos, g->bytes[i],
+    for (size_t i = 0; i < g->ts->sizes.size(); ++i) {
+        GDBG_CUDA(cudaMemcpyAsync(g->ts->d_tables + g->ts->word_off[i], in + pos, g->ts->bytes[i],
                                   cudaMemcpyHostToDevice, g->stream));
-        pos += g->bytes[i];
+        pos += g->ts->bytes[i];
     }
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
     return GDBG_OK;
@@ -850,10 +967,247 @@ int gdbg_stats(gdbg_graph* g, uint64_t* n_unique, uint64_t* n_occupied) {
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
     GDBG_TRY(set_device(g));
     unsigned long long c[2];
-    GDBG_CUDA(cudaMemcpyAsync(c, g->d_counters, sizeof c, cudaMemcpyDeviceToHost, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(c, g->ts->d_counters, sizeof c, cudaMemcpyDeviceToHost, g->stream));
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
     if (n_unique) *n_unique = c[0];
     if (n_occupied) *n_occupied = c[1];
+    return GDBG_OK;
+}
+
+// ---- OXLI v4 table files (Storage::save / Storage::load) -------------------
+//
+// Layout (storage.hh:63-72, bitstorage.cc:151-307, bytestorage.cc:172-290 and
+// 480-521, nibblestorage.cc:132-250): "OXLI", version 4, file type (2 Bit,
+// 1 Byte, 7 Nibble), [Byte: use_bigcount u8], ksize u32, n_tables u8,
+// occupied_bins u64, then per table its size in cells (u64) and its bytes,
+// [Byte: bigcount entry count u64 + entries].  Tables move between HBM and
+// the file through two pinned staging buffers, so the copy of one chunk
+// overlaps the file I/O of the other.
+
+namespace {
+
+constexpr uint8_t OXLI_VERSION = 4;
+constexpr uint64_t IO_CHUNK = 32ull << 20;
+
+uint8_t oxli_type(int storage) {
+    return storage == GDBG_BIT ? 2 : storage == GDBG_BYTE ? 1 : 7;
+}
+
+const char* oxli_noun(int storage) {
+    return storage == GDBG_BIT ? "k-mer graph" : "k-mer count";
+}
+
+struct FileCloser {
+    FILE* f;
+    ~FileCloser() { if (f) std::fclose(f); }
+};
+
+struct Staging {
+    uint8_t* buf[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    ~Staging() {
+        for (int i = 0; i < 2; ++i) {
+            if (ev[i]) { cudaEventSynchronize(ev[i]); cudaEventDestroy(ev[i]); }
+            if (buf[i]) cudaFreeHost(buf[i]);
+        }
+    }
+    int init() {
+        for (int i = 0; i < 2; ++i) {
+            GDBG_CUDA(cudaHostAlloc((void**)&buf[i], IO_CHUNK, cudaHostAllocDefault));
+            GDBG_CUDA(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
+        }
+        return GDBG_OK;
+    }
+};
+
+}  // namespace
+
+int gdbg_save(gdbg_graph* g, const char* path) {
+    if (!g || !path) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    uint64_t n_occ = 0;
+    GDBG_TRY(gdbg_stats(g, nullptr, &n_occ));
+    FileCloser fc{std::fopen(path, "wb")};
+    if (!fc.f) return fail(GDBG_ERR_IO, std::string("cannot open ") + path + ": " + std::strerror(errno));
+    std::vector<uint8_t> head;
+    auto put = [&](const void* p, size_t n) {
+        head.insert(head.end(), (const uint8_t*)p, (const uint8_t*)p + n);
+    };
+    const uint8_t ver = OXLI_VERSION, type = oxli_type(g->storage), bigcount = 0;
+    const uint32_t ksize = g->K;
+    const uint8_t n_tables = (uint8_t)g->ts->sizes.size();
+    put("OXLI", 4);
+    put(&ver, 1);
+    put(&type, 1);
+    if (g->storage == GDBG_BYTE) put(&bigcount, 1);
+    put(&ksize, 4);
+    put(&n_tables, 1);
+    put(&n_occ, 8);
+    if (std::fwrite(head.data(), 1, head.size(), fc.f) != head.size())
+        return fail(GDBG_ERR_IO, std::string("write failed: ") + std::strerror(errno));
+    Staging st;
+    GDBG_TRY(st.init());
+    for (size_t i = 0; i < g->ts->sizes.size(); ++i) {
+        const uint64_t size = g->ts->sizes[i], nb = g->ts->bytes[i];
+        if (std::fwrite(&size, 8, 1, fc.f) != 1)
+            return fail(GDBG_ERR_IO, std::string("write failed: ") + std::strerror(errno));
+        const uint8_t* src = (const uint8_t*)(g->ts->d_tables + g->ts->word_off[i]);
+        const uint64_t n_chunks = (nb + IO_CHUNK - 1) / IO_CHUNK;
+        auto issue = [&](uint64_t c) -> int {
+            const uint64_t o = c * IO_CHUNK, len = std::min(IO_CHUNK, nb - o);
+            GDBG_CUDA(cudaMemcpyAsync(st.buf[c & 1], src + o, len, cudaMemcpyDeviceToHost, g->stream));
+            GDBG_CUDA(cudaEventRecord(st.ev[c & 1], g->stream));
+            return GDBG_OK;
+        };
+        if (n_chunks) GDBG_TRY(issue(0));
+        for (uint64_t c = 0; c < n_chunks; ++c) {
+            if (c + 1 < n_chunks) GDBG_TRY(issue(c + 1));
+            GDBG_CUDA(cudaEventSynchronize(st.ev[c & 1]));
+            const uint64_t len = std::min(IO_CHUNK, nb - c * IO_CHUNK);
+            if (std::fwrite(st.buf[c & 1], 1, len, fc.f) != len)
+                return fail(GDBG_ERR_IO, std::string("write failed: ") + std::strerror(errno));
+        }
+    }
+    if (g->storage == GDBG_BYTE) {
+        const uint64_t n_counts = 0;
+        if (std::fwrite(&n_counts, 8, 1, fc.f) != 1)
+            return fail(GDBG_ERR_IO, std::string("write failed: ") + std::strerror(errno));
+    }
+    FILE* f = fc.f;
+    fc.f = nullptr;
+    if (std::fclose(f) != 0)
+        return fail(GDBG_ERR_IO, std::string("write failed: ") + std::strerror(errno));
+    return GDBG_OK;
+}
+
+int gdbg_load(gdbg_graph* g, const char* path, uint16_t* ksize_out) {
+    if (!g || !path) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    const std::string file(path), noun(oxli_noun(g->storage));
+    FileCloser fc{std::fopen(path, "rb")};
+    if (!fc.f) return fail(GDBG_ERR_IO, "Cannot open " + noun + " file: " + file);
+    const std::string eof_msg = "Unexpected end of " + noun + " file: " + file;
+    auto rd = [&](void* p, size_t n) { return std::fread(p, 1, n, fc.f) == n; };
+    char sig[4];
+    uint8_t ver = 0, type = 0;
+    if (!rd(sig, 4) || !rd(&ver, 1) || !rd(&type, 1)) return fail(GDBG_ERR_IO, eof_msg);
+    if (std::memcmp(sig, "OXLI", 4) != 0) {
+        char hex[16];
+        std::string got;
+        for (int i = 0; i < 4; ++i) {
+            std::snprintf(hex, sizeof hex, "%x", (int)sig[i]);
+            got += hex;
+        }
+        return fail(GDBG_ERR_IO, "Does not start with signature for a oxli file: 0x" + got +
+                                     " Should be: OXLI");
+    }
+    if (ver != OXLI_VERSION)
+        return fail(GDBG_ERR_IO, "Incorrect file format version " + std::to_string(ver) +
+                                     " while reading " + noun + " file from " + file +
+                                     "; should be " + std::to_string(OXLI_VERSION));
+    if (type != oxli_type(g->storage))
+        return fail(GDBG_ERR_IO, "Incorrect file format type " + std::to_string(type) +
+                                     " while reading " + noun + " file from " + file);
+    if (g->storage == GDBG_BYTE) {
+        uint8_t bigcount = 0;
+        if (!rd(&bigcount, 1)) return fail(GDBG_ERR_IO, eof_msg);
+        if (bigcount)
+            return fail(GDBG_ERR_UNSUPPORTED, "counts above 255 (use_bigcount) are not supported: " + file);
+    }
+    uint32_t ksize = 0;
+    uint8_t n_tables = 0;
+    uint64_t n_occ = 0;
+    if (!rd(&ksize, 4) || !rd(&n_tables, 1) || !rd(&n_occ, 8)) return fail(GDBG_ERR_IO, eof_msg);
+    if (n_tables == 0 || n_tables > MAX_TABLES)
+        return fail(GDBG_ERR_UNSUPPORTED, "table count " + std::to_string(n_tables) +
+                                              " outside 1.." + std::to_string(MAX_TABLES) + ": " + file);
+    // pass 1: table sizes and the file length, before any state changes
+    const long data_start = std::ftell(fc.f);
+    std::vector<uint64_t> sizes(n_tables);
+    for (uint8_t i = 0; i < n_tables; ++i) {
+        if (!rd(&sizes[i], 8)) return fail(GDBG_ERR_IO, eof_msg);
+        const uint64_t p = sizes[i];
+        if (p == 0 || p >= (1ull << 32))
+            return fail(GDBG_ERR_UNSUPPORTED, "table size outside 1..2^32-1 cells: " + file);
+        const uint64_t nb = g->storage == GDBG_BIT ? p / 8 + 1 : g->storage == GDBG_NIBBLE ? p / 2 + 1 : p;
+        if (std::fseek(fc.f, (long)nb, SEEK_CUR) != 0) return fail(GDBG_ERR_IO, eof_msg);
+    }
+    const long data_end = std::ftell(fc.f);
+    if (g->storage == GDBG_BYTE) {
+        uint64_t n_counts = 0;
+        if (!rd(&n_counts, 8)) return fail(GDBG_ERR_IO, eof_msg);
+        if (n_counts)
+            return fail(GDBG_ERR_UNSUPPORTED, "bigcount entries are not supported: " + file);
+    }
+    if (std::fseek(fc.f, 0, SEEK_END) != 0) return fail(GDBG_ERR_IO, eof_msg);
+    if (std::ftell(fc.f) < data_end) return fail(GDBG_ERR_IO, eof_msg);
+    // new tables (the old ones stay until the new allocation succeeded)
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    if (sizes != g->ts->sizes) {
+        std::vector<uint64_t> sz, bytes, words, word_off;
+        const uint64_t total = table_layout(g->storage, sizes.data(), n_tables, sz, bytes, words, word_off);
+        uint32_t* fresh = nullptr;
+        GDBG_CUDA(cudaMalloc((void**)&fresh, total * sizeof(uint32_t)));
+        cudaFree(g->ts->d_tables);
+        g->ts->d_tables = fresh;
+        g->ts->sizes = sz;
+        g->ts->bytes = bytes;
+        g->ts->words = words;
+        g->ts->word_off = word_off;
+        g->ts->total_words = total;
+        set_table_params(g);
+    }
+    GDBG_CUDA(cudaMemsetAsync(g->ts->d_tables, 0, g->ts->total_words * sizeof(uint32_t), g->stream));
+    // pass 2: table bytes
+    if (std::fseek(fc.f, data_start, SEEK_SET) != 0) return fail(GDBG_ERR_IO, eof_msg);
+    Staging st;
+    GDBG_TRY(st.init());
+    uint64_t c_all = 0;  // chunks issued so far, alternating buffers
+    for (uint8_t i = 0; i < n_tables; ++i) {
+        uint64_t p = 0;
+        if (!rd(&p, 8)) return fail(GDBG_ERR_IO, eof_msg);
+        uint8_t* dst = (uint8_t*)(g->ts->d_tables + g->ts->word_off[i]);
+        const uint64_t nb = g->ts->bytes[i];
+        for (uint64_t o = 0; o < nb; o += IO_CHUNK, ++c_all) {
+            const uint64_t len = std::min(IO_CHUNK, nb - o);
+            const int b = (int)(c_all & 1);
+            GDBG_CUDA(cudaEventSynchronize(st.ev[b]));   // its previous copy is done
+            if (!rd(st.buf[b], len)) return fail(GDBG_ERR_IO, eof_msg);
+            GDBG_CUDA(cudaMemcpyAsync(dst + o, st.buf[b], len, cudaMemcpyHostToDevice, g->stream));
+            GDBG_CUDA(cudaEventRecord(st.ev[b], g->stream));
+        }
+    }
+    // occupied bins come from the file; n_unique is kept (bitstorage.cc:264-275)
+    unsigned long long occ = n_occ;
+    GDBG_CUDA(cudaMemcpyAsync(g->ts->d_counters + 1, &occ, sizeof occ, cudaMemcpyHostToDevice, g->stream));
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    if (ksize_out) *ksize_out = (uint16_t)ksize;
+    return GDBG_OK;
+}
+
+int gdbg_update_from(gdbg_graph* g, const gdbg_graph* other) {
+    if (!g || !other) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    if (g->storage != GDBG_BIT || other->storage != GDBG_BIT)
+        return fail(GDBG_ERR_UNSUPPORTED, "update_from is defined for BitStorage only");
+    if (g->ts->sizes != other->ts->sizes)
+        return fail(GDBG_ERR_INVALID_ARG, "both nodegraphs must have same table sizes");
+    if (g->device != other->device)
+        return fail(GDBG_ERR_INVALID_ARG, "both nodegraphs must be on the same device");
+    GDBG_TRY(set_device(g));
+    if (g->ts->d_tables == other->ts->d_tables) return GDBG_OK;
+    // the merge reads other's tables after all work queued on its stream
+    if (other->stream != g->stream) {
+        cudaEvent_t ev = nullptr;
+        GDBG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaError_t e = cudaEventRecord(ev, other->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(g->stream, ev, 0);
+        cudaEventDestroy(ev);
+        GDBG_CUDA(e);
+    }
+    GDBG_CUDA(launch_or_merge(g->ts->d_tables, other->ts->d_tables, g->ts->total_words, g->ts->words[0],
+                              g->ts->d_counters + 1, g->stream));
+    g->launches++;
+    GDBG_CUDA(cudaStreamSynchronize(g->stream));
     return GDBG_OK;
 }
 
@@ -928,6 +1282,25 @@ int gdbg_query_sequence(gdbg_graph* g, const char* seq, uint64_t len, int16_t* c
         GDBG_CUDA(cudaMemcpyAsync(hashes, g->st_out64.p, b.n_kmers * sizeof(uint64_t),
                                   cudaMemcpyDeviceToHost, g->stream));
     return check_device_status(g);
+}
+
+int gdbg_insert_and_query_sequence(gdbg_graph* g, const char* seq, uint64_t len, int16_t* counts,
+                                   uint64_t* n_new) {
+    if (!g || !counts) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_string(g, seq, len, &b));
+    GDBG_TRY(g->st_counts.ensure(b.n_kmers));
+    GDBG_TRY(g->st_out64.ensure(1));
+    GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, sizeof(uint64_t), g->stream));
+    GDBG_TRY(run_insert_query(g, b, g->st_counts.p, g->st_out64.p, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(counts, g->st_counts.p, b.n_kmers * sizeof(int16_t),
+                              cudaMemcpyDeviceToHost, g->stream));
+    uint64_t nn = 0;
+    GDBG_CUDA(cudaMemcpyAsync(&nn, g->st_out64.p, sizeof nn, cudaMemcpyDeviceToHost, g->stream));
+    GDBG_TRY(check_device_status(g));
+    if (n_new) *n_new = nn;
+    return GDBG_OK;
 }
 
 int gdbg_hashes(gdbg_graph* g, const char* seq, uint64_t len, uint64_t* values, uint64_t* fw,
@@ -1033,6 +1406,27 @@ int gdbg_query_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
     return check_device_status(g);
 }
 
+int gdbg_insert_and_query_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                                const uint64_t* offsets, uint64_t n_reads, int16_t* counts,
+                                uint64_t* n_new) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b));
+    if (b.n_kmers && !counts) return fail(GDBG_ERR_INVALID_ARG, "NULL counts");
+    GDBG_TRY(g->st_counts.ensure(b.n_kmers + 1));
+    GDBG_TRY(g->st_out64.ensure(n_reads + 1));
+    if (n_reads) GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, n_reads * sizeof(uint64_t), g->stream));
+    GDBG_TRY(run_insert_query(g, b, g->st_counts.p, g->st_out64.p, g->stream));
+    if (b.n_kmers)
+        GDBG_CUDA(cudaMemcpyAsync(counts, g->st_counts.p, b.n_kmers * sizeof(int16_t),
+                                  cudaMemcpyDeviceToHost, g->stream));
+    if (n_new && n_reads)
+        GDBG_CUDA(cudaMemcpyAsync(n_new, g->st_out64.p, n_reads * sizeof(uint64_t),
+                                  cudaMemcpyDeviceToHost, g->stream));
+    return check_device_status(g);
+}
+
 int gdbg_hashes_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                       const uint64_t* offsets, uint64_t n_reads, uint64_t* values, uint64_t* fw,
                       uint64_t* rc) {
@@ -1092,6 +1486,20 @@ int gdbg_query_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t pack
     BatchView b;
     GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b));
     return run_query(g, b, nullptr, b.n_kmers, counts, nullptr, st);
+}
+
+int gdbg_insert_and_query_batch_device(gdbg_graph* g, const uint32_t* packed,
+                                       uint64_t packed_words, const uint64_t* offsets,
+                                       uint64_t n_reads, uint64_t n_kmers_hint, int16_t* counts,
+                                       uint64_t* n_new, void* stream) {
+    if (!g || !offsets) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    cudaStream_t st = pick_stream(g, stream);
+    BatchView b;
+    GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b));
+    if (b.n_kmers && !counts) return fail(GDBG_ERR_INVALID_ARG, "NULL counts");
+    if (n_new && n_reads) GDBG_CUDA(cudaMemsetAsync(n_new, 0, n_reads * sizeof(uint64_t), st));
+    return run_insert_query(g, b, counts, n_new, st);
 }
 
 int gdbg_hashes_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,

@@ -45,27 +45,42 @@ cudaError_t launch_bucket_starts_fix(cudaStream_t st, const BucketParams& bp, ui
 
 uint64_t bucket_tile_records() { return BK_TILE; }
 
-template <int ST>
+template <int ST, bool IQ>
 static cudaError_t apply_one(const TableParams& tp, const BucketParams& bp, const uint64_t* recs,
                              const uint32_t* start, uint32_t* new_bits,
-                             unsigned long long* counters, cudaStream_t st) {
-    const size_t smem = bk_apply_smem((1u << bp.fs) / cells_per_word<ST>());
-    cudaError_t e = cudaFuncSetAttribute(k_bkt_apply<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+                             unsigned long long* counters, uint8_t* vals, cudaStream_t st) {
+    const size_t smem = bk_apply_smem((1u << bp.fs) / cells_per_word<ST>(), IQ);
+    cudaError_t e = cudaFuncSetAttribute(k_bkt_apply<ST, IQ>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_bkt_apply<ST><<<bp.n_buckets, BK_BLOCK, smem, st>>>(tp, bp, recs, start, new_bits, counters);
+    k_bkt_apply<ST, IQ><<<bp.n_buckets, BK_BLOCK, smem, st>>>(tp, bp, recs, start, new_bits,
+                                                              counters, vals);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bucket_apply(int storage, const TableParams& tp, const BucketParams& bp,
                                 const uint64_t* recs, const uint32_t* start, uint32_t* new_bits,
-                                unsigned long long* counters, cudaStream_t st) {
+                                unsigned long long* counters, uint8_t* vals, cudaStream_t st) {
     if (bp.n_buckets == 0) return cudaSuccess;
     switch (storage) {
-    case GDBG_BIT: return apply_one<GDBG_BIT>(tp, bp, recs, start, new_bits, counters, st);
-    case GDBG_BYTE: return apply_one<GDBG_BYTE>(tp, bp, recs, start, new_bits, counters, st);
-    default: return apply_one<GDBG_NIBBLE>(tp, bp, recs, start, new_bits, counters, st);
+    case GDBG_BIT: return apply_one<GDBG_BIT, false>(tp, bp, recs, start, new_bits, counters, nullptr, st);
+    case GDBG_BYTE:
+        return vals ? apply_one<GDBG_BYTE, true>(tp, bp, recs, start, new_bits, counters, vals, st)
+                    : apply_one<GDBG_BYTE, false>(tp, bp, recs, start, new_bits, counters, nullptr, st);
+    default:
+        return vals ? apply_one<GDBG_NIBBLE, true>(tp, bp, recs, start, new_bits, counters, vals, st)
+                    : apply_one<GDBG_NIBBLE, false>(tp, bp, recs, start, new_bits, counters, nullptr, st);
     }
+}
+
+cudaError_t launch_iq_counts(const uint8_t* vals, uint64_t cap, uint32_t n_tables,
+                             const uint32_t* new_bits, const uint64_t* total, int16_t* counts,
+                             bool presence, cudaStream_t st) {
+    if (cap == 0) return cudaSuccess;
+    uint64_t grid = (cap + 255) / 256;
+    if (grid > 152 * 16) grid = 152 * 16;
+    k_iq_counts<<<(unsigned)grid, 256, 0, st>>>(vals, cap, n_tables, new_bits, total, counts, presence);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_bucket_read_new(const uint64_t* kofs, uint64_t n_reads, const uint32_t* new_bits,

@@ -293,11 +293,19 @@ constexpr int BK_AMAP = 2 * BK_CHUNK;             // chunk map slots
 // chunk map (keys, then minimum chunk ranks) and a dirty bit per 32-byte
 // sector of the slice.  Records are applied in chunks of BK_CHUNK in g order;
 // only dirty sectors are written back.
-template <int STORAGE>
+//
+// IQ (insert_and_query counts, bytestorage.cc:142-150): every record's cell
+// goes into the chunk map, whose value is then the head of a list of the
+// chunk's records on that cell; a record's rank is the number of list
+// entries before it in g order.  Its table's value right after its own
+// insert is min(max, value before the chunk + rank + 1), stored to
+// vals[table * kmer_cap + g]; it is new when the value before was 0 and
+// its rank is 0.
+template <int STORAGE, bool IQ>
 __global__ void __launch_bounds__(BK_BLOCK)
 k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
             const uint32_t* __restrict__ start, uint32_t* __restrict__ new_bits,
-            unsigned long long* counters) {
+            unsigned long long* counters, uint8_t* __restrict__ vals) {
     extern __shared__ uint32_t smem[];
     const uint32_t bk = blockIdx.x;
     const uint32_t rs = start[bk], re = start[bk + 1];
@@ -315,6 +323,7 @@ k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
     uint32_t* mkey = smem + region_words;
     uint32_t* mval = mkey + BK_AMAP;
     uint32_t* dirty = mval + BK_AMAP;
+    uint32_t* nxt = dirty + ((region_sectors + 31) / 32);   // IQ: list links per chunk record
     const uint32_t* gsrc = tp.words[ti] + w0;
     const bool vec = ((w0 & 3u) == 0) && ((nw & 3u) == 0);
     if (vec) {
@@ -347,6 +356,7 @@ k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
     }
     for (uint32_t base = rs; base < re; base += BK_CHUNK) {
         uint32_t co[BK_RPT], g[BK_RPT], word[BK_RPT], shift[BK_RPT], slot[BK_RPT];
+        uint32_t before[BK_RPT];
         bool active[BK_RPT], fresh[BK_RPT];
 #pragma unroll
         for (int r = 0; r < BK_RPT; ++r) {
@@ -358,9 +368,10 @@ k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
             co[r] = (uint32_t)(rec >> 32) & co_mask;
             g[r] = (uint32_t)rec;
             region_cell<STORAGE>(co[r], word[r], shift[r]);
-            fresh[r] = active[r] && cell_value<STORAGE>(region[word[r]], shift[r]) == 0;
+            before[r] = active[r] ? cell_value<STORAGE>(region[word[r]], shift[r]) : 1u;
+            fresh[r] = active[r] && before[r] == 0;
             slot[r] = 0;
-            if (fresh[r]) {
+            if (IQ ? active[r] : fresh[r]) {
                 // register the cell in the chunk map (rank order = g order)
                 uint32_t sl = (co[r] * 0x9E3779B1u) >> (32 - 12);
                 for (int it = 0; it < BK_AMAP; ++it) {
@@ -376,13 +387,42 @@ k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
             }
         }
         __syncthreads();
+        uint32_t rank[BK_RPT];
+        if (IQ) {
 #pragma unroll
-        for (int r = 0; r < BK_RPT; ++r)
-            if (fresh[r]) atomicMin(mval + slot[r], r * BK_BLOCK + threadIdx.x);
+            for (int r = 0; r < BK_RPT; ++r)
+                if (active[r]) {
+                    const uint32_t idx = r * BK_BLOCK + threadIdx.x;
+                    nxt[idx] = atomicExch(mval + slot[r], idx);
+                }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < BK_RPT; ++r) {
+                const uint32_t idx = r * BK_BLOCK + threadIdx.x;
+                uint32_t n = 0;
+                if (active[r]) {
+                    uint32_t j = mval[slot[r]];
+                    for (int it = 0; it < BK_CHUNK && j != 0xFFFFFFFFu; ++it) {
+                        n += j < idx;
+                        j = nxt[j];
+                    }
+                }
+                rank[r] = n;
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < BK_RPT; ++r)
+                if (fresh[r]) atomicMin(mval + slot[r], r * BK_BLOCK + threadIdx.x);
+        }
         __syncthreads();
 #pragma unroll
         for (int r = 0; r < BK_RPT; ++r) {
-            const bool isnew = fresh[r] && mval[slot[r]] == r * BK_BLOCK + threadIdx.x;
+            const bool isnew = IQ ? fresh[r] && rank[r] == 0
+                                  : fresh[r] && mval[slot[r]] == r * BK_BLOCK + threadIdx.x;
+            if (IQ && active[r] && g[r] < bp.kmer_cap) {
+                const uint32_t v = min(before[r] + rank[r] + 1u, cell_max<STORAGE>());
+                vals[(uint64_t)ti * bp.kmer_cap + g[r]] = (uint8_t)v;
+            }
             if (active[r]) {
                 bool changed = false;
                 if (STORAGE == GDBG_BIT) {
@@ -415,7 +455,7 @@ k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
         __syncthreads();
 #pragma unroll
         for (int r = 0; r < BK_RPT; ++r)
-            if (fresh[r]) mkey[slot[r]] = 0;
+            if (IQ ? active[r] : fresh[r]) mkey[slot[r]] = 0;
         __syncthreads();
     }
     // write back the dirty 32-byte sectors (8 words each)
@@ -436,8 +476,29 @@ k_bkt_apply(TableParams tp, BucketParams bp, const uint64_t* __restrict__ recs,
     if ((threadIdx.x & 31) == 0 && occ) atomicAdd(counters + 1, occ);
 }
 
-__host__ __device__ constexpr size_t bk_apply_smem(uint32_t region_words) {
-    return (size_t)region_words * 4 + 2 * BK_AMAP * 4 + ((region_words + 7) / 8 + 31) / 32 * 4;
+__host__ __device__ constexpr size_t bk_apply_smem(uint32_t region_words, bool iq = false) {
+    return (size_t)region_words * 4 + 2 * BK_AMAP * 4 + ((region_words + 7) / 8 + 31) / 32 * 4 +
+           (iq ? (size_t)BK_CHUNK * 4 : 0);
+}
+
+// insert_and_query counts per k-mer (bytestorage.cc:142-150,
+// nibblestorage.cc:103-109): 1 when the k-mer was new, else the minimum over
+// the tables of the values right after its own insert; BitStorage always 1
+// (bitstorage.cc:78-84).
+__global__ void k_iq_counts(const uint8_t* __restrict__ vals, uint64_t cap, uint32_t n_tables,
+                            const uint32_t* __restrict__ new_bits, const uint64_t* __restrict__ total,
+                            int16_t* __restrict__ counts, bool presence) {
+    const uint64_t n = min(*total, cap);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        int16_t c = 1;
+        if (!presence && !((__ldg(new_bits + (k >> 5)) >> (k & 31u)) & 1u)) {
+            uint32_t m = 0xFFu;
+            for (uint32_t t = 0; t < n_tables; ++t) m = min(m, (uint32_t)__ldg(vals + t * cap + k));
+            c = (int16_t)m;
+        }
+        counts[k] = c;
+    }
 }
 
 // Per-read new counts from the new-k-mer bitmask, plus the batch total.

@@ -57,9 +57,15 @@ cudaError_t launch_bucket_scatter(bool last, uint32_t n_tiles, cudaStream_t st,
                                   const BucketParams& bp, uint32_t* start);
 cudaError_t launch_bucket_starts_fix(cudaStream_t st, const BucketParams& bp, uint32_t* start);
 uint64_t bucket_tile_records();
+// vals != nullptr (Byte/Nibble): also store each record's post-insert value
+// for insert_and_query (vals[table * kmer_cap + k-mer]).
 cudaError_t launch_bucket_apply(int storage, const TableParams& tp, const BucketParams& bp,
                                 const uint64_t* recs, const uint32_t* start, uint32_t* new_bits,
-                                unsigned long long* counters, cudaStream_t st);
+                                unsigned long long* counters, uint8_t* vals, cudaStream_t st);
+// Per-k-mer insert_and_query counts from vals and the new-k-mer bitmask.
+cudaError_t launch_iq_counts(const uint8_t* vals, uint64_t cap, uint32_t n_tables,
+                             const uint32_t* new_bits, const uint64_t* total, int16_t* counts,
+                             bool presence, cudaStream_t st);
 cudaError_t launch_bucket_read_new(const uint64_t* kofs, uint64_t n_reads, const uint32_t* new_bits,
                                    uint64_t* n_new, unsigned long long* counters, cudaStream_t st);
 uint64_t scan32_partials_needed(uint64_t n);
@@ -77,5 +83,11 @@ cudaError_t launch_task_map(const uint64_t* tofs, uint64_t n_reads, uint64_t cap
                             uint32_t* task_read, cudaStream_t st);
 cudaError_t launch_tile_map(const uint64_t* kofs, uint64_t n_reads, uint64_t n_tiles,
                             uint32_t* tile_read, cudaStream_t st);
+
+// OR-merge of two identically laid out table allocations (n_words, a
+// multiple of 4); cells newly set in the first count_words words are added
+// to *occupied.
+cudaError_t launch_or_merge(uint32_t* dst, const uint32_t* src, uint64_t n_words,
+                            uint64_t count_words, unsigned long long* occupied, cudaStream_t st);
 
 }  // namespace gdbg

@@ -15,6 +15,7 @@ Differences from the reference, all deliberate:
     and device buffers; they are the fast path.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -67,8 +68,23 @@ class CanLemireShifter:
     hash_type = Canonical
 
 
+class _Handle:
+    """Owns one C-ABI handle (gdbg_destroy on collection)."""
+
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value and _lib._lib is not None:
+            _lib._lib.gdbg_destroy(h)
+            self.h = None
+
+
 class _Storage:
-    """Storage parameters; the device tables belong to the graph built on it."""
+    """Storage parameters plus, once a graph is built on it, the device
+    tables: like the reference's shared_ptr<Storage> (dbg.hh:97-101), every
+    dBG built on the same storage object shares its tables and counters."""
     kind = None
     is_counting = False
     is_probabilistic = True
@@ -86,6 +102,13 @@ class _Storage:
                       out.ctypes.data_as(_lib.u64p), _c.byref(got))
             self.tablesizes = [int(v) for v in out[:got.value]]
         self.build_params = (max_table, N)
+        self._anchor = None      # a handle on the device tables, once built
+
+    def _attach(self, h, shifter_kind, K):
+        """Keep the tables of handle h alive with this storage object."""
+        a = _c.c_void_p()
+        _lib.call("gdbg_share_storage", h, shifter_kind, int(K), _c.byref(a))
+        self._anchor = _Handle(a)
 
     @classmethod
     def build(cls, *args):
@@ -180,10 +203,16 @@ class dBGBase:
         """dBG::build(storage, K) (dbg.hh:108-121)."""
         if isinstance(storage, type):
             storage = storage.build()
-        sizes = np.asarray(storage.tablesizes, np.uint64)
         h = _c.c_void_p()
+        if storage._anchor is not None:
+            # a storage already in use: share its tables
+            _lib.call("gdbg_share_storage", storage._anchor.h, cls.shifter_type.kind, int(K),
+                      _c.byref(h))
+            return cls(h, K, storage)
+        sizes = np.asarray(storage.tablesizes, np.uint64)
         _lib.call("gdbg_create_sized", storage.kind, cls.shifter_type.kind, int(K),
                   _p(sizes, _lib.u64p), len(sizes), _c.byref(h))
+        storage._attach(h, cls.shifter_type.kind, K)
         return cls(h, K, storage)
 
     def __del__(self):
@@ -194,10 +223,14 @@ class dBGBase:
 
     # -- storage-level -----------------------------------------------------
     def clone(self):
-        """Empty graph with the same table shape (dbg.hh:128-131)."""
+        """Empty graph on a new storage of the same table shape
+        (dbg.hh:128-131, bitstorage.hh:136-138)."""
         h = _c.c_void_p()
         _lib.call("gdbg_clone", self._h, _c.byref(h))
-        return type(self)(h, self.K, self.storage)
+        storage = type(self.storage)(tablesizes=self.storage.tablesizes)
+        storage.build_params = self.storage.build_params
+        storage._attach(h, self.shifter_type.kind, self.K)
+        return type(self)(h, self.K, storage)
 
     shallow_clone = clone
 
@@ -238,6 +271,69 @@ class dBGBase:
     def set_raw(self, tables):
         flat = np.ascontiguousarray(np.concatenate([np.asarray(t, np.uint8) for t in tables]))
         _lib.call("gdbg_set_tables", self._h, _p(flat, _lib.u8p), flat.size)
+
+    def update_from(self, other):
+        """BitStorage::update_from (bitstorage.cc:103-137), reached in the
+        reference as graph.storage.update_from(other.storage): OR-merge
+        other's Bit tables into this graph's."""
+        _lib.call("gdbg_update_from", self._h, other._h)
+
+    # -- OXLI files ----------------------------------------------------------
+    def _gz(self, filename):
+        # ByteStorageFile::save/load pick the gzip writer/reader by a ".gz"
+        # suffix (bytestorage.cc:153-168, 640-657); Bit and Nibble files are
+        # plain whatever the name.
+        return self.storage_type is ByteStorage and str(filename).rsplit(".", 1)[-1] == "gz"
+
+    def save(self, filename):
+        """dBG::save (dbg.hh:396-398): the tables as an OXLI v4 file."""
+        filename = os.fspath(filename)
+        if not self._gz(filename):
+            _lib.call("gdbg_save", self._h, filename.encode())
+            return
+        import gzip
+        import shutil
+        import tempfile
+        with tempfile.NamedTemporaryFile(dir=os.path.dirname(os.path.abspath(filename)),
+                                         delete=False) as tmp:
+            plain = tmp.name
+        try:
+            _lib.call("gdbg_save", self._h, plain.encode())
+            with open(plain, "rb") as src, gzip.open(filename, "wb") as dst:
+                shutil.copyfileobj(src, dst, 16 << 20)
+        finally:
+            os.unlink(plain)
+
+    def load(self, filename):
+        """dBG::load (dbg.hh:400-403): replace the tables (and their sizes)
+        by an OXLI v4 file's; K stays, the file's ksize is returned."""
+        filename = os.fspath(filename)
+        ks = _lib.c_u16()
+        if not self._gz(filename):
+            _lib.call("gdbg_load", self._h, filename.encode(), _c.byref(ks))
+        else:
+            import gzip
+            import shutil
+            import tempfile
+            with tempfile.NamedTemporaryFile(delete=False) as tmp:
+                plain = tmp.name
+            try:
+                try:
+                    with gzip.open(filename, "rb") as src, open(plain, "wb") as dst:
+                        shutil.copyfileobj(src, dst, 16 << 20)
+                except (OSError, EOFError) as e:
+                    raise _lib.GoetiaFileException(_lib.ERR_IO,
+                                                   f"K-mer count file read error: {filename} {e}")
+                _lib.call("gdbg_load", self._h, plain.encode(), _c.byref(ks))
+            finally:
+                os.unlink(plain)
+        sizes = np.zeros(32, np.uint64)
+        n = _lib.c_u16()
+        _lib.call("gdbg_info", self._h, None, None, None, _c.byref(n))
+        _lib.call("gdbg_get_tablesizes", self._h, _p(sizes, _lib.u64p))
+        new = [int(x) for x in sizes[:n.value]]
+        self.storage.tablesizes = new         # shared with every graph on it
+        return int(ks.value)
 
     # -- hashing -----------------------------------------------------------
     def _wrap(self, value, fw, rc):
@@ -333,9 +429,9 @@ class dBGBase:
         s = _b(sequence)
         if len(out) == 2:
             hashes, counts = out
-            for h in self.hashes(s):
-                hashes.append(h)
-                counts.append(self.insert_and_query(int(h)))
+            hs = self.hashes(s)
+            hashes.extend(hs)
+            counts.extend(self.insert_and_query_sequence(s))
             return len(s) - self.K + 1
         if len(out) == 1 and isinstance(out[0], (list, set)):
             vals = list(self.hashes(s))
@@ -361,7 +457,14 @@ class dBGBase:
 
     def insert_and_query_sequence(self, sequence):
         """Post-insertion counts, k-mer by k-mer (dbg.hh:327-340)."""
-        return [self.insert_and_query(int(h)) for h in self.hashes(sequence)]
+        s = _b(sequence)
+        n = len(s) - self.K + 1
+        if n < 1:
+            raise _lib.SequenceLengthException(_lib.ERR_SEQUENCE_LENGTH,
+                                               "Sequence must have length >= K")
+        c = np.zeros(n, np.int16)
+        _lib.call("gdbg_insert_and_query_sequence", self._h, s, len(s), _p(c, _lib.i16p), None)
+        return [int(x) for x in c]
 
     def query_sequence(self, sequence, counts=None, hashes=None):
         """dBG::query_sequence (dbg.hh:349-394)."""
@@ -470,6 +573,17 @@ class dBGBase:
                   _p(r.offsets, _lib.u64p), r.n_reads, _p(n_new, _lib.u64p), _c.byref(nk))
         return n_new[:r.n_reads]
 
+    def insert_and_query_packed(self, reads):
+        """insert_and_query_sequence for every read in order: (flattened
+        counts, per-read new counts), equal to the sequential calls."""
+        r = self._packed(reads)
+        n = r.n_kmers(self.K)
+        c = np.zeros(max(n, 1), np.int16)
+        n_new = np.zeros(max(r.n_reads, 1), np.uint64)
+        _lib.call("gdbg_insert_and_query_batch", self._h, _p(r.packed, _lib.u32p), r.packed.size,
+                  _p(r.offsets, _lib.u64p), r.n_reads, _p(c, _lib.i16p), _p(n_new, _lib.u64p))
+        return c[:n], n_new[:r.n_reads]
+
     def query_packed(self, reads):
         r = self._packed(reads)
         c = np.zeros(max(r.n_kmers(self.K), 1), np.int16)
@@ -509,6 +623,12 @@ class dBGBase:
         hint = (1 << 64) - 1 if n_kmers is None else int(n_kmers)
         _lib.call("gdbg_insert_batch_device", self._h, packed_ptr, int(packed_words), offsets_ptr,
                   int(n_reads), hint, n_new_ptr, _stream(stream))
+
+    def insert_and_query_device(self, packed_ptr, packed_words, offsets_ptr, n_reads, counts_ptr,
+                                n_new_ptr=None, n_kmers=None, stream=None):
+        hint = (1 << 64) - 1 if n_kmers is None else int(n_kmers)
+        _lib.call("gdbg_insert_and_query_batch_device", self._h, packed_ptr, int(packed_words),
+                  offsets_ptr, int(n_reads), hint, counts_ptr, n_new_ptr, _stream(stream))
 
     def query_device(self, packed_ptr, packed_words, offsets_ptr, n_reads, counts_ptr,
                      n_kmers=None, stream=None):

@@ -14,7 +14,11 @@ samples at once on one GPU:
   `depth` chunks of a stream in flight, so chunks of different streams overlap
   on the device while each stream's chunks apply in arrival order;
 * completion: events are polled; a chunk's latency is completion time minus
-  arrival time.
+  arrival time;
+* release: a finished stream's budget share is returned at once, but its
+  device memory is freed lazily -- only when an admission needs the room, or
+  at the end of the run -- because freeing device memory waits for every
+  stream's in-flight work and would stall the dispatch of all other streams.
 
 Per-chunk new counts equal a sequential replay of each stream, whatever the
 mix (tests/test_gpu_serving.py).
@@ -137,11 +141,15 @@ class Server:
         order = sorted(specs, key=lambda s: s.arrivals[0])
         waiting = collections.deque(order)       # not yet admitted
         active = {}
+        zombies = []                             # finished, memory not yet freed
+        zombie_bytes = 0
         used = 0
         peak_used = 0
         results = {}
         admitted_at = {}
         waited = set()
+        freed_at = []
+        admit_s, dispatch_s, delay = [], [], []    # host-side timings
         total_kmers = 0
         lat = []
         t0 = time.perf_counter()
@@ -160,11 +168,17 @@ class Server:
                 if used + need > self.budget:
                     waited.add(spec.sid)
                     break
+                if zombies and used + zombie_bytes + need > self.budget:
+                    zombies.clear()                 # frees their device memory
+                    zombie_bytes = 0
+                    freed_at.append(now)
                 waiting.popleft()
+                ta = time.perf_counter()
                 st = _Stream(spec, self)
+                admit_s.append(time.perf_counter() - ta)
                 st.need = need
                 used += need
-                peak_used = max(peak_used, used)
+                peak_used = max(peak_used, used + zombie_bytes)   # held on the device
                 active[spec.sid] = st
                 admitted_at[spec.sid] = now
             # dispatch arrived chunks
@@ -174,6 +188,8 @@ class Server:
                        and spec.arrivals[st.next_chunk] <= now):
                     i = st.next_chunk
                     c = spec.chunks[i]
+                    td = time.perf_counter()
+                    delay.append((td - t0) / time_scale - spec.arrivals[i])
                     slot = st.slots[st.free.popleft()]
                     nw, nr = c.packed.size, c.n_reads
                     slot.h_packed[:nw].numpy()[:] = c.packed.view(np.int32)
@@ -191,6 +207,7 @@ class Server:
                         ev.record(st.cuda)
                     st.inflight.append((ev, st.slots.index(slot), i))
                     st.next_chunk += 1
+                    dispatch_s.append(time.perf_counter() - td)
                     if first_dispatch is None:
                         first_dispatch = time.perf_counter()
             # completions (in order per stream)
@@ -213,12 +230,14 @@ class Server:
                     finished.append(sid)
             for sid in finished:
                 st = active.pop(sid)
-                st.graph.synchronize()
                 results[sid] = st.results
                 used -= st.need
+                zombies.append(st)
+                zombie_bytes += st.need
                 del st
         lat_ms = np.array(lat) * 1000.0 * time_scale
         span = (last_done - first_dispatch) if first_dispatch and last_done else 0.0
+        zombies.clear()
         stats = {
             "chunks": len(lat),
             "kmers": total_kmers,
@@ -228,7 +247,15 @@ class Server:
             "max_ms": float(lat_ms.max()) if len(lat_ms) else 0.0,
             "peak_hbm_bytes": peak_used,
             "admission_waits": len(waited),
+            "lazy_frees": len(freed_at),
             "wall_s": span,
+            # host side: stream admission (graph creation), per-chunk dispatch
+            # work, and the wait from a chunk's arrival to its dispatch
+            "admit_ms_max": 1e3 * max(admit_s) if admit_s else 0.0,
+            "admit_ms_total": 1e3 * sum(admit_s),
+            "dispatch_ms_p99": float(np.percentile(dispatch_s, 99)) * 1e3 if dispatch_s else 0.0,
+            "dispatch_delay_ms_p99": (float(np.percentile(delay, 99)) * 1e3 * time_scale
+                                      if delay else 0.0),
         }
         return results, stats
 

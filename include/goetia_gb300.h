@@ -76,6 +76,14 @@ int gdbg_create_sized(int storage, int shifter, uint16_t K, const uint64_t* size
 int gdbg_destroy(gdbg_graph* g);
 /* dBG::clone: a new graph with empty storage of the same shape (dbg.hh:128-131). */
 int gdbg_clone(const gdbg_graph* g, gdbg_graph** out);
+/* dBG::build(storage, K) on a storage that a graph already uses: the
+ * reference's dBGs hold a shared_ptr<Storage> (dbg.hh:73, 97-101), so every
+ * graph built on one storage inserts into and queries the same tables.  The
+ * new handle shares g's device tables, table sizes and n_unique/n_occupied
+ * counters (reference-counted: the tables are freed with the last handle);
+ * its shifter, K, stream and scratch are its own.  Calls on handles that
+ * share a storage must be ordered by the caller, like calls on one handle. */
+int gdbg_share_storage(const gdbg_graph* g, int shifter, uint16_t K, gdbg_graph** out);
 /* dBG::reset / Storage::reset: zero every table (bitstorage.cc:140-148).
  * Like the reference, the n_unique / n_occupied counters are kept. */
 int gdbg_reset(gdbg_graph* g);
@@ -89,6 +97,28 @@ int gdbg_get_tables(gdbg_graph* g, uint8_t* out, uint64_t out_len);
 int gdbg_set_tables(gdbg_graph* g, const uint8_t* in, uint64_t in_len);
 /* dBG::n_unique / n_occupied (dbg.hh:184-196). */
 int gdbg_stats(gdbg_graph* g, uint64_t* n_unique, uint64_t* n_occupied);
+/* dBG::save (dbg.hh:396-398) -> Storage::save: the OXLI v4 file of the
+ * tables (bitstorage.cc:151-186, bytestorage.cc:480-521 with no bigcount
+ * entries, nibblestorage.cc:132-166), byte-identical to the reference's for
+ * the same tables.  Always a plain file: a ".gz" name is not compressed here
+ * (the Python mirror compresses ByteStorage ".gz" files itself). */
+int gdbg_save(gdbg_graph* g, const char* path);
+/* dBG::load (dbg.hh:400-403) -> Storage::load (bitstorage.cc:188-307,
+ * bytestorage.cc:172-290, nibblestorage.cc:168-250): checks signature,
+ * version and file type (GDBG_ERR_IO with the reference's messages), takes
+ * the file's table sizes (reallocating the tables when they differ) and
+ * occupied-bin count; n_unique and K are kept, the file's ksize is returned
+ * in *ksize (may be NULL).  The file is checked to be complete before any
+ * state changes.  Byte files with use_bigcount set or bigcount entries are
+ * GDBG_ERR_UNSUPPORTED (counts saturate at 255 here). */
+int gdbg_load(gdbg_graph* g, const char* path, uint16_t* ksize);
+/* BitStorage::update_from (bitstorage.cc:103-137): OR other's tables into
+ * g's; n_occupied grows by the table-0 cells newly set, n_unique is kept.
+ * Bit graphs only (GDBG_ERR_UNSUPPORTED otherwise, as the reference has no
+ * Byte/Nibble update_from); different table sizes are GDBG_ERR_INVALID_ARG
+ * ("both nodegraphs must have same table sizes").  Ordered after the work
+ * queued on both handles' streams; returns when the merge is done. */
+int gdbg_update_from(gdbg_graph* g, const gdbg_graph* other);
 /* Use the caller's CUDA stream (cudaStream_t) for this handle; NULL restores
  * the handle's own stream. */
 int gdbg_set_stream(gdbg_graph* g, void* stream);
@@ -104,6 +134,11 @@ int gdbg_hash(gdbg_graph* g, const char* kmer, uint64_t len, uint64_t* value,
  * in *n_kmers and the number of new k-mers in *n_new (either may be NULL). */
 int gdbg_insert_sequence(gdbg_graph* g, const char* seq, uint64_t len,
                          uint64_t* n_kmers, uint64_t* n_new);
+/* dBG::insert_and_query_sequence (dbg.hh:327-340): counts (len-K+1 entries)
+ * get each k-mer's insert_and_query result in order; n_new (may be NULL) the
+ * number of new k-mers.  Same limits as gdbg_insert_and_query_batch. */
+int gdbg_insert_and_query_sequence(gdbg_graph* g, const char* seq, uint64_t len,
+                                   int16_t* counts, uint64_t* n_new);
 /* dBG::query_sequence(seq, counts, hashes) (dbg.hh:364-376); counts holds
  * len-K+1 entries, hashes may be NULL. */
 int gdbg_query_sequence(gdbg_graph* g, const char* seq, uint64_t len, int16_t* counts,
@@ -142,6 +177,16 @@ int gdbg_insert_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
 /* query_sequence for every read (dbg.hh:349-362): flattened counts. */
 int gdbg_query_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                      const uint64_t* offsets, uint64_t n_reads, int16_t* counts);
+/* insert_and_query_sequence for every read, in batch order (dbg.hh:327-340;
+ * also the counts of insert_sequence(seq, hashes, counts), dbg.hh:249-265):
+ * per k-mer 1 if it was new, else the storage's count right after its own
+ * insert (bytestorage.cc:142-150, nibblestorage.cc:103-109; always 1 for
+ * BitStorage, bitstorage.cc:78-84), exactly as sequential calls would
+ * return.  n_new (may be NULL) gets the per-read new counts.  Needs at most
+ * 8 tables of at most 2^32 cells in total (GDBG_ERR_UNSUPPORTED otherwise). */
+int gdbg_insert_and_query_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                                const uint64_t* offsets, uint64_t n_reads, int16_t* counts,
+                                uint64_t* n_new);
 /* get_hash_iter for every read: flattened values (and fw/rc, may be NULL). */
 int gdbg_hashes_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                       const uint64_t* offsets, uint64_t n_reads, uint64_t* values,
@@ -165,6 +210,10 @@ int gdbg_insert_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t pac
 int gdbg_query_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                             const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
                             int16_t* counts, void* stream);
+int gdbg_insert_and_query_batch_device(gdbg_graph* g, const uint32_t* packed,
+                                       uint64_t packed_words, const uint64_t* offsets,
+                                       uint64_t n_reads, uint64_t n_kmers_hint, int16_t* counts,
+                                       uint64_t* n_new, void* stream);
 int gdbg_hashes_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                              const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
                              uint64_t* values, uint64_t* fw, uint64_t* rc, void* stream);

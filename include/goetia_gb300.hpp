@@ -40,6 +40,9 @@ struct SequenceLengthException : GoetiaException {
 struct InvalidSequenceException : GoetiaException {
     explicit InvalidSequenceException(const std::string& m) : GoetiaException(m) {}
 };
+struct GoetiaFileException : GoetiaException {   // goetia.hh:155-160
+    explicit GoetiaFileException(const std::string& m) : GoetiaException(m) {}
+};
 
 inline void check(int rc) {
     if (rc == GDBG_OK) return;
@@ -47,6 +50,7 @@ inline void check(int rc) {
     if (rc == GDBG_ERR_SEQUENCE_LENGTH) throw SequenceLengthException(msg);
     if (rc == GDBG_ERR_INVALID_SEQUENCE) throw InvalidSequenceException(msg);
     if (rc == GDBG_ERR_OOM) throw std::bad_alloc();
+    if (rc == GDBG_ERR_IO) throw GoetiaFileException(msg);
     throw GoetiaException(msg);
 }
 
@@ -159,6 +163,22 @@ public:
         return seq.size() - K_ + 1;
     }
 
+    uint64_t insert_sequence(const std::string& seq, std::vector<hash_type>& hashes,
+                             std::vector<count_t>& counts) {
+        auto hs = get_hashes(seq);
+        auto c = insert_and_query_sequence(seq);
+        hashes.insert(hashes.end(), hs.begin(), hs.end());
+        counts.insert(counts.end(), c.begin(), c.end());
+        return seq.size() - K_ + 1;
+    }
+    // dBG::insert_and_query_sequence (dbg.hh:327-340)
+    std::vector<count_t> insert_and_query_sequence(const std::string& seq) {
+        if (seq.size() < K_) throw SequenceLengthException("Sequence must have length >= K");
+        std::vector<count_t> counts(seq.size() - K_ + 1);
+        check(gdbg_insert_and_query_sequence(g_, seq.data(), seq.size(), counts.data(), nullptr));
+        return counts;
+    }
+
     // dBG::query_sequence (dbg.hh:349-376)
     std::vector<count_t> query_sequence(const std::string& seq) {
         if (seq.size() < K_) throw SequenceLengthException("Sequence must have length >= K");
@@ -219,6 +239,14 @@ public:
         return o;
     }
     void reset() { check(gdbg_reset(g_)); }
+    // BitStorage::update_from (bitstorage.cc:103-137): OR-merge other's tables
+    void update_from(const GpuDBG& other) { check(gdbg_update_from(g_, other.g_)); }
+    // dBG::save / dBG::load (dbg.hh:396-403): OXLI v4 table files
+    void save(const std::string& filename) { check(gdbg_save(g_, filename.c_str())); }
+    void load(const std::string& filename) {
+        uint16_t ksize = 0;
+        check(gdbg_load(g_, filename.c_str(), &ksize));
+    }
     std::vector<uint64_t> get_tablesizes() const {
         uint16_t n = 0;
         check(gdbg_info(g_, nullptr, nullptr, nullptr, &n));

@@ -198,3 +198,66 @@ def pack_ascii(seqs, min_length=0):
     kept = lib().orc_pack_ascii(data, _p(so, u64p), len(seqs), min_length, _p(packed, u32p),
                                 _p(offsets, u64p), ctypes.byref(skipped))
     return packed, offsets[:kept + 1].copy(), int(skipped.value)
+
+
+# ---- OXLI v4 table files ----------------------------------------------------
+# The layout written by Storage::save and read by Storage::load:
+#   "OXLI", version 4 (u8), file type (u8: 2 = BitStorage, bitstorage.cc:151-186;
+#   1 = ByteStorage, bytestorage.cc:480-521; 7 = NibbleStorage,
+#   nibblestorage.cc:132-166; codes from storage.hh:63-72),
+#   [ByteStorage only: use_bigcount (u8)], ksize (u32), n_tables (u8),
+#   occupied_bins (u64), then per table: table size in cells (u64) and the
+#   table bytes (size/8+1, size, size/2+1), [ByteStorage only: the number of
+#   bigcount entries (u64) and the entries].  Little-endian throughout.
+
+OXLI_TYPE = {BIT: 2, BYTE: 1, NIBBLE: 7}
+
+
+def oxli_bytes(kind, K, sizes, tables, n_occupied):
+    """The file Storage::save writes for these tables (bytes)."""
+    kind = KINDS[kind] if isinstance(kind, str) else kind
+    out = [b"OXLI", bytes([4, OXLI_TYPE[kind]])]
+    if kind == BYTE:
+        out.append(b"\x00")
+    out.append(np.array([K], "<u4").tobytes())
+    out.append(bytes([len(sizes)]))
+    out.append(np.array([n_occupied], "<u8").tobytes())
+    for s, t in zip(sizes, tables):
+        out.append(np.array([s], "<u8").tobytes())
+        out.append(np.ascontiguousarray(t, np.uint8).tobytes())
+    if kind == BYTE:
+        out.append(np.zeros(1, "<u8").tobytes())
+    return b"".join(out)
+
+
+def parse_oxli(data):
+    """Inverse of oxli_bytes: (kind, K, sizes, tables, n_occupied)."""
+    data = bytes(data)
+    if data[:4] != b"OXLI" or data[4] != 4:
+        raise ValueError("not an OXLI v4 file")
+    kind = {v: k for k, v in OXLI_TYPE.items()}[data[5]]
+    pos = 6
+    if kind == BYTE:
+        pos += 1
+    K = int(np.frombuffer(data, "<u4", 1, pos)[0])
+    n = data[pos + 4]
+    occ = int(np.frombuffer(data, "<u8", 1, pos + 5)[0])
+    pos += 13
+    sizes, tables = [], []
+    for _ in range(n):
+        s = int(np.frombuffer(data, "<u8", 1, pos)[0])
+        nb = s // 8 + 1 if kind == BIT else s // 2 + 1 if kind == NIBBLE else s
+        sizes.append(s)
+        tables.append(np.frombuffer(data, np.uint8, nb, pos + 8).copy())
+        pos += 8 + nb
+    return kind, K, sizes, tables, occ
+
+
+def update_from(tables_a, tables_b, occupied_a):
+    """BitStorage::update_from (bitstorage.cc:103-137): byte-wise OR of B
+    into A; occupied_bins grows by popcount(old ^ merged) over table 0."""
+    if [len(t) for t in tables_a] != [len(t) for t in tables_b]:
+        raise ValueError("both nodegraphs must have same table sizes")
+    merged = [np.bitwise_or(a, b) for a, b in zip(tables_a, tables_b)]
+    added = int(np.unpackbits(np.bitwise_xor(tables_a[0], merged[0])).sum())
+    return merged, occupied_a + added

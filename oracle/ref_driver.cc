@@ -20,7 +20,12 @@
 //     bit 4+i = right extension present, from set_cursor + left/right_extensions
 //     + query (hashextender.hh:352-396, unitig_walker.hh:361-397);
 // plus find_decision_kmers positions (unitig_walker.hh:1025-1045), the raw
-// table bytes (get_raw) and n_unique / n_occupied.
+// table bytes (get_raw), n_unique / n_occupied, and the OXLI file written by
+// dBG::save (dbg.hh:396-398 -> Storage::save, bitstorage.cc:151-186,
+// bytestorage.cc:480-521, nibblestorage.cc:132-166) as saved.oxli, the
+// insert_and_query_sequence counts of all reads on fresh tables, and for
+// Bit storages the tables and counters after BitStorage::update_from
+// (bitstorage.cc:103-137) of two half-read graphs.
 #include "goetia/dbg.hh"
 #include "goetia/storage/bitstorage.hh"
 #include "goetia/storage/bytestorage.hh"
@@ -32,6 +37,7 @@
 #include <fstream>
 #include <iostream>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 using namespace goetia;
@@ -124,6 +130,41 @@ static int run(uint16_t K, uint16_t n_tables, uint64_t max_table,
     }
     std::vector<uint64_t> stats = {graph->n_unique(), graph->n_occupied()};
     dump(out + "/stats.u64", stats);
+    graph->save(out + "/saved.oxli");
+
+    // dBG::insert_and_query_sequence (dbg.hh:327-340) per read on fresh tables
+    {
+        auto s2 = Storage::build(max_table, n_tables);
+        auto g2 = dBG<Storage, Shifter>::build(s2, K);
+        std::vector<int16_t> iq;
+        for (const auto& s : reads) {
+            if (s.size() < K) continue;
+            auto c = g2->insert_and_query_sequence(s);
+            iq.insert(iq.end(), c.begin(), c.end());
+        }
+        dump(out + "/iq_counts.i16", iq);
+    }
+
+    // BitStorage::update_from (bitstorage.cc:103-137): graph A holds the first
+    // half of the reads, graph B the second half; A |= B.
+    if constexpr (std::is_same<Storage, BitStorage>::value) {
+        auto sa = Storage::build(max_table, n_tables), sb = Storage::build(max_table, n_tables);
+        auto ga = dBG<Storage, Shifter>::build(sa, K), gb = dBG<Storage, Shifter>::build(sb, K);
+        for (size_t r = 0; r < reads.size(); ++r) {
+            if (reads[r].size() < K) continue;
+            (r < reads.size() / 2 ? ga : gb)->insert_sequence(reads[r]);
+        }
+        std::vector<uint64_t> pre = {ga->n_unique(), ga->n_occupied(), gb->n_unique(), gb->n_occupied()};
+        sa->update_from(*sb);
+        pre.push_back(ga->n_unique());
+        pre.push_back(ga->n_occupied());
+        dump(out + "/merge_stats.u64", pre);
+        uint8_t** mraw = ga->get_raw();
+        std::vector<uint8_t> merged;
+        for (size_t i = 0; i < sizes.size(); ++i)
+            merged.insert(merged.end(), mraw[i], mraw[i] + sizes[i] / 8 + 1);
+        dump(out + "/merged.u8", merged);
+    }
     return 0;
 }
 

@@ -3,8 +3,10 @@
 Runs oracle/_ref/ref_driver (goetia's own C++ hot path, compiled from the
 reference sources by ``make -C oracle ref``) on seeded read sets and stores
 its answers: k-mer hashes, per-read new-k-mer counts, table bytes,
-query_sequence counts, neighbour masks, find_decision_kmers positions and
-n_unique / n_occupied.  The cases cover every storage kind, both shifters,
+query_sequence counts, neighbour masks, find_decision_kmers positions,
+n_unique / n_occupied, the OXLI file written by dBG::save, the
+insert_and_query_sequence counts and (Bit) the
+tables after BitStorage::update_from of two half-read graphs.  The cases cover every storage kind, both shifters,
 K = 21, 27, 31, 64 (rotation by K mod 64 == 0) and 101 (K > 64), short
 reads, duplicate reads, reverse-complement reads, tiny tables (collisions)
 and homopolymers (Byte saturation at 255, Nibble at 15).
@@ -93,6 +95,11 @@ def run_case(case, workdir):
     tables = [rd(f"table{i}.u8", np.uint8) for i in range(len(sizes))]
     data["tables"] = np.concatenate(tables)
     data["table_bytes"] = np.array([len(t) for t in tables], np.uint64)
+    data["oxli"] = rd("saved.oxli", np.uint8)
+    data["iq_counts"] = rd("iq_counts.i16", np.int16)
+    if kind == "bit":
+        data["merge_stats"] = rd("merge_stats.u64", np.uint64)
+        data["merged"] = rd("merged.u8", np.uint8)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
     return name, len(data["val"])
 

@@ -35,6 +35,13 @@ class Case:
         tb = d["table_bytes"].astype(np.int64)
         t = d["tables"]
         self.tables = [t[a:b] for a, b in zip(np.r_[0, np.cumsum(tb)[:-1]], np.cumsum(tb))]
+        self.oxli = d["oxli"].tobytes()     # the file dBG::save wrote
+        self.iq_counts = d["iq_counts"]      # insert_and_query_sequence, fresh tables
+        # Bit only: A (first half of the reads) after A.update_from(B)
+        self.merge_stats = d["merge_stats"] if "merge_stats" in d else None
+        if "merged" in d:
+            self.merged = [d["merged"][a:b] for a, b in
+                           zip(np.r_[0, np.cumsum(tb)[:-1]], np.cumsum(tb))]
 
     def packed(self):
         """2-bit packed batch of the reads (all of them are pure ACGT)."""

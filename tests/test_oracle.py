@@ -65,6 +65,30 @@ def test_oracle_matches_golden(name):
     masks = st.decision_masks(c.canonical, c.K, packed, off)
     assert np.array_equal(masks, c.masks)
     assert c.decision_positions(masks) == c.dpos
+    # insert_and_query_sequence per read on fresh tables
+    st2 = oracle.Storage(c.storage, c.sizes)
+    assert np.array_equal(st2.insert_and_query_reads(c.canonical, c.K, packed, off), c.iq_counts)
+    # the OXLI file written by the reference's dBG::save, byte for byte
+    u, o = st.stats()
+    assert oracle.oxli_bytes(c.storage, c.K, c.sizes, st.tables(), o) == c.oxli
+    kind, K, sizes, tables, occ = oracle.parse_oxli(c.oxli)
+    assert (K, occ, sizes) == (c.K, c.n_occupied, [int(x) for x in c.sizes])
+    assert all(np.array_equal(a, b) for a, b in zip(tables, c.tables))
+
+
+@pytest.mark.parametrize("name", [n for n in names() if n.startswith("bit")])
+def test_oracle_update_from_matches_golden(name):
+    c = Case(name)
+    half = len(c.reads) // 2
+    sa, sb = oracle.Storage("bit", c.sizes), oracle.Storage("bit", c.sizes)
+    for st, part in ((sa, c.reads[:half]), (sb, c.reads[half:])):
+        packed, off, _ = oracle.pack_ascii(part)
+        st.insert_reads(c.canonical, c.K, packed, off)
+    (ua, oa), (ub, ob) = sa.stats(), sb.stats()
+    assert [ua, oa, ub, ob] == [int(x) for x in c.merge_stats[:4]]
+    merged, occ = oracle.update_from(sa.tables(), sb.tables(), oa)
+    assert occ == int(c.merge_stats[5]) and ua == int(c.merge_stats[4])
+    assert all(np.array_equal(a, b) for a, b in zip(merged, c.merged))
 
 
 def test_pack_policy():
