@@ -571,7 +571,9 @@ def run_gpu(args):
                        "reads_per_step": int(batches[0].n_reads), "read_len": READ_LEN,
                        "genome_bp": GENOME_LEN, "substitution_rate": SUB_RATE,
                        "n_reads_dropped_per_step": int(batches[0].n_skipped),
-                       "insert_path": "bucketed" if "k_bkt_apply" in stages else "persistent",
+                       "insert_path": ("bucketed (segmented)" if "k_sp_apply" in stages else
+                                       "bucketed (ordered)" if "k_bkt_apply" in stages else
+                                       "windowed"),
                        "l2": "inputs larger than L2: 4 GiB of tables, random cells",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "k-mers/s", "h2d_bytes_per_step": h2d // args.steps,

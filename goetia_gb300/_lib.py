@@ -22,7 +22,7 @@ ERR_UNSUPPORTED = 8
 
 BIT, BYTE, NIBBLE = 0, 1, 2
 FWD_LEMIRE, CAN_LEMIRE = 0, 1
-PATH_PERSISTENT, PATH_WINDOWED, PATH_BUCKETED, PATH_AUTO = 0, 1, 2, 3
+PATH_PERSISTENT, PATH_WINDOWED, PATH_BUCKETED, PATH_AUTO, PATH_BUCKETED_ORDERED = 0, 1, 2, 3, 4
 
 c_u64 = ctypes.c_uint64
 c_u32 = ctypes.c_uint32

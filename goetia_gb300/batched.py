@@ -91,7 +91,8 @@ class BatchedInserter:
         self.use_graph = use_graph
         if use_graph:
             if bucketed_fits(graph, self.max_kmers, getattr(graph, "_bucket_bits", 0)):
-                graph.set_insert_path("bucketed")
+                if not str(graph.insert_path()).startswith("bucketed"):
+                    graph.set_insert_path("bucketed")
             else:
                 self.use_graph = False
         self.cuda_graph = None
@@ -178,12 +179,14 @@ def _key(graph, max_reads, max_bases):
 
 
 def candidates(storage_type, use_graph=True):
-    """Schedules tried by the autotuner: the bucketed path at three bucket
-    sizes, and -- without graph replay -- the windowed path at two windows
-    and two k-mers per thread."""
+    """Schedules tried by the autotuner: the segmented bucketed path at its
+    adaptive bucket size, the ordered bucketed path at three bucket sizes,
+    and -- without graph replay -- the windowed path at two windows and two
+    k-mers per thread."""
     from . import dbg as D
     fs0 = {D.BitStorage: 19, D.ByteStorage: 16, D.NibbleStorage: 17}[storage_type]
-    out = [{"path": "bucketed", "bucket_bits": fs} for fs in (fs0 - 1, fs0, fs0 + 1)]
+    out = [{"path": "bucketed", "bucket_bits": 0}]
+    out += [{"path": "bucketed_ordered", "bucket_bits": fs} for fs in (fs0 - 1, fs0, fs0 + 1)]
     if not use_graph:
         out += [{"path": "windowed", "window": w, "kpt": k}
                 for w in (262144, 1048576) for k in (4, 8)]
@@ -192,7 +195,7 @@ def candidates(storage_type, use_graph=True):
 
 def apply_schedule(graph, sched):
     graph.set_insert_path(sched["path"])
-    if sched["path"] == "bucketed":
+    if sched["path"].startswith("bucketed"):
         graph.set_bucket_bits(sched["bucket_bits"])
         graph._bucket_bits = sched["bucket_bits"]
     else:
@@ -223,8 +226,8 @@ def autotune(graph, sample, max_reads, max_bases, repeats=2, use_cache=True, ver
         g = graph.clone()
         try:
             apply_schedule(g, sched)
-            if sched["path"] == "bucketed" and not bucketed_fits(g, max(max_bases - g.K + 1, 1),
-                                                                 sched["bucket_bits"]):
+            if sched["path"].startswith("bucketed") and not bucketed_fits(
+                    g, max(max_bases - g.K + 1, 1), sched["bucket_bits"]):
                 continue
             ins = BatchedInserter(g, max_reads, max_bases, use_graph=use_graph).prepare()
             ins.insert(sample)                       # warm state

@@ -127,6 +127,7 @@ struct gdbg_graph {
     DevBuf<uint64_t> rec_a, rec_b;
     DevBuf<uint32_t> hist, hist_off, scan_parts, bstart, new_bits;
     DevBuf<uint8_t> iq_vals;    // insert_and_query: post-insert value per table and k-mer
+    DevBuf<uint32_t> sp_hist2, sp_off2, sp_plan;   // segmented path: pass-2 counts, plan
     uint32_t* d_epoch = nullptr;
     unsigned int* d_bar = nullptr;
     bool epoch_on_device = false;
@@ -319,10 +320,10 @@ int check_device_status(gdbg_graph* g) {
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
     if (err) {
         cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
-        char buf[160];
+        char buf[200];
         std::snprintf(buf, sizeof buf,
                       "device status 0x%x (1=CAS cap, 2=claims map full, 4=barrier timeout, "
-                      "8=bad read offsets)", err);
+                      "8=bad read offsets, 16=bulk-copy timeout, 32=partition overflow)", err);
         return fail(GDBG_ERR_DEVICE, buf);
     }
     return GDBG_OK;
@@ -425,6 +426,12 @@ uint32_t default_bucket_fs(int storage) {
     return storage == GDBG_BIT ? 19u : storage == GDBG_NIBBLE ? 17u : 16u;
 }
 
+uint32_t default_sort_fs(int storage) {
+    // 32 KB of table per bucket (the region and the fresh-cell map fit two
+    // CTAs per SM)
+    return storage == GDBG_BIT ? 18u : storage == GDBG_NIBBLE ? 16u : 15u;
+}
+
 // Can the bucketed path take this batch?  (tables <= 8, every global cell id
 // and every record index below 2^32)
 bool bucket_fits(const gdbg_graph* g, uint64_t n_kmers, uint32_t fs) {
@@ -436,19 +443,72 @@ bool bucket_fits(const gdbg_graph* g, uint64_t n_kmers, uint32_t fs) {
     return cells <= (1ull << 32);
 }
 
-// Read maps the batch insert will use: the windowed path walks k-mer runs
-// (tile map), the persistent and bucketed paths walk warp tasks (task map).
-int insert_maps(const gdbg_graph* g, uint64_t n_total) {
-    if (n_total == UINT64_MAX) return MAP_TILES | MAP_TASKS;
-    const uint32_t fs = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
+uint64_t buckets_at(const gdbg_graph* g, uint32_t fs) {
+    uint64_t nb = 0;
+    for (auto p : g->ts->sizes) nb += (p + (1ull << fs) - 1) >> fs;
+    return nb;
+}
+
+// Bucket size of the segmented path: the set size, else the default 32 KB
+// region, made smaller (down to 512 B, within 2^17 buckets) while a bucket of
+// the smallest table would get more than 4096 of the batch's records, so a
+// bucket's records fit the apply's shared-memory buffer.
+uint32_t sort_fs(const gdbg_graph* g, uint64_t n_kmers) {
+    if (g->bucket_fs) return g->bucket_fs;
+    uint32_t fs = default_sort_fs(g->storage);
+    const uint32_t min_fs = g->storage == GDBG_BIT ? 12u : g->storage == GDBG_NIBBLE ? 10u : 9u;
+    uint64_t smallest = ~0ull;
+    for (auto p : g->ts->sizes) smallest = std::min(smallest, p);
+    while (fs > min_fs && (double)n_kmers * (double)(1ull << fs) / (double)smallest > 4096.0 &&
+           buckets_at(g, fs - 1) <= (1ull << 17))
+        --fs;
+    return fs;
+}
+
+// Can the segmented bucketed path take this batch?  (bucketed limits at its
+// bucket size, at most 2^17 buckets, a shared-memory region of at most 64 KB)
+bool sort_fits(const gdbg_graph* g, uint64_t n_kmers) {
+    const uint32_t fs = sort_fs(g, n_kmers);
+    if (!bucket_fits(g, n_kmers, fs)) return false;
+    const uint32_t cpw = g->storage == GDBG_BIT ? 32u : g->storage == GDBG_NIBBLE ? 8u : 4u;
+    if (((1ull << fs) / cpw) * 4 > (64u << 10)) return false;
+    return buckets_at(g, fs) <= (1ull << 17);
+}
+
+enum InsertKind { INS_WINDOWED, INS_PERSISTENT, INS_BUCKETED, INS_SORTED };
+
+// The implementation a batch insert of n_total k-mers takes.
+InsertKind insert_kind(const gdbg_graph* g, uint64_t n_total) {
     uint64_t table_bytes = 0;
     for (auto w : g->ts->words) table_bytes += 4 * w;
-    const bool fits = bucket_fits(g, n_total, fs);
-    if (g->path == GDBG_PATH_BUCKETED && fits) return MAP_TASKS;
-    if (g->path == GDBG_PATH_AUTO && fits && table_bytes >= (256ull << 20) && n_total >= (1ull << 22))
-        return MAP_TASKS;
-    if (g->path == GDBG_PATH_PERSISTENT) return MAP_TASKS;
-    return MAP_TILES;
+    const uint32_t fso = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
+    const bool big = table_bytes >= (256ull << 20) && n_total >= (1ull << 22);
+    switch (g->path) {
+    case GDBG_PATH_PERSISTENT: return INS_PERSISTENT;
+    case GDBG_PATH_BUCKETED_ORDERED:
+        return bucket_fits(g, n_total, fso) ? INS_BUCKETED : INS_WINDOWED;
+    case GDBG_PATH_BUCKETED:
+        if (sort_fits(g, n_total)) return INS_SORTED;
+        return bucket_fits(g, n_total, fso) ? INS_BUCKETED : INS_WINDOWED;
+    case GDBG_PATH_AUTO:
+        if (!big) return INS_WINDOWED;
+        if (sort_fits(g, n_total)) return INS_SORTED;
+        return bucket_fits(g, n_total, fso) ? INS_BUCKETED : INS_WINDOWED;
+    default: return INS_WINDOWED;
+    }
+}
+
+// Read maps the batch insert will use: the windowed path walks k-mer runs
+// (tile map), the persistent and bucketed paths walk warp tasks (task map),
+// the segmented path both.
+int insert_maps(const gdbg_graph* g, uint64_t n_total) {
+    if (n_total == UINT64_MAX) return MAP_TILES | MAP_TASKS;
+    switch (insert_kind(g, n_total)) {
+    case INS_PERSISTENT:
+    case INS_BUCKETED: return MAP_TASKS;
+    case INS_SORTED: return MAP_TILES | MAP_TASKS;
+    default: return MAP_TILES;
+    }
 }
 
 int set_error_launch(cudaError_t e, const char* what) {
@@ -558,6 +618,118 @@ int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cuda
     return GDBG_OK;
 }
 
+// Segmented bucketed insert (gdbg_sort.cuh): emit with first-digit counts,
+// one or two unstable digit passes, bucket starts, order-independent apply.
+int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaStream_t st) {
+    const uint64_t nk = b.n_kmers, n = g->ts->sizes.size();
+    if (nk == 0) {
+        if (n_new && b.n_reads) GDBG_CUDA(cudaMemsetAsync(n_new, 0, b.n_reads * sizeof(uint64_t), st));
+        return GDBG_OK;
+    }
+    const uint32_t fs = sort_fs(g, nk);
+    SortParams sp{};
+    sp.fs = fs;
+    uint32_t nb = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        sp.bbase[i] = nb;
+        sp.tbase[i] = (uint64_t)nb << fs;
+        sp.twords[i] = (uint32_t)g->ts->words[i];
+        nb += (uint32_t)((g->ts->sizes[i] + (1ull << fs) - 1) >> fs);
+    }
+    sp.bbase[n] = nb;
+    sp.n_buckets = nb;
+    sp.n_tables = (uint32_t)n;
+    uint32_t bits = 0;
+    while ((1u << bits) < nb) ++bits;
+    if (bits <= 8) {
+        sp.hi_shift = 0;
+        sp.bins1 = 1u << bits;
+        sp.bins2 = 1;
+    } else {
+        sp.hi_shift = bits - 8;
+        sp.bins1 = 256;
+        sp.bins2 = 1u << sp.hi_shift;
+    }
+    sp.total_kmers = b.kofs + b.n_reads;
+    sp.kmer_cap = nk;
+    const uint64_t nrec = nk * n;
+    sp.nseg1 = (uint32_t)((nk + SP_SEGK - 1) / SP_SEGK);
+    sp.nseg2_cap = sp.bins2 > 1 ? (uint32_t)(nrec / SP_SEG2 + sp.bins1 + 1) : 0u;
+    const uint64_t h1 = (uint64_t)sp.bins1 * sp.nseg1;
+    const uint64_t h2 = (uint64_t)sp.bins2 * sp.nseg2_cap;
+    GDBG_TRY(g->rec_a.ensure(nrec + 2));
+    GDBG_TRY(g->rec_b.ensure(nrec + 2));
+    GDBG_TRY(g->hist.ensure(h1));
+    GDBG_TRY(g->hist_off.ensure(h1));
+    if (h2) {
+        GDBG_TRY(g->sp_hist2.ensure(h2));
+        GDBG_TRY(g->sp_off2.ensure(h2));
+    }
+    GDBG_TRY(g->sp_plan.ensure(2 * (sp.bins1 + 1)));
+    GDBG_TRY(g->scan_parts.ensure(scan32_partials_needed(std::max(h1, h2)) + 1));
+    GDBG_TRY(g->bstart.ensure(nb + 1));
+    GDBG_TRY(g->new_bits.ensure(nk / 32 + 2));
+    sp.hist1 = g->hist.p;
+    sp.off1 = g->hist_off.p;
+    sp.hist2 = h2 ? g->sp_hist2.p : nullptr;
+    sp.off2 = h2 ? g->sp_off2.p : nullptr;
+    sp.plan = g->sp_plan.p;
+    sp.err = g->d_err;
+    GDBG_CUDA(cudaMemsetAsync(g->new_bits.p, 0, (nk / 32 + 2) * sizeof(uint32_t), st));
+    const bool canon = g->shifter == GDBG_CAN_LEMIRE;
+    cudaError_t e;
+    {
+        Stage sg(g, "k_sp_emit", st);
+        if ((e = launch_sp_emit(canon, st, b, g->hp, g->ts->tp, sp, g->rec_a.p)) != cudaSuccess)
+            return set_error_launch(e, "segment emit");
+    }
+    {
+        Stage sg(g, "k_scan32", st);
+        if ((e = launch_scan32(sp.hist1, sp.off1, h1, g->scan_parts.p, st)) != cudaSuccess)
+            return set_error_launch(e, "segment scan");
+    }
+    {
+        Stage sg(g, "k_sp_part", st);
+        if ((e = launch_sp_part(false, st, sp, g->rec_a.p, g->rec_b.p)) != cudaSuccess)
+            return set_error_launch(e, "segment partition");
+    }
+    g->launches += 5;   // emit, 3 scan kernels, partition
+    const uint64_t* fin = g->rec_b.p;
+    if (sp.bins2 > 1) {
+        GDBG_CUDA(cudaMemsetAsync(sp.hist2, 0, h2 * sizeof(uint32_t), st));
+        if ((e = launch_sp_plan(st, sp)) != cudaSuccess) return set_error_launch(e, "segment plan");
+        {
+            Stage sg(g, "k_sp_hist2", st);
+            if ((e = launch_sp_hist2(st, sp, g->rec_b.p)) != cudaSuccess)
+                return set_error_launch(e, "segment counts");
+        }
+        {
+            Stage sg(g, "k_scan32", st);
+            if ((e = launch_scan32(sp.hist2, sp.off2, h2, g->scan_parts.p, st)) != cudaSuccess)
+                return set_error_launch(e, "segment scan");
+        }
+        {
+            Stage sg(g, "k_sp_part", st);
+            if ((e = launch_sp_part(true, st, sp, g->rec_b.p, g->rec_a.p)) != cudaSuccess)
+                return set_error_launch(e, "segment partition");
+        }
+        fin = g->rec_a.p;
+        g->launches += 6;   // plan, counts, 3 scan kernels, partition
+    }
+    if ((e = launch_sp_starts(st, sp, g->bstart.p)) != cudaSuccess)
+        return set_error_launch(e, "bucket starts");
+    {
+        Stage sg(g, "k_sp_apply", st);
+        if ((e = launch_sp_apply(g->storage, g->ts->tp, sp, fin, g->bstart.p, g->new_bits.p,
+                                 g->ts->d_counters, st)) != cudaSuccess)
+            return set_error_launch(e, "segment apply");
+    }
+    if ((e = launch_bucket_read_new(b.kofs, b.n_reads, g->new_bits.p, n_new, g->ts->d_counters, st)) != cudaSuccess)
+        return set_error_launch(e, "bucket read counts");
+    g->launches += 3;   // starts, apply, read counts
+    return GDBG_OK;
+}
+
 // Persistent cooperative insert of a read batch (one launch per batch).
 int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaStream_t st) {
     if (b.n_kmers == 0 || b.task_cap == 0) return GDBG_OK;
@@ -611,18 +783,15 @@ int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64
                uint64_t* n_new, cudaStream_t st) {
     if (n_total == 0) return GDBG_OK;
     if (!hashes) {
-        const uint32_t fs = g->bucket_fs ? g->bucket_fs : default_bucket_fs(g->storage);
-        uint64_t table_bytes = 0;
-        for (auto w : g->ts->words) table_bytes += 4 * w;
-        const bool fits = bucket_fits(g, n_total, fs);
-        if (g->path == GDBG_PATH_BUCKETED && fits) return run_insert_bucketed(g, b, n_new, st);
-        if (g->path == GDBG_PATH_AUTO && fits && table_bytes >= (256ull << 20) &&
-            n_total >= (1ull << 22))
-            return run_insert_bucketed(g, b, n_new, st);
         // the cooperative kernel only on request: AUTO stays with kernels that
         // never wait on other blocks, so graphs on concurrent streams cannot
         // hold each other's blocks off the GPU
-        if (g->path == GDBG_PATH_PERSISTENT) return run_insert_persistent(g, b, n_new, st);
+        switch (insert_kind(g, n_total)) {
+        case INS_SORTED: return run_insert_sorted(g, b, n_new, st);
+        case INS_BUCKETED: return run_insert_bucketed(g, b, n_new, st);
+        case INS_PERSISTENT: return run_insert_persistent(g, b, n_new, st);
+        default: break;
+        }
     }
     GDBG_TRY(ensure_insert_scratch(g, st));
     if (g->epoch_on_device) {
@@ -848,6 +1017,7 @@ int gdbg_destroy(gdbg_graph* g) {
     g->task_read.release();
     g->rec_a.release(); g->rec_b.release(); g->hist.release(); g->hist_off.release();
     g->scan_parts.release(); g->bstart.release(); g->new_bits.release(); g->iq_vals.release();
+    g->sp_hist2.release(); g->sp_off2.release(); g->sp_plan.release();
     g->st_packed.release(); g->st_offsets.release(); g->st_out64.release();
     g->st_out64b.release(); g->st_out64c.release(); g->st_counts.release(); g->st_u8.release();
     for (auto& p : g->pending) {
@@ -1544,7 +1714,7 @@ int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmer
 
 int gdbg_set_insert_path(gdbg_graph* g, int path) {
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
-    if (path < GDBG_PATH_PERSISTENT || path > GDBG_PATH_AUTO)
+    if (path < GDBG_PATH_PERSISTENT || path > GDBG_PATH_BUCKETED_ORDERED)
         return fail(GDBG_ERR_INVALID_ARG, "unknown insert path");
     g->path = path;
     return GDBG_OK;

@@ -154,6 +154,27 @@ __device__ __forceinline__ uint32_t cell_value(uint32_t word, uint32_t shift) {
     return (word >> shift) & 0xFu;
 }
 
+// Region-relative cell address in shared memory words.
+template <int STORAGE>
+__device__ __forceinline__ void region_cell(uint32_t co, uint32_t& word, uint32_t& shift) {
+    if (STORAGE == GDBG_BIT) {
+        word = co >> 5;
+        shift = co & 31u;
+    } else if (STORAGE == GDBG_BYTE) {
+        word = co >> 2;
+        shift = (co & 3u) << 3;
+    } else {
+        const uint32_t byte = co >> 1;
+        word = byte >> 2;
+        shift = ((byte & 3u) << 3) + ((co & 1u) ? 0u : 4u);
+    }
+}
+
+template <int STORAGE>
+__host__ __device__ constexpr uint32_t cells_per_word() {
+    return STORAGE == GDBG_BIT ? 32u : STORAGE == GDBG_BYTE ? 4u : 8u;
+}
+
 template <int STORAGE>
 __device__ __forceinline__ uint32_t cell_max() {
     return STORAGE == GDBG_BIT ? 1u : STORAGE == GDBG_BYTE ? 255u : 15u;

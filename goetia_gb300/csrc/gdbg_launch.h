@@ -84,6 +84,19 @@ cudaError_t launch_task_map(const uint64_t* tofs, uint64_t n_reads, uint64_t cap
 cudaError_t launch_tile_map(const uint64_t* kofs, uint64_t n_reads, uint64_t n_tiles,
                             uint32_t* tile_read, cudaStream_t st);
 
+// Segmented bucketed insert (gdbg_sort.cu / gdbg_sort.cuh).
+cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
+                           const TableParams& tp, const SortParams& sp, uint64_t* rout);
+cudaError_t launch_sp_part(bool pass2, cudaStream_t st, const SortParams& sp, const uint64_t* rin,
+                           uint64_t* rout);
+cudaError_t launch_sp_plan(cudaStream_t st, const SortParams& sp);
+cudaError_t launch_sp_hist2(cudaStream_t st, const SortParams& sp, const uint64_t* rin);
+cudaError_t launch_sp_starts(cudaStream_t st, const SortParams& sp, uint32_t* start);
+cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams& sp,
+                            const uint64_t* recs, const uint32_t* start, uint32_t* new_bits,
+                            unsigned long long* counters, cudaStream_t st);
+size_t sp_apply_smem_bytes(int storage, uint32_t fs);
+
 // OR-merge of two identically laid out table allocations (n_words, a
 // multiple of 4); cells newly set in the first count_words words are added
 // to *occupied.

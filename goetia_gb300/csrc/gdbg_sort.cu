@@ -1,0 +1,78 @@
+// Launchers for the segmented bucketed insert (kernels in gdbg_sort.cuh).
+#include "gdbg_launch.h"
+#include "gdbg_sort.cuh"
+
+namespace gdbg {
+
+cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
+                           const TableParams& tp, const SortParams& sp, uint64_t* rout) {
+    if (sp.nseg1 == 0) return cudaSuccess;
+    if (canonical) k_sp_emit<true><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+    else k_sp_emit<false><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sp_part(bool pass2, cudaStream_t st, const SortParams& sp, const uint64_t* rin,
+                           uint64_t* rout) {
+    const uint32_t grid = pass2 ? sp.nseg2_cap : sp.nseg1;
+    if (grid == 0) return cudaSuccess;
+    const size_t smem = sp_part_smem();
+    cudaError_t e;
+    if (pass2) {
+        e = cudaFuncSetAttribute(k_sp_part<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_sp_part<true><<<grid, SP_PART_BLOCK, smem, st>>>(sp, rin, rout);
+    } else {
+        e = cudaFuncSetAttribute(k_sp_part<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_sp_part<false><<<grid, SP_PART_BLOCK, smem, st>>>(sp, rin, rout);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sp_plan(cudaStream_t st, const SortParams& sp) {
+    k_sp_plan<<<1, 256, 0, st>>>(sp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sp_hist2(cudaStream_t st, const SortParams& sp, const uint64_t* rin) {
+    if (sp.nseg2_cap == 0) return cudaSuccess;
+    k_sp_hist2<<<sp.nseg2_cap, SP_PART_BLOCK, 0, st>>>(sp, rin);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sp_starts(cudaStream_t st, const SortParams& sp, uint32_t* start) {
+    const uint32_t n = sp.n_buckets + 1;
+    k_sp_starts<<<(n + 255) / 256, 256, 0, st>>>(sp, start);
+    return cudaGetLastError();
+}
+
+template <int ST>
+static cudaError_t sp_apply_one(const TableParams& tp, const SortParams& sp, const uint64_t* recs,
+                                const uint32_t* start, uint32_t* new_bits,
+                                unsigned long long* counters, cudaStream_t st) {
+    const size_t smem = sp_apply_smem((1u << sp.fs) / cells_per_word<ST>());
+    cudaError_t e = cudaFuncSetAttribute(k_sp_apply<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_sp_apply<ST><<<sp.n_buckets, SP_APPLY_BLOCK, smem, st>>>(tp, sp, recs, start, new_bits, counters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams& sp,
+                            const uint64_t* recs, const uint32_t* start, uint32_t* new_bits,
+                            unsigned long long* counters, cudaStream_t st) {
+    if (sp.n_buckets == 0) return cudaSuccess;
+    switch (storage) {
+    case GDBG_BIT: return sp_apply_one<GDBG_BIT>(tp, sp, recs, start, new_bits, counters, st);
+    case GDBG_BYTE: return sp_apply_one<GDBG_BYTE>(tp, sp, recs, start, new_bits, counters, st);
+    default: return sp_apply_one<GDBG_NIBBLE>(tp, sp, recs, start, new_bits, counters, st);
+    }
+}
+
+size_t sp_apply_smem_bytes(int storage, uint32_t fs) {
+    const uint32_t cpw = storage == GDBG_BIT ? 32u : storage == GDBG_BYTE ? 4u : 8u;
+    return sp_apply_smem((1u << fs) / cpw);
+}
+
+}  // namespace gdbg

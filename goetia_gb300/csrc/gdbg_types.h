@@ -13,7 +13,9 @@ enum : uint32_t {
     GDBG_ERR_CAS_LIMIT = 1u,      // a saturating compare-and-swap loop hit its cap
     GDBG_ERR_CLAIMS_FULL = 2u,    // the first-touch map overflowed
     GDBG_ERR_BARRIER_TIMEOUT = 4u,// a grid barrier wait hit its cap
-    GDBG_ERR_BAD_OFFSETS = 8u     // read offsets decrease or run past the packed stream
+    GDBG_ERR_BAD_OFFSETS = 8u,    // read offsets decrease or run past the packed stream
+    GDBG_ERR_COPY_TIMEOUT = 16u,  // a bulk-copy wait hit its cap
+    GDBG_ERR_PARTITION = 32u      // a partition position fell outside the record array
 };
 
 struct HashParams {
@@ -82,6 +84,36 @@ struct BucketParams {
     const uint64_t* total_kmers;      // device: the batch's k-mer count (kofs[n_reads])
     uint32_t n_tables;
     uint64_t kmer_cap;                // k-mers the new-k-mer bitmask can hold
+};
+
+// Segmented bucketed insert (gdbg_sort.cuh): records partitioned by bucket
+// with two unstable most-significant-digit passes, then applied per bucket
+// in an order-independent way.
+constexpr uint32_t SP_TILE = 4096;       // records per partition tile
+constexpr uint32_t SP_SEGK = 16384;      // k-mers per pass-1 segment (multiple of MAP_TILE)
+constexpr uint32_t SP_SEG2 = 65536;      // records per pass-2 segment
+constexpr uint32_t SP_MAXBINS2 = 512;    // pass-2 digit bins at most
+constexpr uint32_t SP_MAPCAP = 4096;     // apply: fresh-cell map slots
+
+struct SortParams {
+    uint32_t fs;                  // log2(cells per bucket)
+    uint32_t n_buckets;
+    uint32_t n_tables;
+    uint32_t hi_shift;            // pass-1 digit = bucket >> hi_shift
+    uint32_t bins1, bins2;        // digit bins of pass 1 and pass 2 (bins2 == 1: one pass)
+    uint64_t tbase[BK_MAXNT];     // aligned global cell base of each table
+    uint32_t bbase[BK_MAXNT + 1]; // first bucket of each table
+    uint32_t twords[BK_MAXNT];    // padded word count of each table
+    const uint64_t* total_kmers;  // device: the batch's k-mer count
+    uint64_t kmer_cap;            // host bound on k-mers
+    uint32_t nseg1;               // pass-1 segments for kmer_cap k-mers
+    uint32_t nseg2_cap;           // host bound on pass-2 segments
+    uint32_t* hist1;              // bins1 x nseg1, bin-major
+    uint32_t* off1;               // its exclusive scan
+    uint32_t* hist2;              // ordered (group, bin, segment of the group)
+    uint32_t* off2;               // its exclusive scan
+    uint32_t* plan;               // s0[bins1 + 1] then G[bins1 + 1]
+    uint32_t* err;                // device status word
 };
 
 // Persistent batch insert (gdbg_persist.cuh).

@@ -654,15 +654,22 @@ class dBGBase:
 
     PATHS = {"persistent": _lib.PATH_PERSISTENT, "windowed": _lib.PATH_WINDOWED,
              "bucketed": _lib.PATH_BUCKETED, "auto": _lib.PATH_AUTO,
+             "bucketed_ordered": _lib.PATH_BUCKETED_ORDERED,
              True: _lib.PATH_PERSISTENT, False: _lib.PATH_WINDOWED}
 
     def set_insert_path(self, path="auto"):
-        """Batch insert implementation: "persistent", "windowed", "bucketed" or
-        "auto" (True / False mean persistent / windowed)."""
+        """Batch insert implementation: "persistent", "windowed", "bucketed",
+        "bucketed_ordered" or "auto" (True / False mean persistent / windowed)."""
         _lib.call("gdbg_set_insert_path", self._h, self.PATHS[path])
+        self._path = path
+
+    def insert_path(self):
+        """The path last set with set_insert_path ("auto" by default)."""
+        return getattr(self, "_path", "auto")
 
     def set_bucket_bits(self, log2_cells=0):
-        """Cells per bucket (log2) of the bucketed path; 0 = 64 KB of table."""
+        """Cells per bucket (log2) of the bucketed paths; 0 = their default
+        (adaptive for "bucketed", 64 KB of table for "bucketed_ordered")."""
         _lib.call("gdbg_set_bucket_bits", self._h, int(log2_cells))
 
     def insert_schedule(self):

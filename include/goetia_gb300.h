@@ -233,17 +233,23 @@ int gdbg_set_insert_schedule(gdbg_graph* g, uint32_t window_kmers, uint32_t kmer
  *               its blocks wait on each other at grid barriers (bounded), so
  *               do not run two such inserts concurrently on different streams
  *   WINDOWED    one probe and one commit launch per window
- *   BUCKETED    records partitioned by table region, each region applied in
- *               shared memory (large batches on tables far beyond L2)
+ *   BUCKETED    records partitioned by table region with two unstable digit
+ *               passes, each region applied in shared memory independently of
+ *               record order (large batches on tables far beyond L2); falls
+ *               back to BUCKETED_ORDERED outside its limits (more than
+ *               2^17 buckets or regions above 64 KB)
+ *   BUCKETED_ORDERED  the same with stable digit passes and regions applied
+ *               in k-mer order (also the path of insert_and_query batches)
  *   AUTO        BUCKETED for batches of >= 4M k-mers on >= 256 MB of tables,
  *               else WINDOWED (default) */
 #define GDBG_PATH_PERSISTENT 0
 #define GDBG_PATH_WINDOWED 1
 #define GDBG_PATH_BUCKETED 2
 #define GDBG_PATH_AUTO 3
+#define GDBG_PATH_BUCKETED_ORDERED 4
 int gdbg_set_insert_path(gdbg_graph* g, int path);
-/* Cells per bucket of the bucketed path as log2 (0 = default: 64 KB of table
- * per bucket). */
+/* Cells per bucket of the bucketed paths as log2 (0 = default: 32 KB of
+ * table per bucket for BUCKETED, 64 KB for BUCKETED_ORDERED). */
 int gdbg_set_bucket_bits(gdbg_graph* g, uint32_t log2_cells);
 int gdbg_get_insert_schedule(const gdbg_graph* g, uint32_t* window_kmers,
                              uint32_t* kmers_per_thread);

@@ -60,7 +60,8 @@ def test_golden_plain_per_read(cuda_ready, name):
 # insert path, window, k-mers per thread, log2 cells per bucket (0 = default)
 PATHS = [("persistent", 262144, 4, 0), ("persistent", 64, 8, 0), ("persistent", 5, 4, 0),
          ("windowed", 262144, 4, 0), ("windowed", 64, 8, 0), ("windowed", 5, 4, 0),
-         ("bucketed", 0, 0, 0), ("bucketed", 0, 0, 5), ("bucketed", 0, 0, 7)]
+         ("bucketed", 0, 0, 0), ("bucketed", 0, 0, 5), ("bucketed", 0, 0, 7),
+         ("bucketed_ordered", 0, 0, 0), ("bucketed_ordered", 0, 0, 5)]
 
 
 @pytest.mark.parametrize("name", names())
@@ -115,7 +116,7 @@ def _oracle_run(kind, canonical, K, sizes, pr):
     ("bit", False, 25, 7919),
 ])
 @pytest.mark.parametrize("path,fs", [("persistent", 0), ("windowed", 0), ("bucketed", 0),
-                                     ("bucketed", 5)])
+                                     ("bucketed", 5), ("bucketed_ordered", 0)])
 def test_config1_reads_vs_oracle(cuda_ready, kind, canonical, K, max_table, path, fs):
     """10,000 reads of 150 bp from a 100 kb genome, 1% substitutions."""
     gen = synth.genome(100_000, 1)
@@ -146,8 +147,8 @@ def test_batches_in_sequence_vs_oracle(cuda_ready):
     g = graph_for("byte", True, 31, sizes)
     g.set_insert_schedule(2048, 4)
     g.set_bucket_bits(6)
-    for b in range(6):
-        g.set_insert_path(["persistent", "windowed", "bucketed"][b % 3])
+    for b in range(8):
+        g.set_insert_path(["persistent", "windowed", "bucketed", "bucketed_ordered"][b % 4])
         rows = synth.sample_reads(gen, 700, 150, 0.02, 100 + b)
         pr = synth.rows_to_packed(rows)
         _, ref = st.insert_reads(True, 31, pr.packed, pr.offsets)
@@ -163,7 +164,7 @@ def test_uneven_reads_vs_oracle(cuda_ready):
     pr = synth.list_to_packed(rs)
     sizes = oracle.primes(4, 60013)
     st, ref = _oracle_run("nibble", False, 21, sizes, pr)
-    for path in ("persistent", "bucketed"):
+    for path in ("persistent", "bucketed", "bucketed_ordered"):
         g = graph_for("nibble", False, 21, sizes)
         g.set_insert_schedule(4096, 8)
         g.set_insert_path(path)
@@ -255,3 +256,24 @@ def test_device_offsets_validated(cuda_ready):
     assert g.device_status() == 0
     # the graph is still usable
     assert g.insert_sequence("ACGT" * 10) == 10
+
+
+@pytest.mark.parametrize("kind", ["bit", "byte", "nibble"])
+def test_segmented_dense_buckets(cuda_ready, kind):
+    """Tables of one or two buckets each receiving far more distinct zero
+    cells than the apply's fresh-cell map holds, so every bucket is applied
+    in narrower cell ranges; then a second batch on the filled tables."""
+    sizes = {"bit": [250007, 249989], "byte": [30011, 29989, 29983], "nibble": [60013, 59999]}[kind]
+    g = graph_for(kind, True, 25, sizes)
+    g.set_insert_path("bucketed")
+    gen = synth.genome(400_000, 31)
+    ref = oracle.Storage(kind, sizes)
+    for b in range(2):
+        rows = synth.sample_reads(gen, 3000, 120, 0.01, 40 + b)
+        pr = synth.rows_to_packed(rows)
+        n_new = g.insert_packed(pr)
+        _, want = ref.insert_reads(True, 25, pr.packed, pr.offsets)
+        assert np.array_equal(n_new, want), b
+    for a, t in zip(g.get_raw(), ref.tables()):
+        assert np.array_equal(a, t)
+    assert (g.n_unique(), g.n_occupied()) == ref.stats()
