@@ -99,9 +99,16 @@ __global__ void __launch_bounds__(SP_EMIT_BLOCK)
 k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* __restrict__ rout) {
     __shared__ uint64_t stage[SP_EMIT_BLOCK / 32][32 * BK_MAXNT];
     __shared__ uint32_t hist[256];
+    // roll terms by (out, in): fw ^= symk(out) ^ sym(in), rc ^= symk(3-in) ^ sym(3-out)
+    __shared__ uint64_t roll_fw[16], roll_rc[16];
     const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t s = blockIdx.x;
     for (uint32_t k = tid; k < sp.bins1; k += SP_EMIT_BLOCK) hist[k] = 0;
+    if (tid < 16) {
+        const uint32_t out = tid >> 2, in = tid & 3u;
+        roll_fw[tid] = symk(hp, out) ^ sym(in);
+        roll_rc[tid] = symk(hp, 3u - in) ^ sym(3u - out);
+    }
     __syncthreads();
     const uint64_t total = __ldg(b.kofs + b.n_reads);
     uint64_t nk = total < sp.kmer_cap ? total : sp.kmer_cap;
@@ -136,17 +143,48 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
     for (uint32_t j = 0; j < n_steps; ++j) {
         const bool act = j < my_len;
         const uint64_t g = gs + (uint64_t)tid * SP_RUN + j;
+        bool reseed = false;
+        uint64_t rbase = 0;
         if (act && j > 0) {
             if (g >= kend) {
                 do {
                     ++r;
                     kend = __ldg(b.kofs + r + 1);
                 } while (kend <= g);
-                seed(g);
+                rbase = __ldg(b.offsets + r) + (g - __ldg(b.kofs + r));
+                reseed = true;
             } else {
                 const uint32_t out = cout.next();
                 const uint32_t in = cin.next();
-                roll_right<CANON>(hp, out, in, fw, rc);
+                // roll_right with the terms from the table
+                fw = rotl1(fw) ^ roll_fw[out * 4u + in];
+                if (CANON) rc = rotr1(rc ^ roll_rc[out * 4u + in]);
+            }
+        }
+        // lanes that entered a new read: the warp computes each one's seed
+        // together (one base per lane, XOR-reduced), instead of one lane
+        // rolling K bases while the others wait
+        uint32_t need = __ballot_sync(0xFFFFFFFFu, reseed);
+        while (need) {
+            const int L = __ffs(need) - 1;
+            need &= need - 1;
+            const uint64_t pb = __shfl_sync(0xFFFFFFFFu, rbase, L);
+            uint64_t sf = 0, sr = 0;
+            for (uint32_t i = lane; i < K; i += 32) {
+                const uint32_t c = base_at(b.packed, pb + i);
+                sf ^= rotl64(sym(c), (K - 1u - i) & 63u);
+                if (CANON) sr ^= rotl64(sym(3u - c), i & 63u);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sf ^= __shfl_xor_sync(0xFFFFFFFFu, sf, o);
+                if (CANON) sr ^= __shfl_xor_sync(0xFFFFFFFFu, sr, o);
+            }
+            if ((int)lane == L) {
+                fw = sf;
+                rc = sr;
+                cin.init(b.packed, pb + K);
+                cout.init(b.packed, pb);
             }
         }
         // slots of step j: threads active at step j, in thread order
@@ -251,8 +289,18 @@ k_sp_hist2(SortParams sp, const uint64_t* __restrict__ rin) {
     __syncthreads();
     if (!sg.valid) return;
     const uint32_t mask = sp.bins2 - 1;
-    for (uint32_t k = sg.rs + threadIdx.x; k < sg.re; k += SP_PART_BLOCK)
-        atomicAdd(&cnt[sp_bucket(__ldcs(rin + k), sp.fs) & mask], 1u);
+    constexpr int U = 8;   // loads in flight per thread
+    for (uint32_t k0 = sg.rs + threadIdx.x; k0 < sg.re; k0 += U * SP_PART_BLOCK) {
+        uint64_t v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t k = k0 + u * SP_PART_BLOCK;
+            v[u] = k < sg.re ? __ldcs(rin + k) : SP_EMPTY;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (v[u] != SP_EMPTY) atomicAdd(&cnt[sp_bucket(v[u], sp.fs) & mask], 1u);
+    }
     __syncthreads();
     const uint64_t base = (uint64_t)sp.bins2 * sp.plan[sg.group];
     for (uint32_t d = threadIdx.x; d < sp.bins2; d += SP_PART_BLOCK)
