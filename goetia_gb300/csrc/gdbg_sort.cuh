@@ -478,31 +478,79 @@ __global__ void k_sp_starts(SortParams sp, uint32_t* __restrict__ start) {
 
 // ---- 4. order-independent apply -------------------------------------------
 
-constexpr uint32_t SP_RBUF = 5120;   // records of a bucket staged in shared memory at once
+constexpr uint32_t SP_RBUF = 4608;   // records of a bucket staged in shared memory at once
+constexpr uint16_t SP_NOSLOT = 0xFFFFu;
 
 __device__ __forceinline__ uint32_t sp_slot(uint32_t co) {
     return (co * 0x9E3779B1u) >> (32 - 12);   // SP_MAPCAP = 2^12
 }
 
 // Shared-memory layout of k_sp_apply (byte offsets): region words (padded
-// to 16 bytes), fresh-cell map, record buffer (+2 alignment slack), dirty
-// sector bits.
+// to 16 bytes), fresh-cell map, record buffer (+2 alignment slack), the map
+// slot of each staged record (or SP_NOSLOT), dirty sector bits.
 struct ApplyLayout {
-    uint32_t map_off, rec_off, dirty_off, total;
+    uint32_t map_off, rec_off, slot_off, dirty_off, total;
 };
 __host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words) {
     const uint32_t region_b = ((region_words + 3u) & ~3u) * 4u;
     const uint32_t map_b = SP_MAPCAP * 8u;
     const uint32_t rec_b = (SP_RBUF + 2u) * 8u;
+    const uint32_t slot_b = SP_RBUF * 2u;
     const uint32_t dirty_b = (((region_words + 7u) / 8u + 31u) / 32u) * 4u;
     return ApplyLayout{region_b, region_b + map_b, region_b + map_b + rec_b,
-                       region_b + map_b + rec_b + dirty_b};
+                       region_b + map_b + rec_b + slot_b,
+                       region_b + map_b + rec_b + slot_b + dirty_b};
+}
+
+// Map insert of a zero cell with ordinal g: the slot index, or SP_MAPCAP when
+// the map is full; *created is set when this call made the entry.
+__device__ __forceinline__ uint32_t sp_map_insert(uint64_t* map, uint32_t co, uint32_t g,
+                                                  bool* created) {
+    const uint64_t mine = ((uint64_t)g << 32) | co;   // (ordinal << 32) | cell
+    uint32_t sl = sp_slot(co);
+    *created = false;
+    for (uint32_t it = 0; it < SP_MAPCAP; ++it) {
+        uint64_t cur = map[sl];
+        if (cur == SP_EMPTY) {
+            cur = atomicCAS((unsigned long long*)&map[sl], SP_EMPTY, mine);
+            if (cur == SP_EMPTY) {
+                *created = true;
+                return sl;
+            }
+        }
+        if ((uint32_t)cur == co) {
+            if (mine < cur) atomicMin((unsigned long long*)&map[sl], mine);
+            return sl;
+        }
+        sl = (sl + 1) & (SP_MAPCAP - 1);
+    }
+    return SP_MAPCAP;
+}
+
+// Saturating increment of one region cell; true when the word changed.
+template <int STORAGE>
+__device__ __forceinline__ bool sp_increment(uint32_t* region, uint32_t word, uint32_t shift) {
+    if (STORAGE == GDBG_BIT) {
+        const uint32_t bit = 1u << shift;
+        return (atomicOr(region + word, bit) & bit) == 0;
+    }
+    uint32_t cur = region[word];
+    for (int it = 0; it < (1 << 20); ++it) {
+        if (cell_value<STORAGE>(cur, shift) >= cell_max<STORAGE>()) return false;
+        const uint32_t prev = atomicCAS(region + word, cur, cur + (1u << shift));
+        if (prev == cur) return true;
+        cur = prev;
+    }
+    return false;
 }
 
 // One CTA per bucket; the region and the bucket's records are bulk-copied
 // into shared memory.  Pass 1 puts every cell that is zero in the region
 // into the map with the minimum k-mer ordinal of its records; pass 2 applies
 // every record (saturating increment) and flags the map's minimum as new.
+// A bucket whose records fit one staging buffer keeps each record's map slot
+// from pass 1 (pass 2 looks up nothing); larger or denser buckets take the
+// general loop over buffer chunks and cell ranges.
 template <int STORAGE>
 __global__ void __launch_bounds__(SP_APPLY_BLOCK, 2)
 k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
@@ -523,6 +571,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     uint32_t* region = reinterpret_cast<uint32_t*>(sbytes);
     uint64_t* map = reinterpret_cast<uint64_t*>(sbytes + L.map_off);
     uint64_t* rbuf = reinterpret_cast<uint64_t*>(sbytes + L.rec_off);
+    uint16_t* rslot = reinterpret_cast<uint16_t*>(sbytes + L.slot_off);
     uint32_t* dirty = reinterpret_cast<uint32_t*>(sbytes + L.dirty_off);
     const uint64_t c0 = (uint64_t)(bk - sp.bbase[ti]) << sp.fs;
     const uint64_t w0 = c0 / cells_per_word<STORAGE>();
@@ -531,7 +580,10 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     const uint32_t* gsrc = tp.words[ti] + w0;
     // the region by one bulk copy when it is a whole number of 16-byte units
     const bool bulk_region = ((w0 & 3u) == 0) && ((nw & 3u) == 0);
-    const uint32_t n_chunks = (re - rs + SP_RBUF - 1) / SP_RBUF;
+    const uint32_t n_recs = re - rs;
+    const uint32_t n_chunks = (n_recs + SP_RBUF - 1) / SP_RBUF;
+    // dense buckets write the whole region back; sparse ones their dirty sectors
+    const bool track = n_recs < region_sectors;
     uint32_t phase = 0;
     // records of chunk c into rbuf, copied from the even index at or below
     // its first record (and the region with chunk 0)
@@ -546,31 +598,20 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     };
     if (threadIdx.x == 0) {
         abort_s = 0;
+        n_fresh = 0;
+        overflow = 0;
         mbar_init(&bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         chunk_copy(0, bulk_region);
     }
     if (!bulk_region)
         for (uint32_t k = threadIdx.x; k < nw; k += SP_APPLY_BLOCK) region[k] = __ldcs(gsrc + k);
-    for (uint32_t k = threadIdx.x; k < (region_sectors + 31) / 32; k += SP_APPLY_BLOCK) dirty[k] = 0;
+    if (track)
+        for (uint32_t k = threadIdx.x; k < (region_sectors + 31) / 32; k += SP_APPLY_BLOCK) dirty[k] = 0;
+    for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
     __syncthreads();   // the barrier is initialised before anyone waits on it
     if (!mbar_wait(&bar, phase & 1u)) atomicExch(&abort_s, 1u);
     ++phase;
-    uint32_t loaded = 0;   // chunk in rbuf
-    // all threads: make chunk c the one in rbuf (no-op when it already is)
-    auto need_chunk = [&](uint32_t c) -> bool {
-        if (c == loaded) return true;
-        __syncthreads();   // everyone is done with the old chunk
-        if (threadIdx.x == 0) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            chunk_copy(c, false);
-        }
-        if (!mbar_wait(&bar, phase & 1u)) atomicExch(&abort_s, 1u);
-        ++phase;
-        __syncthreads();
-        loaded = c;
-        return abort_s == 0;
-    };
     __syncthreads();
     if (abort_s) {
         if (threadIdx.x == 0) {
@@ -581,139 +622,170 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     }
     const uint32_t co_mask = region_cells - 1;
     unsigned long long occ = 0;
-    // cell ranges [lo, lo + width): one range normally; narrower when the
-    // zero cells of a range overflow the map
-    uint32_t lo = 0, width = region_cells;
-    int guard = 0;
-    bool ok = true;
-    for (; ok && lo < region_cells && guard < 4096; ++guard) {
-        const uint32_t hi = lo + width < region_cells ? lo + width : region_cells;
-        for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
-        if (threadIdx.x == 0) {
-            n_fresh = 0;
-            overflow = 0;
-        }
-        __syncthreads();
-        // pass 1: minimum ordinal per zero cell
+    bool done = false;
+    if (n_chunks == 1) {
+        // fast path: all records staged, the whole region as one cell range
+        const uint64_t* src = rbuf + (rs & 1u);
         uint32_t inserted = 0;
         bool lost = false;
-        for (uint32_t c = 0; c < n_chunks && ok; ++c) {
-            ok = need_chunk(c);
-            if (!ok) break;
-            const uint32_t a = rs + c * SP_RBUF;
-            const uint32_t cnt = re - a < SP_RBUF ? re - a : SP_RBUF;
-            const uint64_t* src = rbuf + (a & 1u);
-            for (uint32_t k = threadIdx.x; k < cnt; k += SP_APPLY_BLOCK) {
-                const uint64_t rec = src[k];
-                const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
-                if (co < lo || co >= hi) continue;
-                uint32_t word, shift;
-                region_cell<STORAGE>(co, word, shift);
-                if (cell_value<STORAGE>(region[word], shift) != 0) continue;
-                const uint64_t mine = (rec << 32) | co;   // (ordinal << 32) | cell
-                uint32_t sl = sp_slot(co);
-                bool done = false;
-                for (uint32_t it = 0; it < SP_MAPCAP; ++it) {
-                    uint64_t cur = map[sl];
-                    if (cur == SP_EMPTY) {
-                        cur = atomicCAS((unsigned long long*)&map[sl], SP_EMPTY, mine);
-                        if (cur == SP_EMPTY) {
-                            ++inserted;
-                            done = true;
-                            break;
-                        }
-                    }
-                    if ((uint32_t)cur == co) {
-                        if (mine < cur) atomicMin((unsigned long long*)&map[sl], mine);
-                        done = true;
-                        break;
-                    }
-                    sl = (sl + 1) & (SP_MAPCAP - 1);
-                }
-                lost |= !done;
+        for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
+            const uint64_t rec = src[k];
+            const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
+            uint32_t word, shift;
+            region_cell<STORAGE>(co, word, shift);
+            uint16_t sl16 = SP_NOSLOT;
+            if (cell_value<STORAGE>(region[word], shift) == 0) {
+                bool created;
+                const uint32_t sl = sp_map_insert(map, co, (uint32_t)rec, &created);
+                inserted += created;
+                lost |= sl >= SP_MAPCAP;
+                sl16 = sl < SP_MAPCAP ? (uint16_t)sl : SP_NOSLOT;
             }
+            rslot[k] = sl16;
         }
-        if (!ok) break;
-        // distinct zero cells of the range: one shared add per warp
         inserted = __reduce_add_sync(0xFFFFFFFFu, inserted);
         if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
         if (lost) overflow = 1;
         __syncthreads();
-        if ((overflow || n_fresh > SP_MAPCAP / 2) && width > 1) {
-            width >>= 1;   // redo this range narrower; nothing was applied yet
-            __syncthreads();
-            continue;
-        }
-        const bool any_fresh = n_fresh != 0;
-        // pass 2: apply every record of the range; the map's minimum is new
-        for (uint32_t c = 0; c < n_chunks && ok; ++c) {
-            ok = need_chunk(c);
-            if (!ok) break;
-            const uint32_t a = rs + c * SP_RBUF;
-            const uint32_t cnt = re - a < SP_RBUF ? re - a : SP_RBUF;
-            const uint64_t* src = rbuf + (a & 1u);
-            for (uint32_t k = threadIdx.x; k < cnt; k += SP_APPLY_BLOCK) {
+        if (!overflow && n_fresh <= SP_MAPCAP / 2) {
+            for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
                 const uint64_t rec = src[k];
                 const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
-                if (co < lo || co >= hi) continue;
                 const uint32_t g = (uint32_t)rec;
                 uint32_t word, shift;
                 region_cell<STORAGE>(co, word, shift);
-                bool changed = false;
-                if (STORAGE == GDBG_BIT) {
-                    const uint32_t bit = 1u << shift;
-                    const uint32_t old = atomicOr(region + word, bit);
-                    changed = (old & bit) == 0;
-                } else {
-                    uint32_t cur = region[word];
-                    for (int it = 0; it < (1 << 20); ++it) {
-                        if (cell_value<STORAGE>(cur, shift) >= cell_max<STORAGE>()) break;
-                        const uint32_t prev = atomicCAS(region + word, cur, cur + (1u << shift));
-                        if (prev == cur) {
-                            changed = true;
-                            break;
-                        }
-                        cur = prev;
-                    }
-                }
-                if (changed) {
+                const bool changed = sp_increment<STORAGE>(region, word, shift);
+                if (track && changed) {
                     const uint32_t sec = word >> 3;
                     atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
                 }
-                if (!any_fresh) continue;
-                // was the cell zero before the batch, and is this its first toucher?
-                uint32_t sl = sp_slot(co);
-                for (uint32_t it = 0; it < SP_MAPCAP; ++it) {
-                    const uint64_t cur = map[sl];
-                    if (cur == SP_EMPTY) break;
-                    if ((uint32_t)cur == co) {
-                        if ((uint32_t)(cur >> 32) == g && g < sp.kmer_cap) {
-                            atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
-                            if (ti == 0) ++occ;
-                        }
-                        break;
-                    }
-                    sl = (sl + 1) & (SP_MAPCAP - 1);
+                const uint16_t sl = rslot[k];
+                if (sl != SP_NOSLOT && (uint32_t)(map[sl] >> 32) == g && g < sp.kmer_cap) {
+                    atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
+                    if (ti == 0) ++occ;
                 }
             }
+            done = true;
         }
-        if (!ok) break;
         __syncthreads();
-        lo = hi;
     }
-    if (!ok) {
-        // a copy wait ran out: flag it, give that copy one more bounded wait, leave
-        if (threadIdx.x == 0) {
-            atomicOr(sp.err, GDBG_ERR_COPY_TIMEOUT);
-            mbar_wait(&bar, (phase - 1) & 1u);
+    if (!done) {
+        uint32_t loaded = 0;   // chunk in rbuf
+        // all threads: make chunk c the one in rbuf (no-op when it already is)
+        auto need_chunk = [&](uint32_t c) -> bool {
+            if (c == loaded) return true;
+            __syncthreads();   // everyone is done with the old chunk
+            if (threadIdx.x == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                chunk_copy(c, false);
+            }
+            if (!mbar_wait(&bar, phase & 1u)) atomicExch(&abort_s, 1u);
+            ++phase;
+            __syncthreads();
+            loaded = c;
+            return abort_s == 0;
+        };
+        // cell ranges [lo, lo + width): narrower when the zero cells of a
+        // range overflow the map (the fast path already tried the whole region)
+        uint32_t lo = 0, width = n_chunks == 1 ? region_cells >> 1 : region_cells;
+        int guard = 0;
+        bool ok = true;
+        for (; ok && lo < region_cells && guard < 4096; ++guard) {
+            const uint32_t hi = lo + width < region_cells ? lo + width : region_cells;
+            for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
+            if (threadIdx.x == 0) {
+                n_fresh = 0;
+                overflow = 0;
+            }
+            __syncthreads();
+            // pass 1: minimum ordinal per zero cell
+            uint32_t inserted = 0;
+            bool lost = false;
+            for (uint32_t c = 0; c < n_chunks && ok; ++c) {
+                ok = need_chunk(c);
+                if (!ok) break;
+                const uint32_t a = rs + c * SP_RBUF;
+                const uint32_t cnt = re - a < SP_RBUF ? re - a : SP_RBUF;
+                const uint64_t* src = rbuf + (a & 1u);
+                for (uint32_t k = threadIdx.x; k < cnt; k += SP_APPLY_BLOCK) {
+                    const uint64_t rec = src[k];
+                    const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
+                    if (co < lo || co >= hi) continue;
+                    uint32_t word, shift;
+                    region_cell<STORAGE>(co, word, shift);
+                    if (cell_value<STORAGE>(region[word], shift) != 0) continue;
+                    bool created;
+                    const uint32_t sl = sp_map_insert(map, co, (uint32_t)rec, &created);
+                    inserted += created;
+                    lost |= sl >= SP_MAPCAP;
+                }
+            }
+            if (!ok) break;
+            inserted = __reduce_add_sync(0xFFFFFFFFu, inserted);
+            if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
+            if (lost) overflow = 1;
+            __syncthreads();
+            if ((overflow || n_fresh > SP_MAPCAP / 2) && width > 1) {
+                width >>= 1;   // redo this range narrower; nothing was applied yet
+                __syncthreads();
+                continue;
+            }
+            const bool any_fresh = n_fresh != 0;
+            // pass 2: apply every record of the range; the map's minimum is new
+            for (uint32_t c = 0; c < n_chunks && ok; ++c) {
+                ok = need_chunk(c);
+                if (!ok) break;
+                const uint32_t a = rs + c * SP_RBUF;
+                const uint32_t cnt = re - a < SP_RBUF ? re - a : SP_RBUF;
+                const uint64_t* src = rbuf + (a & 1u);
+                for (uint32_t k = threadIdx.x; k < cnt; k += SP_APPLY_BLOCK) {
+                    const uint64_t rec = src[k];
+                    const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
+                    if (co < lo || co >= hi) continue;
+                    const uint32_t g = (uint32_t)rec;
+                    uint32_t word, shift;
+                    region_cell<STORAGE>(co, word, shift);
+                    const bool changed = sp_increment<STORAGE>(region, word, shift);
+                    if (track && changed) {
+                        const uint32_t sec = word >> 3;
+                        atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
+                    }
+                    if (!any_fresh) continue;
+                    // was the cell zero before the batch, and is this its first toucher?
+                    uint32_t sl = sp_slot(co);
+                    for (uint32_t it = 0; it < SP_MAPCAP; ++it) {
+                        const uint64_t cur = map[sl];
+                        if (cur == SP_EMPTY) break;
+                        if ((uint32_t)cur == co) {
+                            if ((uint32_t)(cur >> 32) == g && g < sp.kmer_cap) {
+                                atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
+                                if (ti == 0) ++occ;
+                            }
+                            break;
+                        }
+                        sl = (sl + 1) & (SP_MAPCAP - 1);
+                    }
+                }
+            }
+            if (!ok) break;
+            __syncthreads();
+            lo = hi;
         }
-        return;
+        if (!ok) {
+            // a copy wait ran out: flag it, give that copy one more bounded wait, leave
+            if (threadIdx.x == 0) {
+                atomicOr(sp.err, GDBG_ERR_COPY_TIMEOUT);
+                mbar_wait(&bar, (phase - 1) & 1u);
+            }
+            return;
+        }
+        if (lo < region_cells && threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
     }
-    if (lo < region_cells && threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
-    // write back the dirty 32-byte sectors (8 words each)
+    // write back the region: every sector of a dense bucket, the dirty ones
+    // of a sparse one (8 words each)
     uint32_t* gdst = tp.words[ti] + w0;
     for (uint32_t sec = threadIdx.x; sec < region_sectors; sec += SP_APPLY_BLOCK) {
-        if (!((dirty[sec >> 5] >> (sec & 31u)) & 1u)) continue;
+        if (track && !((dirty[sec >> 5] >> (sec & 31u)) & 1u)) continue;
         const uint32_t wb = sec * 8;
         if (bulk_region && wb + 8 <= nw) {
             uint4* g4 = reinterpret_cast<uint4*>(gdst + wb);
