@@ -42,7 +42,7 @@ def test_autotune_then_insert(cuda_ready, tmp_path, monkeypatch):
     g = G.dBG[G.NibbleStorage, G.FwdLemireShifter].build(G.NibbleStorage(tablesizes=sizes), 21)
     batches = batched.split_batches(pr, 64, 150_000)
     best = batched.autotune(g, batches[0][1], 64, 150_000)
-    assert best["schedule"]["path"] == "bucketed" and best["trials"]
+    assert best["schedule"]["path"] in ("bucketed", "bucketed_ordered") and best["trials"]
     again = batched.autotune(g, batches[0][1], 64, 150_000)   # from the cache
     assert again["schedule"] == best["schedule"]
     ref = oracle.Storage("nibble", sizes)
