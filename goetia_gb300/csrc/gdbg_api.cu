@@ -1647,6 +1647,31 @@ int gdbg_insert_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t pac
     return run_insert(g, b, nullptr, b.n_kmers, n_new, st);
 }
 
+int gdbg_insert_batch_async(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                            const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers,
+                            uint64_t* n_new, void* stream) {
+    if (!g || !offsets || (n_words && !packed)) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    cudaStream_t st = pick_stream(g, stream);
+    GDBG_TRY(g->st_packed.ensure(n_words + 1));
+    GDBG_TRY(g->st_offsets.ensure(n_reads + 1));
+    GDBG_TRY(g->st_out64.ensure(n_reads + 1));
+    if (n_words)
+        GDBG_CUDA(cudaMemcpyAsync(g->st_packed.p, packed, n_words * sizeof(uint32_t),
+                                  cudaMemcpyHostToDevice, st));
+    GDBG_CUDA(cudaMemcpyAsync(g->st_offsets.p, offsets, (n_reads + 1) * sizeof(uint64_t),
+                              cudaMemcpyHostToDevice, st));
+    BatchView b;
+    GDBG_TRY(prepare_batch(g, g->st_packed.p, n_words, g->st_offsets.p, n_reads, n_kmers, st, &b,
+                           insert_maps(g, n_kmers)));
+    if (n_reads) GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, n_reads * sizeof(uint64_t), st));
+    GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, g->st_out64.p, st));
+    if (n_new && n_reads)
+        GDBG_CUDA(cudaMemcpyAsync(n_new, g->st_out64.p, n_reads * sizeof(uint64_t),
+                                  cudaMemcpyDeviceToHost, st));
+    return GDBG_OK;
+}
+
 int gdbg_query_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                             const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
                             int16_t* counts, void* stream) {
@@ -1747,6 +1772,15 @@ int gdbg_device_status(gdbg_graph* g, uint32_t* status) {
     GDBG_CUDA(cudaMemcpyAsync(status, g->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
     GDBG_CUDA(cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream));
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    return GDBG_OK;
+}
+
+int gdbg_reserve_staging(gdbg_graph* g, uint64_t max_words, uint64_t max_reads) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    GDBG_TRY(g->st_packed.ensure(max_words + 1));
+    GDBG_TRY(g->st_offsets.ensure(max_reads + 1));
+    GDBG_TRY(g->st_out64.ensure(max_reads + 1));
     return GDBG_OK;
 }
 

@@ -630,6 +630,16 @@ class dBGBase:
         _lib.call("gdbg_insert_and_query_batch_device", self._h, packed_ptr, int(packed_words),
                   offsets_ptr, int(n_reads), hint, counts_ptr, n_new_ptr, _stream(stream))
 
+    def insert_async(self, packed_ptr, packed_words, offsets_ptr, n_reads, n_kmers, n_new_ptr,
+                     stream=None):
+        """gdbg_insert_batch_async: host (pinned) buffers in and out, all work
+        queued on `stream`; returns at once."""
+        _lib.call("gdbg_insert_batch_async", self._h, packed_ptr, int(packed_words), offsets_ptr,
+                  int(n_reads), int(n_kmers), n_new_ptr, _stream(stream))
+
+    def reserve_staging(self, max_words, max_reads):
+        _lib.call("gdbg_reserve_staging", self._h, int(max_words), int(max_reads))
+
     def query_device(self, packed_ptr, packed_words, offsets_ptr, n_reads, counts_ptr,
                      n_kmers=None, stream=None):
         hint = (1 << 64) - 1 if n_kmers is None else int(n_kmers)

@@ -9,10 +9,14 @@ samples at once on one GPU:
 * admission: a stream is admitted when its tables and scratch fit in the HBM
   budget; otherwise it waits until a finished stream releases its memory;
 * continuous batching: every admitted stream has its own CUDA stream; a chunk
-  is dispatched as soon as it arrives (host pinned staging -> H2D copy ->
-  insert -> D2H copy of the per-read new-k-mer counts -> event), up to
-  `depth` chunks of a stream in flight, so chunks of different streams overlap
-  on the device while each stream's chunks apply in arrival order;
+  is dispatched as soon as it arrives (host pinned staging, then one
+  asynchronous library call that queues the H2D copy, the insert and the D2H
+  copy of the per-read new-k-mer counts, then an event), up to `depth` chunks
+  of a stream in flight, so chunks of different streams overlap on the device
+  while each stream's chunks apply in arrival order;
+* admission ahead of arrival: while no arrived chunk waits, streams whose
+  first chunk is due within `lookahead_s` are admitted early, so building a
+  stream's graph does not hold up other streams' chunks;
 * completion: events are polled; a chunk's latency is completion time minus
   arrival time;
 * release: a finished stream's budget share is returned at once, but its
@@ -62,14 +66,17 @@ class ChunkResult:
 
 
 class _Slot:
-    def __init__(self, torch, dev, max_words, max_reads):
-        self.d_packed = torch.empty(max_words, dtype=torch.int32, device=dev)
-        self.d_off = torch.empty(max_reads + 1, dtype=torch.int64, device=dev)
-        self.d_new = torch.empty(max_reads, dtype=torch.int64, device=dev)
+    """Pinned host staging of one in-flight chunk (packed words, offsets, new
+    counts); the device side lives in the graph's staging buffers."""
+
+    def __init__(self, torch, max_words, max_reads):
         self.h_packed = torch.empty(max_words, dtype=torch.int32).pin_memory()
         self.h_off = torch.empty(max_reads + 1, dtype=torch.int64).pin_memory()
         self.h_new = torch.empty(max_reads, dtype=torch.int64).pin_memory()
-        self.nbytes = (max_words * 4 + (2 * max_reads + 1) * 8)
+        self.packed = self.h_packed.numpy()
+        self.off = self.h_off.numpy()
+        self.new = self.h_new.numpy()
+        self.event = torch.cuda.Event()   # recorded after the slot's chunk
 
 
 class _Stream:
@@ -84,7 +91,7 @@ class _Stream:
         self.graph.set_stream(self.cuda.cuda_stream)
         max_reads = max(c.n_reads for c in spec.chunks)
         max_words = max(c.packed.size for c in spec.chunks)
-        self.slots = [_Slot(torch, server.dev, max_words, max_reads) for _ in range(server.depth)]
+        self.slots = [_Slot(torch, max_words, max_reads) for _ in range(server.depth)]
         self.free = collections.deque(range(server.depth))
         self.inflight = collections.deque()      # (event, slot, index)
         self.next_chunk = 0                      # next chunk to dispatch
@@ -94,6 +101,7 @@ class _Stream:
         # allocation (and its device-wide synchronisation) happens while
         # serving
         self.graph.reserve(max_reads, max(c.n_kmers(server.K) for c in spec.chunks))
+        self.graph.reserve_staging(max_words, max_reads)
 
     def table_bytes(self):
         return sum(self.graph.table_bytes())
@@ -116,7 +124,8 @@ class Server:
     """Continuous-batching server for many dBG streams on one GPU."""
 
     def __init__(self, storage_type=D.BitStorage, shifter_type=D.CanLemireShifter, K=31,
-                 n_tables=4, hbm_budget=16 << 30, depth=2, window=262144, device=0):
+                 n_tables=4, hbm_budget=16 << 30, depth=2, window=262144, device=0,
+                 lookahead_s=0.05):
         import torch
         self.torch = torch
         self.dev = torch.device("cuda", device)
@@ -127,16 +136,31 @@ class Server:
         self.budget = hbm_budget
         self.depth = depth
         self.window = window
+        self.lookahead = lookahead_s
 
     def footprint(self, spec):
+        """Device bytes of a stream: tables and insert scratch, plus the
+        staging of its largest chunk."""
         return stream_footprint(self.storage_type, spec.max_table, self.n_tables, self.window) + \
-            self.depth * (max(c.packed.size for c in spec.chunks) * 4 +
-                          (2 * max(c.n_reads for c in spec.chunks) + 1) * 8)
+            (max(c.packed.size for c in spec.chunks) * 4 +
+             (2 * max(c.n_reads for c in spec.chunks) + 1) * 8)
 
     def run(self, specs, time_scale=1.0, max_seconds=600.0):
         """Serve every stream's chunks at their arrival times.  Returns
         (results, stats): results per stream id (list of ChunkResult in chunk
-        order), stats with latency percentiles, throughput and admission."""
+        order), stats with latency percentiles, throughput and admission.
+        Python's cyclic garbage collector is paused for the run (a full
+        collection would stall dispatch for tens of milliseconds)."""
+        import gc
+        was_enabled = gc.isenabled()
+        gc.disable()
+        try:
+            return self._run(specs, time_scale, max_seconds)
+        finally:
+            if was_enabled:
+                gc.enable()
+
+    def _run(self, specs, time_scale, max_seconds):
         torch = self.torch
         order = sorted(specs, key=lambda s: s.arrivals[0])
         waiting = collections.deque(order)       # not yet admitted
@@ -159,14 +183,20 @@ class Server:
             now = (time.perf_counter() - t0) / time_scale
             if now > max_seconds:
                 raise TimeoutError("serving run exceeded its time limit")
-            # admission: streams whose first chunk has arrived, in arrival order
-            while waiting and waiting[0].arrivals[0] <= now:
+            # admission: streams whose first chunk has arrived, in arrival
+            # order; ahead of their arrival when nothing is waiting to go
+            idle = all(not (st.free and st.next_chunk < len(st.spec.chunks)
+                            and st.spec.arrivals[st.next_chunk] <= now)
+                       for st in active.values())
+            horizon = now + (self.lookahead if idle else 0.0)
+            while waiting and waiting[0].arrivals[0] <= horizon:
                 spec = waiting[0]
                 need = self.footprint(spec)
                 if need > self.budget:
                     raise MemoryError(f"stream {spec.sid} needs {need} bytes, over the budget")
                 if used + need > self.budget:
-                    waited.add(spec.sid)
+                    if spec.arrivals[0] <= now:
+                        waited.add(spec.sid)
                     break
                 if zombies and used + zombie_bytes + need > self.budget:
                     zombies.clear()                 # frees their device memory
@@ -190,22 +220,16 @@ class Server:
                     c = spec.chunks[i]
                     td = time.perf_counter()
                     delay.append((td - t0) / time_scale - spec.arrivals[i])
-                    slot = st.slots[st.free.popleft()]
+                    si = st.free.popleft()
+                    slot = st.slots[si]
                     nw, nr = c.packed.size, c.n_reads
-                    slot.h_packed[:nw].numpy()[:] = c.packed.view(np.int32)
-                    slot.h_off[:nr + 1].numpy()[:] = c.offsets.view(np.int64)
-                    with torch.cuda.stream(st.cuda):
-                        slot.d_packed[:nw].copy_(slot.h_packed[:nw], non_blocking=True)
-                        slot.d_off[:nr + 1].copy_(slot.h_off[:nr + 1], non_blocking=True)
-                    nk = c.n_kmers(self.K)
-                    st.graph.insert_device(slot.d_packed.data_ptr(), nw, slot.d_off.data_ptr(),
-                                           nr, n_kmers=nk, n_new_ptr=slot.d_new.data_ptr(),
-                                           stream=st.cuda.cuda_stream)
-                    with torch.cuda.stream(st.cuda):
-                        slot.h_new[:nr].copy_(slot.d_new[:nr], non_blocking=True)
-                        ev = torch.cuda.Event()
-                        ev.record(st.cuda)
-                    st.inflight.append((ev, st.slots.index(slot), i))
+                    slot.packed[:nw] = c.packed.view(np.int32)
+                    slot.off[:nr + 1] = c.offsets.view(np.int64)
+                    st.graph.insert_async(slot.h_packed.data_ptr(), nw, slot.h_off.data_ptr(), nr,
+                                          c.n_kmers(self.K), slot.h_new.data_ptr(),
+                                          stream=st.cuda.cuda_stream)
+                    slot.event.record(st.cuda)
+                    st.inflight.append((slot.event, si, i))
                     st.next_chunk += 1
                     dispatch_s.append(time.perf_counter() - td)
                     if first_dispatch is None:
@@ -219,7 +243,7 @@ class Server:
                     c = st.spec.chunks[i]
                     slot = st.slots[si]
                     r = ChunkResult(sid, i, c.n_reads, c.n_kmers(self.K),
-                                    slot.h_new[:c.n_reads].numpy().view(np.uint64).copy(),
+                                    slot.new[:c.n_reads].view(np.uint64).copy(),
                                     st.spec.arrivals[i], done)
                     st.results.append(r)
                     lat.append(r.latency)

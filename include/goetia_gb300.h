@@ -207,6 +207,17 @@ int gdbg_neighbor_masks_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_
 int gdbg_insert_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                              const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
                              uint64_t* n_new, void* stream);
+/* gdbg_insert_batch_device fed from host buffers, asynchronously: the copy
+ * of packed/offsets to the handle's staging buffers, the insert and the copy
+ * of the per-read new counts back to n_new (may be NULL) are all queued on
+ * `stream`; the call returns at once.  The host buffers must stay untouched
+ * until the stream has passed this call (record an event after it); with
+ * pinned buffers the copies overlap other streams' work.  n_kmers is the
+ * batch's k-mer count (or an upper bound).  Calls on one handle reuse its
+ * staging buffers in stream order. */
+int gdbg_insert_batch_async(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                            const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers,
+                            uint64_t* n_new, void* stream);
 int gdbg_query_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                             const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
                             int16_t* counts, void* stream);
@@ -259,6 +270,10 @@ int gdbg_device_status(gdbg_graph* g, uint32_t* status);
  * max_reads reads and max_kmers k-mers now, so later inserts within that
  * size allocate nothing. */
 int gdbg_reserve(gdbg_graph* g, uint64_t max_reads, uint64_t max_kmers);
+/* Grow the host-call staging buffers for batches of up to max_words packed
+ * words and max_reads reads (gdbg_insert_batch_async and the host-buffer
+ * batch calls then allocate nothing up to that size). */
+int gdbg_reserve_staging(gdbg_graph* g, uint64_t max_words, uint64_t max_reads);
 /* Per-stage timing: when on, every stage of a batch insert is bracketed by
  * CUDA events on its stream.  gdbg_stage_times synchronises, returns the
  * accumulated milliseconds and launch counts per stage (names comma-separated
