@@ -69,6 +69,9 @@ SIGNATURES = {
     "gdbg_insert_and_query_batch": [c_vp, u32p, c_u64, u64p, c_u64, i16p, u64p],
     "gdbg_hashes_batch": [c_vp, u32p, c_u64, u64p, c_u64, u64p, u64p, u64p],
     "gdbg_neighbor_masks_batch": [c_vp, u32p, c_u64, u64p, c_u64, u8p],
+    "gdbg_compactor_sequence": [c_vp, c_cp, c_u64, u8p, u8p],
+    "gdbg_compactor_batch": [c_vp, u32p, c_u64, u64p, c_u64, u8p, u8p],
+    "gdbg_compactor_batch_device": [c_vp, c_vp, c_u64, c_vp, c_u64, c_u64, c_vp, c_vp, c_vp],
     "gdbg_insert_batch_device": [c_vp, c_vp, c_u64, c_vp, c_u64, c_u64, c_vp, c_vp],
     "gdbg_insert_batch_async": [c_vp, c_vp, c_u64, c_vp, c_u64, c_u64, c_vp, c_vp],
     "gdbg_reserve_staging": [c_vp, c_u64, c_u64],

@@ -128,6 +128,8 @@ struct gdbg_graph {
     DevBuf<uint32_t> hist, hist_off, scan_parts, bstart, new_bits;
     DevBuf<uint8_t> iq_vals;    // insert_and_query: post-insert value per table and k-mer
     DevBuf<uint32_t> sp_hist2, sp_off2, sp_plan;   // segmented path: pass-2 counts, plan
+    DevBuf<uint64_t> cq_keys;                      // compactor query: per-read new-k-mer sets
+    DevBuf<uint32_t> cq_min, cq_ones;
     uint32_t* d_epoch = nullptr;
     unsigned int* d_bar = nullptr;
     bool epoch_on_device = false;
@@ -848,6 +850,25 @@ int run_insert_query(gdbg_graph* g, const BatchView& b, int16_t* counts, uint64_
     return run_insert_bucketed(g, b, n_new, st, counts);
 }
 
+// Compactor query of a batch (gdbg_compactor.cu): flags and masks per k-mer.
+int run_compactor(gdbg_graph* g, const BatchView& b, uint8_t* flags, uint8_t* masks,
+                  cudaStream_t st) {
+    if (b.n_kmers == 0) return GDBG_OK;
+    if (b.n_reads >= 0xFFFFFFFFull) return fail(GDBG_ERR_INVALID_ARG, "too many reads");
+    const uint64_t slots = compactor_slots(b.n_kmers, b.n_reads);
+    GDBG_TRY(g->cq_keys.ensure(slots));
+    GDBG_TRY(g->cq_min.ensure(slots));
+    GDBG_TRY(g->cq_ones.ensure(b.n_reads + 1));
+    GDBG_CUDA(cudaMemsetAsync(g->cq_keys.p, 0xFF, slots * sizeof(uint64_t), st));
+    GDBG_CUDA(cudaMemsetAsync(g->cq_min.p, 0xFF, slots * sizeof(uint32_t), st));
+    GDBG_CUDA(cudaMemsetAsync(g->cq_ones.p, 0xFF, (b.n_reads + 1) * sizeof(uint32_t), st));
+    cudaError_t e = launch_compactor(g->storage, g->shape(4), st, b, g->hp, g->ts->tp, g->cq_keys.p,
+                                     g->cq_min.p, g->cq_ones.p, flags, masks, g->d_err);
+    if (e != cudaSuccess) return fail(GDBG_ERR_CUDA, std::string("compactor launch: ") + cudaGetErrorString(e));
+    g->launches += 2;
+    return GDBG_OK;
+}
+
 int run_query(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64_t n_total,
               int16_t* counts, uint64_t* values, cudaStream_t st) {
     if (n_total == 0) return GDBG_OK;
@@ -1018,6 +1039,7 @@ int gdbg_destroy(gdbg_graph* g) {
     g->rec_a.release(); g->rec_b.release(); g->hist.release(); g->hist_off.release();
     g->scan_parts.release(); g->bstart.release(); g->new_bits.release(); g->iq_vals.release();
     g->sp_hist2.release(); g->sp_off2.release(); g->sp_plan.release();
+    g->cq_keys.release(); g->cq_min.release(); g->cq_ones.release();
     g->st_packed.release(); g->st_offsets.release(); g->st_out64.release();
     g->st_out64b.release(); g->st_out64c.release(); g->st_counts.release(); g->st_u8.release();
     for (auto& p : g->pending) {
@@ -1633,6 +1655,52 @@ int gdbg_neighbor_masks_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_
 }
 
 // ---- packed batches, device buffers ---------------------------------------
+
+int gdbg_compactor_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                         const uint64_t* offsets, uint64_t n_reads, uint8_t* flags,
+                         uint8_t* masks) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b));
+    if (b.n_kmers && (!flags || !masks)) return fail(GDBG_ERR_INVALID_ARG, "NULL output");
+    GDBG_TRY(g->st_u8.ensure(2 * b.n_kmers + 2));
+    uint8_t* dflags = g->st_u8.p;
+    uint8_t* dmasks = g->st_u8.p + b.n_kmers + 1;
+    GDBG_TRY(run_compactor(g, b, dflags, dmasks, g->stream));
+    if (b.n_kmers) {
+        GDBG_CUDA(cudaMemcpyAsync(flags, dflags, b.n_kmers, cudaMemcpyDeviceToHost, g->stream));
+        GDBG_CUDA(cudaMemcpyAsync(masks, dmasks, b.n_kmers, cudaMemcpyDeviceToHost, g->stream));
+    }
+    return check_device_status(g);
+}
+
+int gdbg_compactor_sequence(gdbg_graph* g, const char* seq, uint64_t len, uint8_t* flags,
+                            uint8_t* masks) {
+    if (!g || !flags || !masks) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    BatchView b;
+    GDBG_TRY(stage_string(g, seq, len, &b));
+    GDBG_TRY(g->st_u8.ensure(2 * b.n_kmers + 2));
+    uint8_t* dflags = g->st_u8.p;
+    uint8_t* dmasks = g->st_u8.p + b.n_kmers + 1;
+    GDBG_TRY(run_compactor(g, b, dflags, dmasks, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(flags, dflags, b.n_kmers, cudaMemcpyDeviceToHost, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(masks, dmasks, b.n_kmers, cudaMemcpyDeviceToHost, g->stream));
+    return check_device_status(g);
+}
+
+int gdbg_compactor_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                                const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
+                                uint8_t* flags, uint8_t* masks, void* stream) {
+    if (!g || !offsets) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
+    GDBG_TRY(set_device(g));
+    cudaStream_t st = pick_stream(g, stream);
+    BatchView b;
+    GDBG_TRY(prepare_batch(g, packed, packed_words, offsets, n_reads, n_kmers_hint, st, &b));
+    if (b.n_kmers && (!flags || !masks)) return fail(GDBG_ERR_INVALID_ARG, "NULL output");
+    return run_compactor(g, b, flags, masks, st);
+}
 
 int gdbg_insert_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                              const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,

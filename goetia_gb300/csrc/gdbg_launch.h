@@ -97,6 +97,15 @@ cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams
                             unsigned long long* counters, cudaStream_t st);
 size_t sp_apply_smem_bytes(int storage, uint32_t fs);
 
+// Compactor query (gdbg_compactor.cu): per k-mer new / seen flags and the
+// neighbour masks over the storage plus each read's new k-mers.  keys /
+// minpos hold compactor_slots() entries set to all ones, allones n_reads.
+cudaError_t launch_compactor(int storage, const LaunchShape& s, cudaStream_t st, const BatchView& b,
+                             const HashParams& hp, const TableParams& tp, uint64_t* keys,
+                             uint32_t* minpos, uint32_t* allones, uint8_t* flags, uint8_t* masks,
+                             uint32_t* err);
+uint64_t compactor_slots(uint64_t n_kmers, uint64_t n_reads);
+
 // OR-merge of two identically laid out table allocations (n_words, a
 // multiple of 4); cells newly set in the first count_words words are added
 // to *occupied.

@@ -573,6 +573,34 @@ class dBGBase:
                   _p(r.offsets, _lib.u64p), r.n_reads, _p(n_new, _lib.u64p), _c.byref(nk))
         return n_new[:r.n_reads]
 
+    def compactor_query(self, sequence):
+        """The compactor's per-k-mer query of one sequence (compactor.hh:
+        346-466) against the storage as it is: (new, seen, masks) arrays --
+        new = query() == 0, seen = already in the sequence's new-k-mer set,
+        masks = neighbour masks over the storage plus the sequence's new
+        k-mers (filter_nodes with extras, unitig_walker.hh:457-469)."""
+        s = _b(sequence)
+        n = len(s) - self.K + 1
+        if n < 1:
+            raise _lib.SequenceLengthException(_lib.ERR_SEQUENCE_LENGTH,
+                                               "Sequence must have length >= K")
+        fl = np.zeros(n, np.uint8)
+        ms = np.zeros(n, np.uint8)
+        _lib.call("gdbg_compactor_sequence", self._h, s, len(s), _p(fl, _lib.u8p), _p(ms, _lib.u8p))
+        return (fl & 1).astype(bool), (fl & 2).astype(bool), ms
+
+    def compactor_query_packed(self, reads):
+        """compactor_query for every read of a batch (each against the
+        storage as it is before the call): flattened (flags, masks), flags
+        bit 0 = new, bit 1 = seen."""
+        r = self._packed(reads)
+        n = r.n_kmers(self.K)
+        fl = np.zeros(max(n, 1), np.uint8)
+        ms = np.zeros(max(n, 1), np.uint8)
+        _lib.call("gdbg_compactor_batch", self._h, _p(r.packed, _lib.u32p), r.packed.size,
+                  _p(r.offsets, _lib.u64p), r.n_reads, _p(fl, _lib.u8p), _p(ms, _lib.u8p))
+        return fl[:n], ms[:n]
+
     def insert_and_query_packed(self, reads):
         """insert_and_query_sequence for every read in order: (flattened
         counts, per-read new counts), equal to the sequential calls."""

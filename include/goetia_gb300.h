@@ -196,6 +196,24 @@ int gdbg_hashes_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
 int gdbg_neighbor_masks_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                               const uint64_t* offsets, uint64_t n_reads, uint8_t* masks);
 
+/* The compactor's per-k-mer query (StreamingCompactor::find_new_segments,
+ * compactor.hh:346-466), every read against the storage as it is (the
+ * compactor inserts a sequence's k-mers only after this query):
+ *   flags bit 0: new   -- query() == 0 (compactor.hh:364)
+ *   flags bit 1: seen  -- the hash is already in the read's new-k-mer set
+ *                         at this position (compactor.hh:365)
+ *   masks: the 8-bit neighbour mask (as gdbg_neighbor_masks) where a
+ *          neighbour is present when query() != 0 or it is one of the
+ *          read's new k-mers (filter_nodes with extras, unitig_walker.hh:
+ *          457-469; get_decision_neighbors(..., union_nodes), :1054-1083).
+ * Decision k-mers of the compactor's segments are those whose mask has more
+ * than one left or more than one right neighbour. */
+int gdbg_compactor_sequence(gdbg_graph* g, const char* seq, uint64_t len, uint8_t* flags,
+                            uint8_t* masks);
+int gdbg_compactor_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                         const uint64_t* offsets, uint64_t n_reads, uint8_t* flags,
+                         uint8_t* masks);
+
 /* ---- packed batches, device buffers (asynchronous) --------------------- */
 
 /* Same as gdbg_insert_batch with device pointers, asynchronous on `stream`.
@@ -228,6 +246,9 @@ int gdbg_insert_and_query_batch_device(gdbg_graph* g, const uint32_t* packed,
 int gdbg_hashes_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                              const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
                              uint64_t* values, uint64_t* fw, uint64_t* rc, void* stream);
+int gdbg_compactor_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
+                                const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers_hint,
+                                uint8_t* flags, uint8_t* masks, void* stream);
 int gdbg_neighbor_masks_batch_device(gdbg_graph* g, const uint32_t* packed,
                                      uint64_t packed_words, const uint64_t* offsets,
                                      uint64_t n_reads, uint64_t n_kmers_hint, uint8_t* masks,

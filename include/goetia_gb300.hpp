@@ -194,6 +194,16 @@ public:
         hashes.insert(hashes.end(), h.begin(), h.end());
     }
 
+    // the compactor's per-k-mer query (compactor.hh:346-466): flags bit 0 new,
+    // bit 1 seen; masks over the storage plus the sequence's new k-mers
+    void compactor_query(const std::string& seq, std::vector<uint8_t>& flags,
+                         std::vector<uint8_t>& masks) {
+        if (seq.size() < K_) throw SequenceLengthException("Sequence must have length >= K");
+        flags.assign(seq.size() - K_ + 1, 0);
+        masks.assign(seq.size() - K_ + 1, 0);
+        check(gdbg_compactor_sequence(g_, seq.data(), seq.size(), flags.data(), masks.data()));
+    }
+
     // get_hash_iter as a vector (dbg.hh:421-425)
     std::vector<hash_type> get_hashes(const std::string& seq) const {
         if (seq.size() < K_) throw SequenceLengthException("Sequence must have length >= K");

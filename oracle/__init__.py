@@ -71,6 +71,7 @@ def lib():
         L.orc_insert_and_query_reads.argtypes = [ctypes.c_void_p] + batch + [i16p]
         L.orc_query_reads.argtypes = [ctypes.c_void_p] + batch + [i16p]
         L.orc_decision_masks.argtypes = [ctypes.c_void_p] + batch + [u8p]
+        L.orc_compactor_reads.argtypes = [ctypes.c_void_p] + batch + [u8p, u8p]
         L.orc_insert_reads_mt.restype = ctypes.c_uint64
         L.orc_insert_reads_mt.argtypes = [ctypes.c_void_p] + batch + [ctypes.c_int]
         L.orc_pack_ascii.restype = ctypes.c_int64
@@ -163,6 +164,16 @@ class Storage:
         lib().orc_query_reads(self.h, int(canonical), K, _p(packed, u32p), _p(offsets, u64p),
                               len(offsets) - 1, _p(out, i16p))
         return out[:nk]
+
+    def compactor_reads(self, canonical, K, packed, offsets):
+        """Per k-mer (flags, masks) of the compactor query: bit 0 new, bit 1
+        seen; masks over the storage plus each read's new k-mers."""
+        nk = count_kmers(K, offsets)
+        fl = np.zeros(max(nk, 1), np.uint8)
+        ms = np.zeros(max(nk, 1), np.uint8)
+        lib().orc_compactor_reads(self.h, int(canonical), K, _p(packed, u32p), _p(offsets, u64p),
+                                  len(offsets) - 1, _p(fl, u8p), _p(ms, u8p))
+        return fl[:nk], ms[:nk]
 
     def decision_masks(self, canonical, K, packed, offsets):
         nk = count_kmers(K, offsets)

@@ -387,6 +387,87 @@ void orc_decision_masks(const orc_storage* s, int canonical, uint16_t K, const u
     walk_reads(canonical, K, packed, off, n, 0, 1, m_cb, &x);
 }
 
+/* ---- compactor query (compactor.hh:346-466) ------------------------------ */
+/* Per k-mer of a read, against the storage as it is: flags bit 0 = new
+ * (query() == 0), bit 1 = seen (the hash is already in the read's new-k-mer
+ * set at this position); mask = neighbour mask where a neighbour is present
+ * when query() != 0 or it is one of the read's new k-mers (filter_nodes with
+ * extras, unitig_walker.hh:457-469). */
+typedef struct { uint64_t h; uint64_t p; } hp_pair;
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return x < y ? -1 : x > y;
+}
+static int cmp_hp(const void* a, const void* b) {
+    const hp_pair* x = (const hp_pair*)a; const hp_pair* y = (const hp_pair*)b;
+    if (x->h != y->h) return x->h < y->h ? -1 : 1;
+    return x->p < y->p ? -1 : x->p > y->p;
+}
+typedef struct { uint64_t* h; uint64_t k; } collect_ctx;
+static void collect_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    collect_ctx* x = (collect_ctx*)c;
+    x->h[x->k++] = sh_value(sh);
+}
+typedef struct {
+    const orc_storage* s; const uint64_t* set; uint64_t n_set;
+    uint8_t* masks; uint64_t k; const uint32_t* packed; const uint64_t* off; uint16_t K;
+} cm_ctx;
+static int in_set(const cm_ctx* x, uint64_t h) {
+    return x->n_set && bsearch(&h, x->set, x->n_set, sizeof(uint64_t), cmp_u64) != NULL;
+}
+static void cm_cb(void* c, uint64_t r, uint64_t p, const shifter* cur) {
+    cm_ctx* x = (cm_ctx*)c;
+    uint64_t b = x->off[r] + p;
+    int front = packed_at(x->packed, b), back = packed_at(x->packed, b + x->K - 1);
+    shifter s = *cur;
+    uint8_t m = 0;
+    for (int sym = 0; sym < 4; ++sym) {
+        sh_shift_left(&s, sym, back);
+        uint64_t h = sh_value(&s);
+        if (orc_query(x->s, h) || in_set(x, h)) m |= (uint8_t)(1u << sym);
+        sh_shift_right(&s, sym, back);
+    }
+    for (int sym = 0; sym < 4; ++sym) {
+        sh_shift_right(&s, front, sym);
+        uint64_t h = sh_value(&s);
+        if (orc_query(x->s, h) || in_set(x, h)) m |= (uint8_t)(1u << (4 + sym));
+        sh_shift_left(&s, front, sym);
+    }
+    x->masks[x->k++] = m;
+}
+
+void orc_compactor_reads(const orc_storage* s, int canonical, uint16_t K, const uint32_t* packed,
+                         const uint64_t* off, uint64_t n, uint8_t* flags, uint8_t* masks) {
+    uint64_t k0 = 0;
+    for (uint64_t r = 0; r < n; ++r) {
+        uint64_t L = off[r + 1] - off[r];
+        if (L < K) continue;
+        uint64_t nk = L - K + 1;
+        uint64_t* h = (uint64_t*)malloc(nk * sizeof(uint64_t));
+        hp_pair* pairs = (hp_pair*)malloc(nk * sizeof(hp_pair));
+        uint64_t* set = (uint64_t*)malloc(nk * sizeof(uint64_t));
+        collect_ctx cc = {h, 0};
+        walk_reads(canonical, K, packed, off + r, 1, 0, 1, collect_cb, &cc);
+        uint64_t np = 0;
+        for (uint64_t p = 0; p < nk; ++p) {
+            int is_new = orc_query(s, h[p]) == 0;
+            flags[k0 + p] = (uint8_t)is_new;
+            if (is_new) { pairs[np].h = h[p]; pairs[np].p = p; ++np; }
+        }
+        qsort(pairs, np, sizeof(hp_pair), cmp_hp);
+        uint64_t ns = 0;
+        for (uint64_t i = 0; i < np; ++i) {
+            if (i > 0 && pairs[i].h == pairs[i - 1].h) flags[k0 + pairs[i].p] |= 2;   /* seen */
+            else set[ns++] = pairs[i].h;
+        }
+        cm_ctx mc = {s, set, ns, masks + k0, 0, packed, off + r, K};
+        /* walk_reads indexes offsets by the local read 0 */
+        walk_reads(canonical, K, packed, off + r, 1, 0, 1, cm_cb, &mc);
+        free(h); free(pairs); free(set);
+        k0 += nk;
+    }
+}
+
 /* ---- multi-threaded insert (throughput baseline) ----------------------- */
 /* Atomic cell updates in the spirit of the reference's thread-safe storages
  * (__sync_fetch_and_or bitstorage.hh:203-209; __sync_add_and_fetch

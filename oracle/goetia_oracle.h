@@ -61,6 +61,11 @@ void     orc_insert_and_query_reads(orc_storage* s, int canonical, uint16_t K,
 void     orc_query_reads(const orc_storage* s, int canonical, uint16_t K,
                          const uint32_t* packed, const uint64_t* offsets,
                          uint64_t n_reads, int16_t* counts);
+/* compactor.hh:346-466: per k-mer new / seen flags and neighbour masks over
+ * the storage plus the read's new k-mers. */
+void     orc_compactor_reads(const orc_storage* s, int canonical, uint16_t K,
+                             const uint32_t* packed, const uint64_t* off, uint64_t n,
+                             uint8_t* flags, uint8_t* masks);
 void     orc_decision_masks(const orc_storage* s, int canonical, uint16_t K,
                             const uint32_t* packed, const uint64_t* offsets,
                             uint64_t n_reads, uint8_t* masks);

@@ -36,6 +36,7 @@
 #include <cstdlib>
 #include <fstream>
 #include <iostream>
+#include <set>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -143,6 +144,45 @@ static int run(uint16_t K, uint16_t n_tables, uint64_t max_table,
             iq.insert(iq.end(), c.begin(), c.end());
         }
         dump(out + "/iq_counts.i16", iq);
+    }
+
+    // Compactor query (compactor.hh:346-466 with filter_nodes and extras,
+    // unitig_walker.hh:457-469): graph H holds the first half of the reads;
+    // every k-mer of the second half gets new = query() == 0, seen = already
+    // in the read's new-k-mer set, and its neighbour mask over the storage
+    // plus the read's new k-mers.
+    {
+        auto sh = Storage::build(max_table, n_tables);
+        auto gh = dBG<Storage, Shifter>::build(sh, K);
+        const size_t half = reads.size() / 2;
+        for (size_t r = 0; r < half; ++r)
+            if (reads[r].size() >= K) gh->insert_sequence(reads[r]);
+        std::vector<uint8_t> cflags, cmasks;
+        auto sym_index = [](char c) { return c == 'A' ? 0 : c == 'C' ? 1 : c == 'G' ? 2 : 3; };
+        for (size_t r = half; r < reads.size(); ++r) {
+            const std::string& s = reads[r];
+            if (s.size() < K) continue;
+            std::set<hash_type> new_kmers;
+            auto it = gh->get_hash_iter(s);
+            while (!it->done()) {
+                hash_type h = it->next();
+                const bool cur_new = gh->query(h) == 0;
+                const bool cur_seen = new_kmers.count(h) > 0;
+                if (cur_new && !cur_seen) new_kmers.insert(h);
+                cflags.push_back((uint8_t)((cur_new ? 1 : 0) | (cur_seen ? 2 : 0)));
+            }
+            for (size_t p = 0; p + K <= s.size(); ++p) {
+                gh->set_cursor(s.substr(p, K));
+                auto left = gh->filter_nodes(gh->left_extensions(), new_kmers);
+                auto right = gh->filter_nodes(gh->right_extensions(), new_kmers);
+                uint8_t m = 0;
+                for (auto& e : left) m |= (uint8_t)(1u << sym_index(e.symbol));
+                for (auto& e : right) m |= (uint8_t)(1u << (4 + sym_index(e.symbol)));
+                cmasks.push_back(m);
+            }
+        }
+        dump(out + "/compactor_flags.u8", cflags);
+        dump(out + "/compactor_masks.u8", cmasks);
     }
 
     // BitStorage::update_from (bitstorage.cc:103-137): graph A holds the first

@@ -5,7 +5,9 @@ reference sources by ``make -C oracle ref``) on seeded read sets and stores
 its answers: k-mer hashes, per-read new-k-mer counts, table bytes,
 query_sequence counts, neighbour masks, find_decision_kmers positions,
 n_unique / n_occupied, the OXLI file written by dBG::save, the
-insert_and_query_sequence counts and (Bit) the
+insert_and_query_sequence counts, the compactor's per-k-mer new / seen flags
+and neighbour masks with the read's new k-mers (second half of the reads
+against a graph of the first half) and (Bit) the
 tables after BitStorage::update_from of two half-read graphs.  The cases cover every storage kind, both shifters,
 K = 21, 27, 31, 64 (rotation by K mod 64 == 0) and 101 (K > 64), short
 reads, duplicate reads, reverse-complement reads, tiny tables (collisions)
@@ -97,6 +99,8 @@ def run_case(case, workdir):
     data["table_bytes"] = np.array([len(t) for t in tables], np.uint64)
     data["oxli"] = rd("saved.oxli", np.uint8)
     data["iq_counts"] = rd("iq_counts.i16", np.int16)
+    data["compactor_flags"] = rd("compactor_flags.u8", np.uint8)
+    data["compactor_masks"] = rd("compactor_masks.u8", np.uint8)
     if kind == "bit":
         data["merge_stats"] = rd("merge_stats.u64", np.uint64)
         data["merged"] = rd("merged.u8", np.uint8)

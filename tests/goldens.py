@@ -37,6 +37,9 @@ class Case:
         self.tables = [t[a:b] for a, b in zip(np.r_[0, np.cumsum(tb)[:-1]], np.cumsum(tb))]
         self.oxli = d["oxli"].tobytes()     # the file dBG::save wrote
         self.iq_counts = d["iq_counts"]      # insert_and_query_sequence, fresh tables
+        # compactor query of the second half of the reads against a graph of the first half
+        self.compactor_flags = d["compactor_flags"]
+        self.compactor_masks = d["compactor_masks"]
         # Bit only: A (first half of the reads) after A.update_from(B)
         self.merge_stats = d["merge_stats"] if "merge_stats" in d else None
         if "merged" in d:

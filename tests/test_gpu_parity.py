@@ -277,3 +277,48 @@ def test_segmented_dense_buckets(cuda_ready, kind):
     for a, t in zip(g.get_raw(), ref.tables()):
         assert np.array_equal(a, t)
     assert (g.n_unique(), g.n_occupied()) == ref.stats()
+
+
+@pytest.mark.parametrize("name", names())
+def test_compactor_query_golden(cuda_ready, name):
+    """Second half of the reads against a graph of the first half: new / seen
+    flags and masks with the read's new k-mers equal the reference's
+    (find_new_segments' loop and filter_nodes with extras)."""
+    c = Case(name)
+    half = len(c.reads) // 2
+    g = graph_for(c.storage, c.canonical, c.K, c.sizes)
+    for s in c.reads[:half]:
+        if len(s) >= c.K:
+            g.insert_sequence(s)
+    flags, masks = g.compactor_query_packed(G.pack_reads(c.reads[half:]))
+    assert np.array_equal(flags, c.compactor_flags)
+    assert np.array_equal(masks, c.compactor_masks)
+    # per sequence
+    k = 0
+    for s in c.reads[half:]:
+        if len(s) < c.K:
+            continue
+        n = len(s) - c.K + 1
+        new, seen, m = g.compactor_query(s)
+        assert np.array_equal(new, (c.compactor_flags[k:k + n] & 1) == 1)
+        assert np.array_equal(seen, (c.compactor_flags[k:k + n] & 2) == 2)
+        assert np.array_equal(m, c.compactor_masks[k:k + n])
+        k += n
+
+
+def test_compactor_query_vs_oracle(cuda_ready):
+    """Uneven reads with repeats inside reads, against a partly filled graph."""
+    gens = [synth.genome(30_000, 60 + i) for i in range(3)]
+    rs = synth.uneven_reads(gens, [1, 2, 4], 400, 300, 1.0, 10, 4000, 0.03, 0.01, 0.01, 19)
+    rs += [np.tile(np.array([0, 1, 2, 3, 3, 1], np.uint8), 80)] * 3
+    pr = synth.list_to_packed(rs)
+    sizes = oracle.primes(4, 200_003)
+    st = oracle.Storage("byte", sizes)
+    g = graph_for("byte", True, 25, sizes)
+    first = synth.list_to_packed(rs[:150])
+    st.insert_reads(True, 25, first.packed, first.offsets)
+    g.insert_packed(first)
+    flags, masks = g.compactor_query_packed(pr)
+    want_f, want_m = st.compactor_reads(True, 25, pr.packed, pr.offsets)
+    assert np.array_equal(flags, want_f)
+    assert np.array_equal(masks, want_m)

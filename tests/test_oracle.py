@@ -91,6 +91,19 @@ def test_oracle_update_from_matches_golden(name):
     assert all(np.array_equal(a, b) for a, b in zip(merged, c.merged))
 
 
+@pytest.mark.parametrize("name", names())
+def test_oracle_compactor_matches_golden(name):
+    c = Case(name)
+    half = len(c.reads) // 2
+    st = oracle.Storage(c.storage, c.sizes)
+    packed, off, _ = oracle.pack_ascii(c.reads[:half])
+    st.insert_reads(c.canonical, c.K, packed, off)
+    packed, off, _ = oracle.pack_ascii(c.reads[half:])
+    flags, masks = st.compactor_reads(c.canonical, c.K, packed, off)
+    assert np.array_equal(flags, c.compactor_flags)
+    assert np.array_equal(masks, c.compactor_masks)
+
+
 def test_pack_policy():
     reads = ["ACGT", "acgtN", "aCgT", "", "ACGX", "TTTT"]
     packed, off, skipped = oracle.pack_ascii(reads)
