@@ -1,0 +1,147 @@
+// Device-side read packing: text reads already in device memory -> 2-bit
+// packed stream + base offsets, with the FASTX policy of goetia's DNA_SIMPLE
+// reader (FastxParser::next, include/goetia/parsing/readers.hh:150-219;
+// Alphabet::validate, include/goetia/sequences/alphabets.hh:41-56,107-130):
+// lowercase acgt are upper-cased, a read holding any other symbol or shorter
+// than min_length is dropped and counted.  Same output as gdbg_pack_reads.
+//
+//   k_pk_check  one warp per read: validity and kept length
+//   scans       kept bases and kept reads (exclusive, 32-bit)
+//   k_pk_write  one warp per kept read: each lane builds whole output words
+//               of the read and ORs them in (words at read boundaries are
+//               shared with the neighbour read); the read's end offset
+//   k_pk_final  counts and offsets[0]
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "gdbg_launch.h"
+#include "goetia_gb300.h"
+
+namespace gdbg {
+
+constexpr int PK_BLOCK = 256;
+
+__device__ __forceinline__ uint32_t pk_code(unsigned char c) {
+    const unsigned char lc = c | 0x20u;   // 'A'..'Z' -> 'a'..'z'; leaves other symbols non-letters
+    return lc == 'a' ? 0u : lc == 'c' ? 1u : lc == 'g' ? 2u : lc == 't' ? 3u : 4u;
+}
+
+__global__ void __launch_bounds__(PK_BLOCK)
+k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ so, uint64_t n,
+           uint32_t min_len, uint32_t* __restrict__ klen, uint32_t* __restrict__ kflag,
+           uint32_t* err) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n_warps = (uint64_t)gridDim.x * PK_BLOCK / 32;
+    for (uint64_t r = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32; r < n; r += n_warps) {
+        const uint64_t a = so[r], b = so[r + 1];
+        bool ok = b >= a && b - a < (1ull << 31);
+        if (!ok && lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
+        const uint64_t L = ok ? b - a : 0;
+        for (uint64_t i = lane; i < L && ok; i += 32) ok = pk_code(seqs[a + i]) < 4u;
+        ok = __all_sync(0xFFFFFFFFu, ok);
+        const bool kept = ok && L >= min_len;
+        if (lane == 0) {
+            klen[r] = kept ? (uint32_t)L : 0u;
+            kflag[r] = kept ? 1u : 0u;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(PK_BLOCK)
+k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ so, uint64_t n,
+           const uint32_t* __restrict__ klen, const uint32_t* __restrict__ kflag,
+           const uint32_t* __restrict__ kbase, const uint32_t* __restrict__ kidx,
+           uint32_t* __restrict__ packed, uint64_t packed_words, uint64_t* __restrict__ offsets,
+           uint32_t* err) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n_warps = (uint64_t)gridDim.x * PK_BLOCK / 32;
+    for (uint64_t r = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32; r < n; r += n_warps) {
+        if (!kflag[r]) continue;   // kept reads include empty ones (min_length 0)
+        const uint64_t L = klen[r];
+        const uint64_t a = so[r], ob0 = kbase[r], ob1 = ob0 + L;
+        for (uint64_t w = ob0 / 16 + lane; w * 16 < ob1; w += 32) {
+            if (w >= packed_words) {
+                atomicOr(err, GDBG_ERR_BAD_OFFSETS);
+                break;
+            }
+            uint32_t v = 0;
+            for (uint32_t q = 0; q < 16; ++q) {
+                const uint64_t j = w * 16 + q;
+                if (j >= ob0 && j < ob1) v |= pk_code(seqs[a + (j - ob0)]) << (2u * q);
+            }
+            if (v) atomicOr(packed + w, v);
+        }
+        if (lane == 0) offsets[(uint64_t)kidx[r] + 1] = ob1;
+    }
+}
+
+__global__ void k_pk_final(const uint32_t* klen, const uint32_t* kbase, const uint32_t* kflag,
+                           const uint32_t* kidx, uint64_t n, uint64_t* offsets, uint64_t* counts) {
+    offsets[0] = 0;
+    const uint64_t kept = n ? (uint64_t)kidx[n - 1] + kflag[n - 1] : 0;
+    counts[0] = kept;
+    counts[1] = n - kept;
+    counts[2] = n ? (uint64_t)kbase[n - 1] + klen[n - 1] : 0;
+}
+
+}  // namespace gdbg
+
+using namespace gdbg;
+
+extern "C" int gdbg_pack_reads_device(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
+                                      uint32_t min_length, uint32_t* packed, uint64_t packed_words,
+                                      uint64_t* offsets, uint64_t* n_kept, uint64_t* n_skipped,
+                                      void* stream) {
+    if (!seq_offsets || !offsets || !n_kept || !n_skipped || (!seqs && n_seqs) ||
+        (!packed && packed_words))
+        return report_error(GDBG_ERR_INVALID_ARG, "NULL argument");
+    if (n_seqs >= (1ull << 31)) return report_error(GDBG_ERR_INVALID_ARG, "too many reads for one call");
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint64_t parts = scan32_partials_needed(n_seqs + 1) + 1;
+    // scratch: klen, kflag, kbase, kidx (n + 1 each), scan partials, err, counts
+    const size_t bytes = (4 * (n_seqs + 1) + parts + 1) * sizeof(uint32_t) + 4 * sizeof(uint64_t);
+    void* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, bytes, st);
+    if (e != cudaSuccess) return report_error(GDBG_ERR_OOM, std::string("pack scratch: ") + cudaGetErrorString(e));
+    uint32_t* klen = (uint32_t*)scratch;
+    uint32_t* kflag = klen + (n_seqs + 1);
+    uint32_t* kbase = kflag + (n_seqs + 1);
+    uint32_t* kidx = kbase + (n_seqs + 1);
+    uint32_t* partials = kidx + (n_seqs + 1);
+    uint32_t* err = partials + parts;
+    uint64_t* counts = (uint64_t*)(((uintptr_t)(err + 1) + 7) & ~(uintptr_t)7);
+    auto done = [&](int rc, const std::string& msg) {
+        cudaFreeAsync(scratch, st);
+        cudaStreamSynchronize(st);
+        return rc == GDBG_OK ? rc : report_error(rc, msg);
+    };
+    if ((e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st)) != cudaSuccess ||
+        (packed_words && (e = cudaMemsetAsync(packed, 0, packed_words * sizeof(uint32_t), st)) != cudaSuccess))
+        return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    uint64_t grid = (n_seqs * 32 + PK_BLOCK - 1) / PK_BLOCK;
+    if (grid > 152 * 32) grid = 152 * 32;
+    if (grid == 0) grid = 1;
+    k_pk_check<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, seq_offsets, n_seqs,
+                                                    min_length, klen, kflag, err);
+    if (n_seqs) {
+        if ((e = launch_scan32(klen, kbase, n_seqs, partials, st)) != cudaSuccess ||
+            (e = launch_scan32(kflag, kidx, n_seqs, partials, st)) != cudaSuccess)
+            return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    k_pk_write<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, seq_offsets, n_seqs,
+                                                    klen, kflag, kbase, kidx, packed, packed_words,
+                                                    offsets, err);
+    k_pk_final<<<1, 1, 0, st>>>(klen, kbase, kflag, kidx, n_seqs, offsets, counts);
+    if ((e = cudaGetLastError()) != cudaSuccess) return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    uint64_t hc[3] = {0, 0, 0};
+    uint32_t herr = 0;
+    cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(scratch, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return report_error(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    if (herr) return report_error(GDBG_ERR_INVALID_ARG, "read offsets decrease, a read is 2^31 bases or longer, or packed is too small");
+    *n_kept = hc[0];
+    *n_skipped = hc[1];
+    return GDBG_OK;
+}

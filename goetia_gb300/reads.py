@@ -107,3 +107,23 @@ def concat(parts):
         offs.append(p.offsets[1:].astype(np.uint64) + np.uint64(B))
         B += nb
     return PackedReads(out.astype(np.uint32), np.concatenate(offs))
+
+
+def pack_reads_device(seqs, seq_offsets, min_length=0, stream=None):
+    """pack_reads on the GPU.  seqs: torch uint8 CUDA tensor of the reads'
+    bytes; seq_offsets: torch int64 CUDA tensor of n+1 byte offsets.
+    Returns (packed int32 tensor, offsets int64 tensor of n_kept+1, n_kept,
+    n_skipped), all on the same device."""
+    import torch
+    n = int(seq_offsets.numel()) - 1
+    dev = seqs.device
+    words = int(seqs.numel()) // 16 + 1
+    packed = torch.empty(words, dtype=torch.int32, device=dev)
+    offsets = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    kept, skipped = _lib.c_u64(), _lib.c_u64()
+    if stream is None:
+        stream = torch.cuda.current_stream(dev).cuda_stream
+    _lib.call("gdbg_pack_reads_device", seqs.data_ptr(), seq_offsets.data_ptr(), n, min_length,
+              packed.data_ptr(), words, offsets.data_ptr(), kept, skipped, stream or None)
+    k = int(kept.value)
+    return packed, offsets[:k + 1], k, int(skipped.value)

@@ -165,6 +165,15 @@ int gdbg_neighbor_masks(gdbg_graph* g, const char* seq, uint64_t len, uint8_t* m
 int gdbg_pack_reads(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
                     uint32_t min_length, uint32_t* packed, uint64_t packed_words,
                     uint64_t* offsets, uint64_t* n_kept, uint64_t* n_skipped);
+/* gdbg_pack_reads on the GPU: text reads and their n_seqs+1 byte offsets in
+ * device memory, packed / offsets outputs in device memory (packed_words
+ * words, zeroed here).  Kept bases in one call must stay below 2^32; a read
+ * must be shorter than 2^31 bases.  Runs on `stream` (NULL = legacy default)
+ * and returns when done, with the kept / skipped counts on the host. */
+int gdbg_pack_reads_device(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
+                           uint32_t min_length, uint32_t* packed, uint64_t packed_words,
+                           uint64_t* offsets, uint64_t* n_kept, uint64_t* n_skipped,
+                           void* stream);
 /* 2-bit codes (one byte each, values 0..3) to the packed stream. */
 int gdbg_pack_codes(const uint8_t* codes, uint64_t n, uint32_t* packed);
 

@@ -322,3 +322,36 @@ def test_compactor_query_vs_oracle(cuda_ready):
     want_f, want_m = st.compactor_reads(True, 25, pr.packed, pr.offsets)
     assert np.array_equal(flags, want_f)
     assert np.array_equal(masks, want_m)
+
+
+def test_pack_reads_device_matches_host_policy(cuda_ready):
+    """The GPU packer keeps, drops and packs exactly like the host packer and
+    the oracle's FASTX policy: lowercase, N and other symbols, short reads,
+    empty reads, lengths around word boundaries."""
+    import torch
+    rng = np.random.default_rng(77)
+    seqs = []
+    for i in range(3000):
+        L = int(rng.integers(0, 300))
+        s = "".join(rng.choice(list("ACGTacgt"), L))
+        if i % 7 == 0 and L:
+            p = int(rng.integers(0, L))
+            s = s[:p] + rng.choice(list("NnXx-.")) + s[p + 1:]
+        seqs.append(s)
+    seqs += ["A" * 16, "C" * 17, "g" * 15, "", "ACGTN", "T" * 1000]
+    data = b"".join(s.encode() for s in seqs)
+    so = np.zeros(len(seqs) + 1, np.uint64)
+    so[1:] = np.cumsum([len(s) for s in seqs])
+    for min_len in (0, 50):
+        host = G.pack_reads(seqs, min_length=min_len)
+        d_seqs = torch.from_numpy(np.frombuffer(data, np.uint8).copy()).cuda()
+        d_so = torch.from_numpy(so.view(np.int64)).cuda()
+        packed, offsets, kept, skipped = G.reads.pack_reads_device(d_seqs, d_so, min_len)
+        torch.cuda.synchronize()
+        assert kept == host.n_reads and skipped == host.n_skipped
+        off = offsets.cpu().numpy().view(np.uint64)
+        assert np.array_equal(off, host.offsets)
+        nw = (int(off[-1]) + 15) // 16
+        assert np.array_equal(packed.cpu().numpy().view(np.uint32)[:nw], host.packed[:nw])
+        p2, o2, sk = oracle.pack_ascii(seqs, min_len)
+        assert np.array_equal(o2, host.offsets) and sk == skipped
