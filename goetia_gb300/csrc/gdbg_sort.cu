@@ -7,8 +7,14 @@ namespace gdbg {
 cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
                            const TableParams& tp, const SortParams& sp, uint64_t* rout) {
     if (sp.nseg1 == 0) return cudaSuccess;
-    if (canonical) k_sp_emit<true><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
-    else k_sp_emit<false><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+    const bool t4 = sp.n_tables == 4;
+    if (canonical) {
+        if (t4) k_sp_emit<true, 4><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+        else k_sp_emit<true, 0><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+    } else {
+        if (t4) k_sp_emit<false, 4><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+        else k_sp_emit<false, 0><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+    }
     return cudaGetLastError();
 }
 

@@ -94,10 +94,10 @@ constexpr uint32_t SP_RUN = SP_SEGK / SP_EMIT_BLOCK;   // k-mers hashed by one t
 // partition passes do not keep it), so step j of every thread goes to the
 // segment slots j * (active threads) + t: each warp writes one contiguous
 // run per step.
-template <bool CANON>
+template <bool CANON, int NT>
 __global__ void __launch_bounds__(SP_EMIT_BLOCK)
 k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* __restrict__ rout) {
-    __shared__ uint64_t stage[SP_EMIT_BLOCK / 32][32 * BK_MAXNT];
+    __shared__ __align__(16) uint64_t stage[SP_EMIT_BLOCK / 32][32 * BK_MAXNT];
     __shared__ uint32_t hist[256];
     // roll terms by (out, in): fw ^= symk(out) ^ sym(in), rc ^= symk(3-in) ^ sym(3-out)
     __shared__ uint64_t roll_fw[16], roll_rc[16];
@@ -116,7 +116,7 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
     const uint64_t gs = (uint64_t)s * SP_SEGK;
     const uint32_t m = gs < nk ? (uint32_t)(nk - gs < SP_SEGK ? nk - gs : SP_SEGK) : 0u;
     const uint32_t F = m / SP_RUN, P = m % SP_RUN;   // full runs, length of the partial one
-    const uint32_t n = sp.n_tables;
+    const uint32_t n = NT > 0 ? (uint32_t)NT : sp.n_tables;
     const uint32_t my_len = tid < F ? SP_RUN : (tid == F ? P : 0u);
     uint64_t r = 0, kend = 0, fw = 0, rc = 0;
     BaseCursor cin, cout;
@@ -193,11 +193,12 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
         if (act) {
             const uint64_t h = hash_value<CANON>(fw, rc);
 #pragma unroll
-            for (int i = 0; i < BK_MAXNT; ++i) {
-                if (i < (int)n) {
-                    const uint64_t gc = sp.tbase[i] + fastmod(h, tp.p[i], tp.m[i]);
-                    stage[w][lane * n + i] = (gc << 32) | (uint32_t)g;
-                    atomicAdd(&hist[(uint32_t)(gc >> sp.fs) >> sp.hi_shift], 1u);
+            for (int i = 0; i < (NT > 0 ? NT : BK_MAXNT); ++i) {
+                if (NT > 0 || i < (int)n) {
+                    // global cells are below 2^32: 32-bit cell, bucket and digit
+                    const uint32_t gc = (uint32_t)sp.tbase[i] + (uint32_t)fastmod(h, tp.p[i], tp.m[i]);
+                    stage[w][lane * n + i] = ((uint64_t)gc << 32) | (uint32_t)g;
+                    atomicAdd(&hist[(gc >> sp.fs) >> sp.hi_shift], 1u);
                 }
             }
         }
@@ -206,7 +207,14 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
         const uint32_t wa = A > w * 32 ? (A - w * 32 < 32 ? A - w * 32 : 32u) : 0u;
         if (wa) {
             uint64_t* dst = rout + (gs + slot0 + w * 32) * n;
-            for (uint32_t k = lane; k < wa * n; k += 32) dst[k] = stage[w][k];
+            if (NT == 4) {
+                // 16-byte stores: a slot's 4 records are 32 bytes, 32-byte aligned
+                uint4* d4 = reinterpret_cast<uint4*>(dst);
+                const uint4* s4 = reinterpret_cast<const uint4*>(stage[w]);
+                for (uint32_t k = lane; k < wa * 2; k += 32) d4[k] = s4[k];
+            } else {
+                for (uint32_t k = lane; k < wa * n; k += 32) dst[k] = stage[w][k];
+            }
         }
         __syncwarp();
     }
