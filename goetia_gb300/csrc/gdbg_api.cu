@@ -259,13 +259,14 @@ int init_handle(gdbg_graph* g, int storage, int shifter, uint16_t K) {
     if (cudaStreamCreateWithFlags(&g->own_stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(GDBG_ERR_CUDA, "cudaStreamCreate failed");
     g->stream = g->own_stream;
-    if (cudaMalloc((void**)&g->d_err, sizeof(uint32_t)) != cudaSuccess ||
+    // d_err[0]: device status bits; d_err[1]: offset check of a host batch
+    if (cudaMalloc((void**)&g->d_err, 2 * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc((void**)&g->d_epoch, sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc((void**)&g->d_bar, 2 * sizeof(unsigned int)) != cudaSuccess)
         return fail(GDBG_ERR_OOM, "counter allocation failed");
     cudaMemsetAsync(g->d_epoch, 0, sizeof(uint32_t), g->stream);
     cudaMemsetAsync(g->d_bar, 0, 2 * sizeof(unsigned int), g->stream);
-    cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
+    cudaMemsetAsync(g->d_err, 0, 2 * sizeof(uint32_t), g->stream);
     g->hp.K = K;
     for (int c = 0; c < 4; ++c) g->hp.tk[c] = host_rotl(HSYM[c], K % 64u);
     return GDBG_OK;
@@ -332,33 +333,46 @@ int check_device_status(gdbg_graph* g) {
 }
 
 // Per-read k-mer prefix + tile map for a device-resident batch.
-enum MapNeed { MAP_TILES = 1, MAP_TASKS = 2 };
+// MAP_FOR_INSERT: the maps the insert path chosen for the batch's total needs
+enum MapNeed { MAP_TILES = 1, MAP_TASKS = 2, MAP_FOR_INSERT = 4 };
+int insert_maps(const gdbg_graph* g, uint64_t n_total);
 
+// checked: the offsets came from a host batch and are validated by the prefix
+// kernel into their own status word; with hint UINT64_MAX that word comes back
+// with the total, so a bad batch fails before any table is touched.
 int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                   const uint64_t* offsets, uint64_t n_reads, uint64_t hint, cudaStream_t st,
-                  BatchView* view, int maps = MAP_TILES | MAP_TASKS) {
+                  BatchView* view, int maps = MAP_TILES | MAP_TASKS, bool checked = false) {
     GDBG_TRY(g->kofs.ensure(n_reads + 1));
     GDBG_TRY(g->tofs.ensure(n_reads + 1));
     GDBG_TRY(g->partials.ensure(2 * (n_reads / 1024 + 2)));
     int nl = 0;
     Stage stage_prep(g, "prepare", st);
+    uint32_t* perr = checked ? g->d_err + 1 : g->d_err;
+    if (checked) GDBG_CUDA(cudaMemsetAsync(perr, 0, sizeof(uint32_t), st));
     GDBG_CUDA(launch_kmer_prefix(offsets, n_reads, g->K, packed_words * 16ull, g->partials.p,
-                                 g->kofs.p, g->tofs.p, g->d_err, st, &nl));
+                                 g->kofs.p, g->tofs.p, perr, st, &nl));
     g->launches += nl;
     uint64_t total = hint, tasks = 0;
     if (total == UINT64_MAX) {
-        uint64_t tt[2];
+        uint64_t tt[3] = {0, 0, 0};
         GDBG_CUDA(cudaMemcpyAsync(&tt[0], g->kofs.p + n_reads, sizeof(uint64_t),
                                   cudaMemcpyDeviceToHost, st));
         GDBG_CUDA(cudaMemcpyAsync(&tt[1], g->tofs.p + n_reads, sizeof(uint64_t),
                                   cudaMemcpyDeviceToHost, st));
+        if (checked)
+            GDBG_CUDA(cudaMemcpyAsync(&tt[2], perr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         GDBG_CUDA(cudaStreamSynchronize(st));
+        if (tt[2])
+            return fail(GDBG_ERR_INVALID_ARG,
+                        "offsets must be non-decreasing and end within the packed stream");
         total = tt[0];
         tasks = tt[1];
     } else {
         // every read adds at most one partly filled task
         tasks = total / TASK_KMERS + std::min<uint64_t>(n_reads, total);
     }
+    if (maps & MAP_FOR_INSERT) maps = insert_maps(g, total);
     uint64_t tiles = (total + MAP_TILE - 1) / MAP_TILE;
     GDBG_TRY(g->tile_read.ensure(tiles + 1));
     GDBG_TRY(g->task_read.ensure(tasks + 1));
@@ -898,36 +912,16 @@ int run_masks(gdbg_graph* g, const BatchView& b, uint8_t* masks, cudaStream_t st
     return GDBG_OK;
 }
 
-uint64_t host_kmer_total(const uint64_t* off, uint64_t n, uint16_t K) {
-    uint64_t t = 0;
-    for (uint64_t r = 0; r < n; ++r) {
-        if (off[r + 1] < off[r]) return UINT64_MAX;
-        uint64_t L = off[r + 1] - off[r];
-        if (L >= K) t += L - K + 1;
-    }
-    return t;
-}
-
-int check_host_batch(const gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
-                     const uint64_t* offsets, uint64_t n_reads, uint64_t* total) {
-    if (!offsets || (n_reads && !packed && n_words))
-        return fail(GDBG_ERR_INVALID_ARG, "NULL batch buffers");
-    for (uint64_t r = 0; r < n_reads; ++r)
-        if (offsets[r + 1] < offsets[r]) return fail(GDBG_ERR_INVALID_ARG, "offsets must be non-decreasing");
-    if (n_reads && offsets[n_reads] > n_words * 16ull)
-        return fail(GDBG_ERR_INVALID_ARG, "offsets run past the packed stream");
-    *total = host_kmer_total(offsets, n_reads, g->K);
-    return GDBG_OK;
-}
-
 // Copy a host batch into the handle's staging buffers and prepare it.
-int insert_maps(const gdbg_graph* g, uint64_t n_total);
-
+// total: the batch's k-mer count when the offsets were built here, else
+// UINT64_MAX: the prefix kernel validates the caller's offsets (they must not
+// decrease nor run past the packed stream) and computes the total, which
+// comes back before anything else is launched.
 int stage_host_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                      const uint64_t* offsets, uint64_t n_reads, BatchView* view,
-                     bool for_insert = false) {
-    uint64_t total = 0;
-    GDBG_TRY(check_host_batch(g, packed, n_words, offsets, n_reads, &total));
+                     bool for_insert = false, uint64_t total = UINT64_MAX) {
+    if (!offsets || (n_reads && !packed && n_words))
+        return fail(GDBG_ERR_INVALID_ARG, "NULL batch buffers");
     GDBG_TRY(g->st_packed.ensure(n_words + 1));
     GDBG_TRY(g->st_offsets.ensure(n_reads + 1));
     if (n_words)
@@ -935,8 +929,10 @@ int stage_host_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                                   cudaMemcpyHostToDevice, g->stream));
     GDBG_CUDA(cudaMemcpyAsync(g->st_offsets.p, offsets, (n_reads + 1) * sizeof(uint64_t),
                               cudaMemcpyHostToDevice, g->stream));
+    const int maps = for_insert ? (total == UINT64_MAX ? MAP_FOR_INSERT : insert_maps(g, total))
+                                : (MAP_TILES | MAP_TASKS);
     return prepare_batch(g, g->st_packed.p, n_words, g->st_offsets.p, n_reads, total, g->stream,
-                         view, for_insert ? insert_maps(g, total) : (MAP_TILES | MAP_TASKS));
+                         view, maps, total == UINT64_MAX);
 }
 
 // Validate a string against DNA_SIMPLE and pack it as a one-read batch.
@@ -965,7 +961,8 @@ int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view,
     std::vector<uint32_t> packed;
     GDBG_TRY(pack_string(seq, len, packed));
     uint64_t off[2] = {0, len};
-    return stage_host_batch(g, packed.data(), packed.size(), off, 1, view, for_insert);
+    return stage_host_batch(g, packed.data(), packed.size(), off, 1, view, for_insert,
+                            len - g->K + 1);
 }
 
 }  // namespace

@@ -330,7 +330,8 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
     uint64_t* inbuf = sm;                       // SP_NBUF x SP_BUF
     uint64_t* stage = sm + SP_NBUF * SP_BUF;    // SP_TILE
     constexpr uint32_t MB = PASS2 ? SP_MAXBINS2 : 256u;
-    __shared__ uint32_t cnt[MB], lstart[MB], cursor[MB], gbase[MB];
+    __shared__ uint32_t cnt[MB], lstart[MB], cursor[MB], delta[MB];
+    __shared__ uint32_t wsum[SP_PART_BLOCK / 32];
     __shared__ __align__(8) uint64_t bars[SP_NBUF];
     __shared__ uint32_t rs_s, re_s, abort_s;
     const uint32_t tid = threadIdx.x;
@@ -370,9 +371,11 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
             cursor[d] = sp.off1[(uint64_t)d * sp.nseg1 + blockIdx.x];
     }
     const uint32_t n_tiles = (re - rs + SP_TILE - 1) / SP_TILE;
-    const uint32_t shift = PASS2 ? 0u : sp.hi_shift;
+    // digit of a record: (cell >> (fs + shift)) & mask
+    const uint32_t dshift = sp.fs + (PASS2 ? 0u : sp.hi_shift);
     const uint32_t mask = PASS2 ? sp.bins2 - 1 : 0xFFFFFFFFu;
-    const uint64_t n_recs = sp_records(sp);
+    const uint32_t n_recs = (uint32_t)sp_records(sp);
+    const uint32_t lane = tid & 31u, w = tid >> 5;
     // tile i covers records [rs + i*SP_TILE, ...); its copy starts at the
     // even index at or below, so the copy is 16-byte aligned and sized
     auto issue = [&](uint32_t i) {
@@ -383,15 +386,17 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
         mbar_expect(bar, (a1 - a0) * 8u);
         bulk_load(inbuf + (i % SP_NBUF) * SP_BUF, rin + a0, (a1 - a0) * 8u, bar);
     };
+    for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK) cnt[d] = 0;
     if (tid == 0)
         for (uint32_t i = 0; i < SP_NBUF && i < n_tiles; ++i) issue(i);
+    constexpr int IPT = SP_TILE / SP_PART_BLOCK;
     for (uint32_t i = 0; i < n_tiles; ++i) {
         const uint32_t ts = rs + i * SP_TILE;
         const uint32_t nt = re - ts < SP_TILE ? re - ts : SP_TILE;
-        const uint32_t off = ts & 1u;
-        const uint64_t* src = inbuf + (i % SP_NBUF) * SP_BUF + off;
-        for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK) cnt[d] = 0;
+        const uint64_t* src = inbuf + (i % SP_NBUF) * SP_BUF + (ts & 1u);
         if (!mbar_wait(&bars[i % SP_NBUF], (i / SP_NBUF) & 1u)) atomicExch(&abort_s, 1u);
+        // also orders the previous tile's reads of stage / delta before this
+        // tile's writes
         __syncthreads();
         if (abort_s) {
             // give the copies in flight a last bounded wait, then leave
@@ -402,14 +407,19 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
             }
             return;
         }
-        constexpr int IPT = SP_TILE / SP_PART_BLOCK;
+        // ranks inside the tile: all loads first, then all atomics
         uint64_t r[IPT];
-        uint32_t pos[IPT];
+        uint32_t dg[IPT], pos[IPT];
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             const uint32_t k = j * SP_PART_BLOCK + tid;
             r[j] = k < nt ? src[k] : 0;
-            pos[j] = k < nt ? atomicAdd(&cnt[(sp_bucket(r[j], sp.fs) >> shift) & mask], 1u) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) {
+            const uint32_t k = j * SP_PART_BLOCK + tid;
+            dg[j] = ((uint32_t)(r[j] >> 32) >> dshift) & mask;
+            pos[j] = k < nt ? atomicAdd(&cnt[dg[j]], 1u) : 0u;
         }
         __syncthreads();
         // buffer consumed: refill it with tile i + SP_NBUF
@@ -417,49 +427,44 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(i + SP_NBUF);
         }
-        // tile-local bin starts (exclusive scan by warp 0) and global bases
-        if (tid < 32) {
-            constexpr uint32_t PER = MB / 32;
-            uint32_t v[PER], sum = 0;
+        // tile-local bin starts: one bin per thread, warp scans, then the
+        // warps' totals; delta[d] = global base - local start
+        const uint32_t c = tid < bins ? cnt[tid] : 0u;
+        if (tid < bins) cnt[tid] = 0;
+        uint32_t inc = c;
 #pragma unroll
-            for (uint32_t q = 0; q < PER; ++q) {
-                const uint32_t d = tid * PER + q;
-                v[q] = d < bins ? cnt[d] : 0u;
-                sum += v[q];
-            }
-            uint32_t inc = sum;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-                if (tid >= (uint32_t)o) inc += y;
-            }
-            uint32_t run = inc - sum;
-#pragma unroll
-            for (uint32_t q = 0; q < PER; ++q) {
-                const uint32_t d = tid * PER + q;
-                if (d < bins) lstart[d] = run;
-                run += v[q];
-            }
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= (uint32_t)o) inc += y;
         }
-        for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK) {
-            gbase[d] = cursor[d];
-            cursor[d] += cnt[d];
+        if (lane == 31) wsum[w] = inc;
+        __syncthreads();
+        if (tid < bins) {
+            uint32_t pre = 0;
+            for (uint32_t q = 0; q < w; ++q) pre += wsum[q];
+            const uint32_t ex = pre + inc - c;
+            lstart[tid] = ex;
+            delta[tid] = cursor[tid] - ex;
+            cursor[tid] += c;
         }
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < IPT; ++j) {
             const uint32_t k = j * SP_PART_BLOCK + tid;
-            if (k < nt) stage[lstart[(sp_bucket(r[j], sp.fs) >> shift) & mask] + pos[j]] = r[j];
+            if (k < nt) stage[lstart[dg[j]] + pos[j]] = r[j];
         }
         __syncthreads();
-        for (uint32_t k = tid; k < nt; k += SP_PART_BLOCK) {
-            const uint64_t v = stage[k];
-            const uint32_t d = (sp_bucket(v, sp.fs) >> shift) & mask;
-            const uint64_t p = (uint64_t)gbase[d] + (k - lstart[d]);
-            if (p < n_recs) rout[p] = v;
-            else atomicOr(sp.err, GDBG_ERR_PARTITION);
+        // runs of equal digits go out contiguously
+#pragma unroll
+        for (int j = 0; j < IPT; ++j) {
+            const uint32_t k = j * SP_PART_BLOCK + tid;
+            if (k < nt) {
+                const uint64_t v = stage[k];
+                const uint32_t p = delta[((uint32_t)(v >> 32) >> dshift) & mask] + k;
+                if (p < n_recs) rout[p] = v;
+                else atomicOr(sp.err, GDBG_ERR_PARTITION);
+            }
         }
-        __syncthreads();
     }
 }
 

@@ -258,6 +258,36 @@ def test_device_offsets_validated(cuda_ready):
     assert g.insert_sequence("ACGT" * 10) == 10
 
 
+@pytest.mark.parametrize("path", ["bucketed", "windowed"])
+def test_host_offsets_rejected_before_tables_change(cuda_ready, path):
+    """A host batch whose offsets decrease or run past the packed stream is
+    refused with INVALID_ARG by the device's offset check, before any table
+    changes; a valid batch on the same handle then inserts as usual."""
+    g = graph_for("byte", True, 21, oracle.primes(4, 100003))
+    g.set_insert_path(path)
+    rows = synth.sample_reads(synth.genome(20_000, 3), 200, 100, 0.01, 4)
+    pr = synth.rows_to_packed(rows)
+    g.insert_packed(pr)
+    before = [t.copy() for t in g.get_raw()]
+    stats = (g.n_unique(), g.n_occupied())
+    bad = [pr.offsets.copy(), pr.offsets.copy()]
+    bad[0][50], bad[0][51] = bad[0][51], bad[0][50]        # decreasing pair
+    bad[1][-1] = pr.packed.size * 16 + 1                     # past the stream
+    for off in bad:
+        with pytest.raises(G.GoetiaError) as e:
+            g.insert_packed(G.PackedReads(pr.packed, off))
+        assert e.value.code == G._lib.ERR_INVALID_ARG
+        for a, t in zip(g.get_raw(), before):
+            assert np.array_equal(a, t)
+        assert (g.n_unique(), g.n_occupied()) == stats
+    assert g.device_status() == 0
+    ref = oracle.Storage("byte", oracle.primes(4, 100003))
+    ref.insert_reads(True, 21, pr.packed, pr.offsets)
+    pr2 = synth.rows_to_packed(synth.sample_reads(synth.genome(20_000, 3), 100, 90, 0.01, 5))
+    _, want = ref.insert_reads(True, 21, pr2.packed, pr2.offsets)
+    assert np.array_equal(g.insert_packed(pr2), want)
+
+
 @pytest.mark.parametrize("kind", ["bit", "byte", "nibble"])
 def test_segmented_dense_buckets(cuda_ready, kind):
     """Tables of one or two buckets each receiving far more distinct zero
