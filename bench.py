@@ -51,6 +51,20 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", 0))
 
 
+def over_ranks(dt, kmers, dev, world):
+    """Whole-job figures of the replicas: the slowest rank's time and the
+    k-mers all ranks inserted (each rank inserts its own batches)."""
+    if world <= 1:
+        return dt, float(kmers)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([dt], dtype=torch.float64, device=dev)
+    k = torch.tensor([float(kmers)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(k)
+    return float(t.item()), float(k.item())
+
+
 def make_batches(n_batches, reads_per_step, seed0=4):
     """Seeded batches of packed reads (N-reads already dropped)."""
     from goetia_gb300 import synth
@@ -448,15 +462,7 @@ def run_gpu(args):
     torch.cuda.synchronize(dev)
     stages = g_prof.stage_times()
     del g_prof
-    if world > 1:
-        t = torch.tensor([dt], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
-        kt = torch.tensor([kmers], device=dev, dtype=torch.float64)
-        dist.all_reduce(kt)
-        total_kmers = float(kt.item())
-    else:
-        total_kmers = float(kmers)
+    dt, total_kmers = over_ranks(dt, kmers, dev, world)
     value = total_kmers / dt
 
     # e2e: host-buffer C-ABI call on a fresh graph, copies inside the timed region
@@ -494,11 +500,8 @@ def run_gpu(args):
         d2h += c
     torch.cuda.synchronize(dev)
     e2e_dt = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_dt], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_dt = float(t.item())
-    e2e_value = e2e_kmers * world / e2e_dt
+    e2e_dt, e2e_total = over_ranks(e2e_dt, e2e_kmers, dev, world)
+    e2e_value = e2e_total / e2e_dt
     # parity spot check of the two arms: same batches into fresh tables
     same = bool(np.array_equal(pinned[-1][1][:batches[-1].n_reads],
                                d_batches[-1][2].cpu().numpy().view(np.uint64)))
