@@ -492,27 +492,41 @@ __global__ void k_sp_starts(SortParams sp, uint32_t* __restrict__ start) {
 // ---- 4. order-independent apply -------------------------------------------
 
 constexpr uint32_t SP_RBUF = 4608;   // records of a bucket staged in shared memory at once
-constexpr uint16_t SP_NOSLOT = 0xFFFFu;
 
 __device__ __forceinline__ uint32_t sp_slot(uint32_t co) {
     return (co * 0x9E3779B1u) >> (32 - 12);   // SP_MAPCAP = 2^12
 }
 
 // Shared-memory layout of k_sp_apply (byte offsets): region words (padded
-// to 16 bytes), fresh-cell map, record buffer (+2 alignment slack), the map
-// slot of each staged record (or SP_NOSLOT), dirty sector bits.
+// to 16 bytes), fresh-cell map, record buffer (+2 alignment slack), dirty
+// sector bits.
 struct ApplyLayout {
-    uint32_t map_off, rec_off, slot_off, dirty_off, total;
+    uint32_t map_off, rec_off, dirty_off, total;
 };
 __host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words) {
     const uint32_t region_b = ((region_words + 3u) & ~3u) * 4u;
     const uint32_t map_b = SP_MAPCAP * 8u;
     const uint32_t rec_b = (SP_RBUF + 2u) * 8u;
-    const uint32_t slot_b = SP_RBUF * 2u;
     const uint32_t dirty_b = (((region_words + 7u) / 8u + 31u) / 32u) * 4u;
     return ApplyLayout{region_b, region_b + map_b, region_b + map_b + rec_b,
-                       region_b + map_b + rec_b + slot_b,
-                       region_b + map_b + rec_b + slot_b + dirty_b};
+                       region_b + map_b + rec_b + dirty_b};
+}
+
+// After pass 1 the map holds every cell of the range that was zero before
+// the batch, with the minimum ordinal of its records: that k-mer is the
+// cell's first toucher, so it is new.  Each thread reads its own slots.
+__device__ __forceinline__ void sp_map_winners(const uint64_t* map, const SortParams& sp, int ti,
+                                               uint32_t* __restrict__ new_bits,
+                                               unsigned long long& occ) {
+    for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) {
+        const uint64_t e = map[k];
+        if (e == SP_EMPTY) continue;
+        const uint32_t g = (uint32_t)(e >> 32);
+        if (g < sp.kmer_cap) {
+            atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
+            if (ti == 0) ++occ;
+        }
+    }
 }
 
 // Map insert of a zero cell with ordinal g: the slot index, or SP_MAPCAP when
@@ -584,7 +598,6 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     uint32_t* region = reinterpret_cast<uint32_t*>(sbytes);
     uint64_t* map = reinterpret_cast<uint64_t*>(sbytes + L.map_off);
     uint64_t* rbuf = reinterpret_cast<uint64_t*>(sbytes + L.rec_off);
-    uint16_t* rslot = reinterpret_cast<uint16_t*>(sbytes + L.slot_off);
     uint32_t* dirty = reinterpret_cast<uint32_t*>(sbytes + L.dirty_off);
     const uint64_t c0 = (uint64_t)(bk - sp.bbase[ti]) << sp.fs;
     const uint64_t w0 = c0 / cells_per_word<STORAGE>();
@@ -646,15 +659,12 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
             const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
             uint32_t word, shift;
             region_cell<STORAGE>(co, word, shift);
-            uint16_t sl16 = SP_NOSLOT;
             if (cell_value<STORAGE>(region[word], shift) == 0) {
                 bool created;
                 const uint32_t sl = sp_map_insert(map, co, (uint32_t)rec, &created);
                 inserted += created;
                 lost |= sl >= SP_MAPCAP;
-                sl16 = sl < SP_MAPCAP ? (uint16_t)sl : SP_NOSLOT;
             }
-            rslot[k] = sl16;
         }
         inserted = __reduce_add_sync(0xFFFFFFFFu, inserted);
         if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
@@ -664,7 +674,6 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
             for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
                 const uint64_t rec = src[k];
                 const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
-                const uint32_t g = (uint32_t)rec;
                 uint32_t word, shift;
                 region_cell<STORAGE>(co, word, shift);
                 const bool changed = sp_increment<STORAGE>(region, word, shift);
@@ -672,12 +681,8 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                     const uint32_t sec = word >> 3;
                     atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
                 }
-                const uint16_t sl = rslot[k];
-                if (sl != SP_NOSLOT && (uint32_t)(map[sl] >> 32) == g && g < sp.kmer_cap) {
-                    atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
-                    if (ti == 0) ++occ;
-                }
             }
+            sp_map_winners(map, sp, ti, new_bits, occ);
             done = true;
         }
         __syncthreads();
@@ -743,8 +748,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                 __syncthreads();
                 continue;
             }
-            const bool any_fresh = n_fresh != 0;
-            // pass 2: apply every record of the range; the map's minimum is new
+            // pass 2: apply every record of the range; the map's minima are new
             for (uint32_t c = 0; c < n_chunks && ok; ++c) {
                 ok = need_chunk(c);
                 if (!ok) break;
@@ -755,7 +759,6 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                     const uint64_t rec = src[k];
                     const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
                     if (co < lo || co >= hi) continue;
-                    const uint32_t g = (uint32_t)rec;
                     uint32_t word, shift;
                     region_cell<STORAGE>(co, word, shift);
                     const bool changed = sp_increment<STORAGE>(region, word, shift);
@@ -763,24 +766,10 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                         const uint32_t sec = word >> 3;
                         atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
                     }
-                    if (!any_fresh) continue;
-                    // was the cell zero before the batch, and is this its first toucher?
-                    uint32_t sl = sp_slot(co);
-                    for (uint32_t it = 0; it < SP_MAPCAP; ++it) {
-                        const uint64_t cur = map[sl];
-                        if (cur == SP_EMPTY) break;
-                        if ((uint32_t)cur == co) {
-                            if ((uint32_t)(cur >> 32) == g && g < sp.kmer_cap) {
-                                atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
-                                if (ti == 0) ++occ;
-                            }
-                            break;
-                        }
-                        sl = (sl + 1) & (SP_MAPCAP - 1);
-                    }
                 }
             }
             if (!ok) break;
+            sp_map_winners(map, sp, ti, new_bits, occ);
             __syncthreads();
             lo = hi;
         }
