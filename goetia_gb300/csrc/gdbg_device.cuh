@@ -50,6 +50,14 @@ __device__ __forceinline__ uint64_t fastmod(uint64_t h, uint64_t p, uint64_t m) 
     uint64_t r = h - q * p;
     return r >= p ? r - p : r;
 }
+// fastmod for p < 2^31.  The Barrett quotient is floor(h/p) or one less, so
+// the remainder before the correction is below 2p <= 2^32 and its low 32
+// bits are exact: one 32-bit multiply-subtract and an unsigned min.
+__device__ __forceinline__ uint32_t fastmod_small(uint64_t h, uint32_t p, uint64_t m) {
+    const uint64_t q = __umul64hi(h, m);
+    const uint32_t r = (uint32_t)h - (uint32_t)q * p;
+    return min(r, r - p);
+}
 
 // ---- 2-bit packed base stream ---------------------------------------------
 // base j lives in bits 2*(j%16) of word j/16.

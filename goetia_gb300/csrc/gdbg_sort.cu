@@ -8,13 +8,18 @@ cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, 
                            const TableParams& tp, const SortParams& sp, uint64_t* rout) {
     if (sp.nseg1 == 0) return cudaSuccess;
     const bool t4 = sp.n_tables == 4;
+    bool small = true;   // every table below 2^31 cells: 32-bit remainders
+    for (int i = 0; i < tp.n; ++i) small = small && tp.p[i] < (1ull << 31);
+    const unsigned g = sp.nseg1;
+#define GDBG_EMIT(C, N, S) k_sp_emit<C, N, S><<<g, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout)
     if (canonical) {
-        if (t4) k_sp_emit<true, 4><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
-        else k_sp_emit<true, 0><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+        if (t4) small ? GDBG_EMIT(true, 4, true) : GDBG_EMIT(true, 4, false);
+        else small ? GDBG_EMIT(true, 0, true) : GDBG_EMIT(true, 0, false);
     } else {
-        if (t4) k_sp_emit<false, 4><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
-        else k_sp_emit<false, 0><<<sp.nseg1, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout);
+        if (t4) small ? GDBG_EMIT(false, 4, true) : GDBG_EMIT(false, 4, false);
+        else small ? GDBG_EMIT(false, 0, true) : GDBG_EMIT(false, 0, false);
     }
+#undef GDBG_EMIT
     return cudaGetLastError();
 }
 

@@ -94,10 +94,10 @@ constexpr uint32_t SP_RUN = SP_SEGK / SP_EMIT_BLOCK;   // k-mers hashed by one t
 // partition passes do not keep it), so step j of every thread goes to the
 // segment slots j * (active threads) + t: each warp writes one contiguous
 // run per step.
-template <bool CANON, int NT>
+template <bool CANON, int NT, bool SMALLP>
 __global__ void __launch_bounds__(SP_EMIT_BLOCK)
 k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* __restrict__ rout) {
-    __shared__ __align__(16) uint64_t stage[SP_EMIT_BLOCK / 32][32 * BK_MAXNT];
+    __shared__ __align__(16) uint64_t stage[NT == 4 ? 1 : SP_EMIT_BLOCK / 32][32 * BK_MAXNT];
     __shared__ uint32_t hist[256];
     // roll terms by (out, in): fw ^= symk(out) ^ sym(in), rc ^= symk(3-in) ^ sym(3-out)
     __shared__ uint64_t roll_fw[16], roll_rc[16];
@@ -187,36 +187,50 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
                 cout.init(b.packed, pb);
             }
         }
-        // slots of step j: threads active at step j, in thread order
+        // slots of step j: threads active at step j, in thread order (the
+        // active threads are 0 .. A-1, so thread t takes slot slot0 + t)
         const uint32_t A = j < P ? F + 1 : F;
         const uint32_t slot0 = j < P ? j * (F + 1) : P * (F + 1) + (j - P) * F;
-        if (act) {
-            const uint64_t h = hash_value<CANON>(fw, rc);
+        if (NT == 4) {
+            if (act) {
+                const uint64_t h = hash_value<CANON>(fw, rc);
+                // global cells are below 2^32: 32-bit cell, bucket and digit
+                uint32_t gc[4];
 #pragma unroll
-            for (int i = 0; i < (NT > 0 ? NT : BK_MAXNT); ++i) {
-                if (NT > 0 || i < (int)n) {
-                    // global cells are below 2^32: 32-bit cell, bucket and digit
-                    const uint32_t gc = (uint32_t)sp.tbase[i] + (uint32_t)fastmod(h, tp.p[i], tp.m[i]);
-                    stage[w][lane * n + i] = ((uint64_t)gc << 32) | (uint32_t)g;
-                    atomicAdd(&hist[(gc >> sp.fs) >> sp.hi_shift], 1u);
+                for (int i = 0; i < 4; ++i) {
+                    gc[i] = (uint32_t)sp.tbase[i] + (SMALLP ? fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
+                                                            : (uint32_t)fastmod(h, tp.p[i], tp.m[i]));
+                    atomicAdd(&hist[(gc[i] >> sp.fs) >> sp.hi_shift], 1u);
+                }
+                // the slot's 4 records, (cell << 32) | ordinal, as two 16-byte
+                // stores; consecutive threads write consecutive 32-byte slots
+                const uint32_t gl = (uint32_t)g;
+                uint4* d4 = reinterpret_cast<uint4*>(rout + (gs + slot0 + tid) * 4u);
+                d4[0] = make_uint4(gl, gc[0], gl, gc[1]);
+                d4[1] = make_uint4(gl, gc[2], gl, gc[3]);
+            }
+        } else {
+            if (act) {
+                const uint64_t h = hash_value<CANON>(fw, rc);
+#pragma unroll
+                for (int i = 0; i < BK_MAXNT; ++i) {
+                    if (i < (int)n) {
+                        const uint32_t gc = (uint32_t)sp.tbase[i] +
+                                            (SMALLP ? fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
+                                                    : (uint32_t)fastmod(h, tp.p[i], tp.m[i]));
+                        stage[w][lane * n + i] = ((uint64_t)gc << 32) | (uint32_t)g;
+                        atomicAdd(&hist[(gc >> sp.fs) >> sp.hi_shift], 1u);
+                    }
                 }
             }
-        }
-        __syncwarp();
-        // the warp's active lanes are a prefix (threads 0 .. A-1 are active)
-        const uint32_t wa = A > w * 32 ? (A - w * 32 < 32 ? A - w * 32 : 32u) : 0u;
-        if (wa) {
-            uint64_t* dst = rout + (gs + slot0 + w * 32) * n;
-            if (NT == 4) {
-                // 16-byte stores: a slot's 4 records are 32 bytes, 32-byte aligned
-                uint4* d4 = reinterpret_cast<uint4*>(dst);
-                const uint4* s4 = reinterpret_cast<const uint4*>(stage[w]);
-                for (uint32_t k = lane; k < wa * 2; k += 32) d4[k] = s4[k];
-            } else {
+            __syncwarp();
+            const uint32_t wa = A > w * 32 ? (A - w * 32 < 32 ? A - w * 32 : 32u) : 0u;
+            if (wa) {
+                uint64_t* dst = rout + (gs + slot0 + w * 32) * n;
                 for (uint32_t k = lane; k < wa * n; k += 32) dst[k] = stage[w][k];
             }
+            __syncwarp();
         }
-        __syncwarp();
     }
     __syncthreads();
     for (uint32_t k = tid; k < sp.bins1; k += SP_EMIT_BLOCK)
