@@ -334,7 +334,8 @@ k_hashes(BatchView b, HashParams hp, uint64_t* __restrict__ values, uint64_t* __
 // neighbour masks: the 4 left and 4 right extensions of every k-mer
 // (hashextender.hh:352-396), each present iff every table cell is non-zero
 // (query() != 0, unitig_walker.hh:361-372).
-template <int STORAGE, bool CANON, int NT>
+// SMALLP: every table is below 2^31 cells (32-bit remainders).
+template <int STORAGE, bool CANON, int NT, bool SMALLP = false>
 __device__ __forceinline__ bool present(const TableParams& tp, uint64_t h) {
     const int n = NT > 0 ? NT : tp.n;
     bool ok = true;
@@ -342,7 +343,8 @@ __device__ __forceinline__ bool present(const TableParams& tp, uint64_t h) {
         uint32_t word[NT > 0 ? NT : 1], shift[NT > 0 ? NT : 1];
 #pragma unroll
         for (int i = 0; i < (NT > 0 ? NT : 1); ++i) {
-            Cell c = cell_of<STORAGE>(tp, i, fastmod(h, tp.p[i], tp.m[i]));
+            Cell c = cell_of<STORAGE>(tp, i, SMALLP ? (uint64_t)fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
+                                                    : fastmod(h, tp.p[i], tp.m[i]));
             shift[i] = c.shift;
             word[i] = __ldcg(c.word);
         }
@@ -358,7 +360,7 @@ __device__ __forceinline__ bool present(const TableParams& tp, uint64_t h) {
     return ok;
 }
 
-template <int STORAGE, bool CANON, int H, int NT>
+template <int STORAGE, bool CANON, int H, int NT, bool SMALLP>
 __global__ void __launch_bounds__(BLOCK)
 k_masks(BatchView b, HashParams hp, TableParams tp, uint8_t* __restrict__ masks) {
     const uint64_t tid = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
@@ -383,7 +385,7 @@ k_masks(BatchView b, HashParams hp, TableParams tp, uint8_t* __restrict__ masks)
         uint32_t m = 0;
 #pragma unroll
         for (int k = 0; k < 8; ++k)
-            if (present<STORAGE, CANON, NT>(tp, nh[k])) m |= 1u << k;
+            if (present<STORAGE, CANON, NT, SMALLP>(tp, nh[k])) m |= 1u << k;
         masks[g0 + j] = (uint8_t)m;
     }
 }

@@ -80,7 +80,10 @@ cudaError_t masks_one(cudaStream_t st, const BatchView& b, const HashParams& hp,
     constexpr int H = 2;
     uint64_t n_threads = (b.n_kmers + H - 1) / H;
     if (n_threads == 0) return cudaSuccess;
-    k_masks<ST, C, H, NT><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hp, tp, masks);
+    bool small = NT == 4;   // the generic table count keeps 64-bit remainders
+    for (int i = 0; i < tp.n; ++i) small = small && tp.p[i] < (1ull << 31);
+    if (small) k_masks<ST, C, H, NT, true><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hp, tp, masks);
+    else k_masks<ST, C, H, NT, false><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hp, tp, masks);
     return cudaGetLastError();
 }
 
