@@ -137,6 +137,18 @@ struct gdbg_graph {
     // batch scratch
     DevBuf<uint64_t> kofs, tofs, partials;
     DevBuf<uint32_t> tile_read, task_read;
+    // one-sequence calls: the read, its prefix and its maps built on the host
+    // in one pinned block and moved by one copy; small results come back
+    // through the pinned ret block
+    uint8_t* h_single = nullptr;
+    size_t h_single_cap = 0;
+    DevBuf<uint8_t> d_single;
+    cudaEvent_t single_done = nullptr;   // the last copy out of h_single
+    uint64_t* single_nnew = nullptr;     // device n_new slot of the staged read
+    struct Ret {
+        uint32_t err, pad;
+        uint64_t v[7];
+    }* h_ret = nullptr;
     // staging for host-pointer calls
     DevBuf<uint32_t> st_packed;
     DevBuf<uint64_t> st_offsets, st_out64, st_out64b, st_out64c;
@@ -267,6 +279,9 @@ int init_handle(gdbg_graph* g, int storage, int shifter, uint16_t K) {
     cudaMemsetAsync(g->d_epoch, 0, sizeof(uint32_t), g->stream);
     cudaMemsetAsync(g->d_bar, 0, 2 * sizeof(unsigned int), g->stream);
     cudaMemsetAsync(g->d_err, 0, 2 * sizeof(uint32_t), g->stream);
+    if (cudaHostAlloc((void**)&g->h_ret, sizeof(gdbg_graph::Ret), cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g->single_done, cudaEventDisableTiming) != cudaSuccess)
+        return fail(GDBG_ERR_OOM, "pinned status allocation failed");
     g->hp.K = K;
     for (int c = 0; c < 4; ++c) g->hp.tk[c] = host_rotl(HSYM[c], K % 64u);
     return GDBG_OK;
@@ -318,9 +333,10 @@ int make_graph(int storage, int shifter, uint16_t K, const uint64_t* sizes, uint
 }
 
 int check_device_status(gdbg_graph* g) {
-    uint32_t err = 0;
-    GDBG_CUDA(cudaMemcpyAsync(&err, g->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(&g->h_ret->err, g->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                              g->stream));
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
+    const uint32_t err = g->h_ret->err;
     if (err) {
         cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
         char buf[200];
@@ -834,6 +850,11 @@ int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64
         w.counters = g->ts->d_counters;
         w.err = g->d_err;
         uint64_t n_threads = (end - start + kpt - 1) / kpt;
+        if (n_threads <= (uint64_t)SMALL_BLOCK) {
+            // a small window: probe and commit in one block, one launch
+            GDBG_TRY(launch_pass(g, 2, s, n_threads, st, b, hashes, w));
+            continue;
+        }
         GDBG_TRY(launch_pass(g, 0, s, n_threads, st, b, hashes, w));
         GDBG_TRY(launch_pass(g, 1, s, n_threads, st, b, hashes, w));
     }
@@ -935,10 +956,36 @@ int stage_host_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                          view, maps, total == UINT64_MAX);
 }
 
-// Validate a string against DNA_SIMPLE and pack it as a one-read batch.
-int pack_string(const char* seq, uint64_t len, std::vector<uint32_t>& packed) {
-    if (!seq && len) return fail(GDBG_ERR_INVALID_ARG, "NULL sequence");
-    packed.assign(len / 16 + 1, 0u);
+// One read of len >= K bases as a batch: offsets {0, len}, k-mer prefix
+// {0, n}, task prefix {0, ceil(n / TASK_KMERS)}, zero tile and task maps, a
+// zero n_new slot and the packed bases, written into the pinned block and
+// copied to the device in one transfer (no prefix or map kernels).
+int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view) {
+    if (len < g->K) return fail(GDBG_ERR_SEQUENCE_LENGTH, "Sequence must have length >= K");
+    if (!seq) return fail(GDBG_ERR_INVALID_ARG, "NULL sequence");
+    const uint64_t nk = len - g->K + 1, words = len / 16 + 1;
+    const uint64_t tiles = (nk + MAP_TILE - 1) / MAP_TILE;
+    const uint64_t tasks = (nk + TASK_KMERS - 1) / TASK_KMERS;
+    auto up16 = [](uint64_t x) { return (x + 15) & ~uint64_t(15); };
+    const uint64_t o_tile = 64, o_task = up16(o_tile + (tiles + 1) * 4);
+    const uint64_t o_pack = up16(o_task + (tasks + 1) * 4), total = o_pack + words * 4;
+    // the previous call's copy out of the block has finished
+    GDBG_CUDA(cudaEventSynchronize(g->single_done));
+    if (g->h_single_cap < total) {
+        if (g->h_single) cudaFreeHost(g->h_single);
+        g->h_single = nullptr;
+        g->h_single_cap = 0;
+        const size_t want = std::max<size_t>(total + total / 4, 65536);
+        if (cudaHostAlloc((void**)&g->h_single, want, cudaHostAllocDefault) != cudaSuccess) {
+            g->h_single = nullptr;
+            return fail(GDBG_ERR_OOM, "pinned staging allocation failed");
+        }
+        g->h_single_cap = want;
+    }
+    GDBG_TRY(g->d_single.ensure(total));
+    uint8_t* h = g->h_single;
+    uint32_t* packed = reinterpret_cast<uint32_t*>(h + o_pack);
+    std::memset(packed, 0, words * 4);
     for (uint64_t i = 0; i < len; ++i) {
         uint32_t c;
         switch (seq[i]) {
@@ -952,17 +999,31 @@ int pack_string(const char* seq, uint64_t len, std::vector<uint32_t>& packed) {
         }
         packed[i >> 4] |= c << ((i & 15u) << 1);
     }
+    uint64_t* hdr = reinterpret_cast<uint64_t*>(h);
+    hdr[0] = 0;        // offsets
+    hdr[1] = len;
+    hdr[2] = 0;        // k-mer prefix
+    hdr[3] = nk;
+    hdr[4] = 0;        // task prefix
+    hdr[5] = tasks;
+    hdr[6] = 0;        // n_new
+    hdr[7] = 0;
+    std::memset(h + o_tile, 0, o_pack - o_tile);
+    uint8_t* d = g->d_single.p;
+    GDBG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, g->stream));
+    GDBG_CUDA(cudaEventRecord(g->single_done, g->stream));
+    view->packed = reinterpret_cast<const uint32_t*>(d + o_pack);
+    view->offsets = reinterpret_cast<const uint64_t*>(d);
+    view->kofs = reinterpret_cast<const uint64_t*>(d + 16);
+    view->tile_read = reinterpret_cast<const uint32_t*>(d + o_tile);
+    view->n_reads = 1;
+    view->n_kmers = nk;
+    view->n_map_tiles = tiles;
+    view->tofs = reinterpret_cast<const uint64_t*>(d + 32);
+    view->task_read = reinterpret_cast<const uint32_t*>(d + o_task);
+    view->task_cap = tasks;
+    g->single_nnew = reinterpret_cast<uint64_t*>(d + 48);
     return GDBG_OK;
-}
-
-int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view,
-                 bool for_insert = false) {
-    if (len < g->K) return fail(GDBG_ERR_SEQUENCE_LENGTH, "Sequence must have length >= K");
-    std::vector<uint32_t> packed;
-    GDBG_TRY(pack_string(seq, len, packed));
-    uint64_t off[2] = {0, len};
-    return stage_host_batch(g, packed.data(), packed.size(), off, 1, view, for_insert,
-                            len - g->K + 1);
 }
 
 }  // namespace
@@ -1030,6 +1091,10 @@ int gdbg_destroy(gdbg_graph* g) {
     if (g->d_err) cudaFree(g->d_err);
     if (g->d_epoch) cudaFree(g->d_epoch);
     if (g->d_bar) cudaFree(g->d_bar);
+    if (g->h_single) cudaFreeHost(g->h_single);
+    if (g->h_ret) cudaFreeHost(g->h_ret);
+    if (g->single_done) cudaEventDestroy(g->single_done);
+    g->d_single.release();
     g->fresh.release(); g->words_seen.release(); g->claims.release();
     g->kofs.release(); g->tofs.release(); g->partials.release(); g->tile_read.release();
     g->task_read.release();
@@ -1443,15 +1508,13 @@ int gdbg_insert_sequence(gdbg_graph* g, const char* seq, uint64_t len, uint64_t*
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
     GDBG_TRY(set_device(g));
     BatchView b;
-    GDBG_TRY(stage_string(g, seq, len, &b, true));
-    GDBG_TRY(g->st_out64.ensure(1));
-    GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, sizeof(uint64_t), g->stream));
-    GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, g->st_out64.p, g->stream));
-    uint64_t nn = 0;
-    GDBG_CUDA(cudaMemcpyAsync(&nn, g->st_out64.p, sizeof nn, cudaMemcpyDeviceToHost, g->stream));
+    GDBG_TRY(stage_string(g, seq, len, &b));
+    GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, g->single_nnew, g->stream));
+    GDBG_CUDA(cudaMemcpyAsync(&g->h_ret->v[0], g->single_nnew, sizeof(uint64_t),
+                              cudaMemcpyDeviceToHost, g->stream));
     GDBG_TRY(check_device_status(g));
     if (n_kmers) *n_kmers = len - g->K + 1;
-    if (n_new) *n_new = nn;
+    if (n_new) *n_new = g->h_ret->v[0];
     return GDBG_OK;
 }
 

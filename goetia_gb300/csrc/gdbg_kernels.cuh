@@ -139,17 +139,10 @@ __device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long 
 }
 
 // ---------------------------------------------------------------------------
-// probe pass
-template <int STORAGE, bool CANON, int H, int NT, bool FROM_HASHES>
-__global__ void __launch_bounds__(BLOCK)
-k_probe(BatchView b, const uint64_t* __restrict__ hashes, HashParams hp, TableParams tp,
-        WindowParams w) {
-    const uint64_t tid = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
-    const uint64_t g0 = w.start + tid * H;
-    Run<H> run;
-    if (FROM_HASHES) hash_run<H>(hashes, g0, w.end, run);
-    else make_run<CANON, H, false>(b, hp, g0, w.end, run);
-
+// probe pass over the run of k-mers g0 .. g0+H-1
+template <int STORAGE, int H, int NT>
+__device__ __forceinline__ void probe_run(const TableParams& tp, const WindowParams& w,
+                                          uint64_t g0, const Run<H>& run) {
     const int n = NT > 0 ? NT : tp.n;
     constexpr int TG = NT > 0 ? NT : 1;   // tables handled together
     uint32_t fresh[H];
@@ -199,18 +192,23 @@ k_probe(BatchView b, const uint64_t* __restrict__ hashes, HashParams hp, TablePa
     warp_add(w.counters + 1, occupied);
 }
 
-// ---------------------------------------------------------------------------
-// commit pass
 template <int STORAGE, bool CANON, int H, int NT, bool FROM_HASHES>
 __global__ void __launch_bounds__(BLOCK)
-k_commit(BatchView b, const uint64_t* __restrict__ hashes, HashParams hp, TableParams tp,
-         WindowParams w) {
+k_probe(BatchView b, const uint64_t* __restrict__ hashes, HashParams hp, TableParams tp,
+        WindowParams w) {
     const uint64_t tid = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
     const uint64_t g0 = w.start + tid * H;
     Run<H> run;
     if (FROM_HASHES) hash_run<H>(hashes, g0, w.end, run);
     else make_run<CANON, H, false>(b, hp, g0, w.end, run);
+    probe_run<STORAGE, H, NT>(tp, w, g0, run);
+}
 
+// ---------------------------------------------------------------------------
+// commit pass over the run of k-mers g0 .. g0+H-1
+template <int STORAGE, int H, int NT>
+__device__ __forceinline__ void commit_run(const TableParams& tp, const WindowParams& w,
+                                           uint64_t g0, const Run<H>& run) {
     const int n = NT > 0 ? NT : tp.n;
     constexpr int TG = NT > 0 ? NT : 1;
     uint32_t fresh[H];
@@ -262,6 +260,36 @@ k_commit(BatchView b, const uint64_t* __restrict__ hashes, HashParams hp, TableP
     }
     total = __popc(isnew);
     warp_add(w.counters + 0, total);
+}
+
+template <int STORAGE, bool CANON, int H, int NT, bool FROM_HASHES>
+__global__ void __launch_bounds__(BLOCK)
+k_commit(BatchView b, const uint64_t* __restrict__ hashes, HashParams hp, TableParams tp,
+         WindowParams w) {
+    const uint64_t tid = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
+    const uint64_t g0 = w.start + tid * H;
+    Run<H> run;
+    if (FROM_HASHES) hash_run<H>(hashes, g0, w.end, run);
+    else make_run<CANON, H, false>(b, hp, g0, w.end, run);
+    commit_run<STORAGE, H, NT>(tp, w, g0, run);
+}
+
+// ---------------------------------------------------------------------------
+// a window of at most SMALL_BLOCK * H k-mers in one block: the probe pass, a
+// block barrier (the probe's global writes are visible to the whole block
+// after it), then the commit pass on the same hashes -- one launch instead
+// of two for a single read or a small chunk of reads
+template <int STORAGE, bool CANON, int H, int NT, bool FROM_HASHES>
+__global__ void __launch_bounds__(SMALL_BLOCK, 1)
+k_insert_small(BatchView b, const uint64_t* __restrict__ hashes, HashParams hp, TableParams tp,
+               WindowParams w) {
+    const uint64_t g0 = w.start + (uint64_t)threadIdx.x * H;
+    Run<H> run;
+    if (FROM_HASHES) hash_run<H>(hashes, g0, w.end, run);
+    else make_run<CANON, H, false>(b, hp, g0, w.end, run);
+    probe_run<STORAGE, H, NT>(tp, w, g0, run);
+    __syncthreads();
+    commit_run<STORAGE, H, NT>(tp, w, g0, run);
 }
 
 // ---------------------------------------------------------------------------

@@ -18,8 +18,12 @@ cudaError_t insert_pass_one(int pass, uint64_t n_threads, cudaStream_t st, const
     if (n_threads == 0) return cudaSuccess;
     if (pass == 0)
         k_probe<ST, C, H, NT, FH><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hashes, hp, tp, w);
-    else
+    else if (pass == 1)
         k_commit<ST, C, H, NT, FH><<<grid_for(n_threads), BLOCK, 0, st>>>(b, hashes, hp, tp, w);
+    else if (n_threads <= (uint64_t)SMALL_BLOCK)
+        k_insert_small<ST, C, H, NT, FH><<<1, SMALL_BLOCK, 0, st>>>(b, hashes, hp, tp, w);
+    else
+        return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 

@@ -46,6 +46,7 @@ struct BatchView {
 
 constexpr uint64_t MAP_TILE = 1024;  // k-mers per entry of tile_read
 constexpr uint32_t TASK_KMERS = 32;  // k-mers per warp task (one lane each)
+constexpr int SMALL_BLOCK = 512;      // threads of the one-block insert of a small window
 
 // One window of the insert: k-mers [start, end) of the batch.
 struct WindowParams {
