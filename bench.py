@@ -347,6 +347,27 @@ def run_batched(args, check_reads=300):
                         "5 x 10 Mbp genomes 1:2:4:8:16, 8% errors; Nibble 4 x ~2^28 cells, K=21"}
 
 
+def run_profile_case(args):
+    """The small case the ncu captures run: dBG<ByteStorage, CanLemireShifter>,
+    K=31, 4 x ~2^28 cells (1 GiB of tables, 8x L2) through the segmented path,
+    three batches of 250,000 reads x 150 bp from a 20 Mbp seeded genome with
+    0.5% substitutions -- the benchmark's tables-to-batch ratio (36 table bytes
+    per k-mer) at a quarter of its size."""
+    import goetia_gb300 as G
+    from goetia_gb300 import build as gbuild, synth
+    gbuild.build()
+    gen = synth.genome(20_000_000, 3)
+    g = G.dBG[G.ByteStorage, G.CanLemireShifter].build(G.ByteStorage.build(1 << 28, 4), K)
+    g.set_insert_path("bucketed")
+    for b in range(3):
+        pr = synth.rows_to_packed(synth.sample_reads(gen, 250_000, READ_LEN, SUB_RATE, 10 + b))
+        n = g.insert_packed(pr)
+        print(json.dumps({"profile_case_batch": b, "kmers": pr.n_kmers(K),
+                          "new_kmers": int(n.sum())}), flush=True)
+    g.synchronize()
+    return 0
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -619,7 +640,11 @@ def main():
     ap.add_argument("--serve-scale", type=float, default=0.02)
     ap.add_argument("--serve-gap", type=float, default=0.002)
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run only the small insert case the ncu captures profile")
     args = ap.parse_args()
+    if args.profile_case:
+        return run_profile_case(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
