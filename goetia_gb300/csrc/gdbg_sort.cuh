@@ -600,6 +600,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     extern __shared__ __align__(128) unsigned char sbytes[];
     __shared__ uint32_t n_fresh, overflow, abort_s;
     __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t used[SP_MAPCAP / 32];   // map slots created by the fast path
     const uint32_t bk = blockIdx.x;
     const uint32_t rs = start[bk], re = start[bk + 1];
     if (rs >= re) return;
@@ -649,6 +650,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     if (track)
         for (uint32_t k = threadIdx.x; k < (region_sectors + 31) / 32; k += SP_APPLY_BLOCK) dirty[k] = 0;
     for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
+    for (uint32_t k = threadIdx.x; k < SP_MAPCAP / 32; k += SP_APPLY_BLOCK) used[k] = 0;
     __syncthreads();   // the barrier is initialised before anyone waits on it
     if (!mbar_wait(&bar, phase & 1u)) atomicExch(&abort_s, 1u);
     ++phase;
@@ -678,6 +680,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                 const uint32_t sl = sp_map_insert(map, co, (uint32_t)rec, &created);
                 inserted += created;
                 lost |= sl >= SP_MAPCAP;
+                if (created) atomicOr(&used[sl >> 5], 1u << (sl & 31u));
             }
         }
         inserted = __reduce_add_sync(0xFFFFFFFFu, inserted);
@@ -696,7 +699,17 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                     atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
                 }
             }
-            sp_map_winners(map, sp, ti, new_bits, occ);
+            // the first touchers: the created map slots, word by word of the
+            // used bits
+            for (uint32_t wd = threadIdx.x; wd < SP_MAPCAP / 32; wd += SP_APPLY_BLOCK) {
+                for (uint32_t m = used[wd]; m; m &= m - 1) {
+                    const uint32_t g = (uint32_t)(map[wd * 32 + __ffs(m) - 1] >> 32);
+                    if (g < sp.kmer_cap) {
+                        atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
+                        if (ti == 0) ++occ;
+                    }
+                }
+            }
             done = true;
         }
         __syncthreads();
