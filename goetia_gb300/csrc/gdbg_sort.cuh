@@ -88,6 +88,31 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
 
 constexpr uint32_t SP_RUN = SP_SEGK / SP_EMIT_BLOCK;   // k-mers hashed by one thread
 
+// Sequential 2-bit base reader.  A word is loaded only when a base of it is
+// read (a cursor placed at the end of the stream reads nothing past it):
+// `p` is the next word to load, `first` the base offset inside it, `left` the
+// bases still in `word`.
+struct EmitCursor {
+    const uint32_t* __restrict__ p;
+    uint32_t word, left, first;
+    __device__ __forceinline__ void init(const uint32_t* packed, uint64_t pos) {
+        p = packed + (pos >> 4);
+        first = (uint32_t)(pos & 15u);
+        left = 0;
+    }
+    __device__ __forceinline__ uint32_t next() {
+        if (left == 0) {
+            word = __ldg(p++) >> (first << 1);
+            left = 16u - first;
+            first = 0;
+        }
+        const uint32_t c = word & 3u;
+        word >>= 2;
+        --left;
+        return c;
+    }
+};
+
 // One block per segment of SP_SEGK k-mers; thread t hashes the run of SP_RUN
 // consecutive k-mers starting at k-mer t * SP_RUN of the segment by rolling
 // (re-seeding at read starts).  Record order inside a segment is free (the
@@ -119,7 +144,8 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
     const uint32_t n = NT > 0 ? (uint32_t)NT : sp.n_tables;
     const uint32_t my_len = tid < F ? SP_RUN : (tid == F ? P : 0u);
     uint64_t r = 0, kend = 0, fw = 0, rc = 0;
-    BaseCursor cin, cout;
+    uint32_t left = 0;   // k-mers of the current read from the current one on
+    EmitCursor cin, cout;
     const uint32_t K = hp.K;
     auto seed = [&](uint64_t g) {
         const uint64_t base = __ldg(b.offsets + r) + (g - __ldg(b.kofs + r));
@@ -137,20 +163,26 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
         const uint64_t ga = gs + (uint64_t)tid * SP_RUN;
         r = find_read(b, ga, total);
         kend = __ldg(b.kofs + r + 1);
+        left = (uint32_t)(kend - ga);
         seed(ga);
     }
+    // ordinals are below 2^32; the records of step j start at slot slot0
+    const uint32_t g0 = (uint32_t)gs + tid * SP_RUN;
+    uint4* const obase = reinterpret_cast<uint4*>(rout + (gs + tid) * 4u);
+    uint32_t slot0 = 0;
     const uint32_t n_steps = F ? SP_RUN : P;   // the longest run of the block
     for (uint32_t j = 0; j < n_steps; ++j) {
         const bool act = j < my_len;
-        const uint64_t g = gs + (uint64_t)tid * SP_RUN + j;
         bool reseed = false;
         uint64_t rbase = 0;
         if (act && j > 0) {
-            if (g >= kend) {
+            if (--left == 0) {
+                const uint64_t g = gs + (uint64_t)tid * SP_RUN + j;
                 do {
                     ++r;
                     kend = __ldg(b.kofs + r + 1);
                 } while (kend <= g);
+                left = (uint32_t)(kend - g);
                 rbase = __ldg(b.offsets + r) + (g - __ldg(b.kofs + r));
                 reseed = true;
             } else {
@@ -190,7 +222,6 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
         // slots of step j: threads active at step j, in thread order (the
         // active threads are 0 .. A-1, so thread t takes slot slot0 + t)
         const uint32_t A = j < P ? F + 1 : F;
-        const uint32_t slot0 = j < P ? j * (F + 1) : P * (F + 1) + (j - P) * F;
         if (NT == 4) {
             if (act) {
                 const uint64_t h = hash_value<CANON>(fw, rc);
@@ -204,8 +235,8 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
                 }
                 // the slot's 4 records, (cell << 32) | ordinal, as two 16-byte
                 // stores; consecutive threads write consecutive 32-byte slots
-                const uint32_t gl = (uint32_t)g;
-                uint4* d4 = reinterpret_cast<uint4*>(rout + (gs + slot0 + tid) * 4u);
+                const uint32_t gl = g0 + j;
+                uint4* d4 = obase + 2u * slot0;
                 d4[0] = make_uint4(gl, gc[0], gl, gc[1]);
                 d4[1] = make_uint4(gl, gc[2], gl, gc[3]);
             }
@@ -218,7 +249,7 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
                         const uint32_t gc = (uint32_t)sp.tbase[i] +
                                             (SMALLP ? fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
                                                     : (uint32_t)fastmod(h, tp.p[i], tp.m[i]));
-                        stage[w][lane * n + i] = ((uint64_t)gc << 32) | (uint32_t)g;
+                        stage[w][lane * n + i] = ((uint64_t)gc << 32) | (g0 + j);
                         atomicAdd(&hist[(gc >> sp.fs) >> sp.hi_shift], 1u);
                     }
                 }
@@ -231,6 +262,7 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
             }
             __syncwarp();
         }
+        slot0 += A;
     }
     __syncthreads();
     for (uint32_t k = tid; k < sp.bins1; k += SP_EMIT_BLOCK)
