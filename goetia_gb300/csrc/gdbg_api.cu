@@ -530,15 +530,14 @@ InsertKind insert_kind(const gdbg_graph* g, uint64_t n_total) {
     }
 }
 
-// Read maps the batch insert will use: the windowed path walks k-mer runs
-// (tile map), the persistent and bucketed paths walk warp tasks (task map),
-// the segmented path both.
+// Read maps the batch insert will use: the windowed and segmented paths walk
+// k-mer runs (tile map), the persistent and ordered bucketed paths warp tasks
+// (task map).
 int insert_maps(const gdbg_graph* g, uint64_t n_total) {
     if (n_total == UINT64_MAX) return MAP_TILES | MAP_TASKS;
     switch (insert_kind(g, n_total)) {
     case INS_PERSISTENT:
     case INS_BUCKETED: return MAP_TASKS;
-    case INS_SORTED: return MAP_TILES | MAP_TASKS;
     default: return MAP_TILES;
     }
 }

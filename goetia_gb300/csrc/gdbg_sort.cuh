@@ -168,6 +168,7 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
     }
     // ordinals are below 2^32; the records of step j start at slot slot0
     const uint32_t g0 = (uint32_t)gs + tid * SP_RUN;
+    const uint32_t dsh = sp.fs + sp.hi_shift;   // first digit = cell >> dsh (dsh < 32)
     uint4* const obase = reinterpret_cast<uint4*>(rout + (gs + tid) * 4u);
     uint32_t slot0 = 0;
     const uint32_t n_steps = F ? SP_RUN : P;   // the longest run of the block
@@ -231,7 +232,7 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
                 for (int i = 0; i < 4; ++i) {
                     gc[i] = (uint32_t)sp.tbase[i] + (SMALLP ? fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
                                                             : (uint32_t)fastmod(h, tp.p[i], tp.m[i]));
-                    atomicAdd(&hist[(gc[i] >> sp.fs) >> sp.hi_shift], 1u);
+                    atomicAdd(&hist[gc[i] >> dsh], 1u);
                 }
                 // the slot's 4 records, (cell << 32) | ordinal, as two 16-byte
                 // stores; consecutive threads write consecutive 32-byte slots
@@ -250,7 +251,7 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
                                             (SMALLP ? fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
                                                     : (uint32_t)fastmod(h, tp.p[i], tp.m[i]));
                         stage[w][lane * n + i] = ((uint64_t)gc << 32) | (g0 + j);
-                        atomicAdd(&hist[(gc >> sp.fs) >> sp.hi_shift], 1u);
+                        atomicAdd(&hist[gc >> dsh], 1u);
                     }
                 }
             }
