@@ -85,9 +85,12 @@ class BatchedInserter:
         self.d_packed = torch.zeros(self.max_words, dtype=torch.int32, device=dev)
         self.d_off = torch.zeros(self.max_reads + 1, dtype=torch.int64, device=dev)
         self.d_new = torch.zeros(self.max_reads, dtype=torch.int64, device=dev)
-        self.h_packed = torch.zeros(self.max_words, dtype=torch.int32).pin_memory()
-        self.h_off = torch.zeros(self.max_reads + 1, dtype=torch.int64).pin_memory()
-        self.h_new = torch.zeros(self.max_reads, dtype=torch.int64).pin_memory()
+        # two pinned staging sets: insert_stream fills one on the host while
+        # the batch staged from the other is on the GPU
+        self.h_packed = [torch.zeros(self.max_words, dtype=torch.int32).pin_memory() for _ in range(2)]
+        self.h_off = [torch.zeros(self.max_reads + 1, dtype=torch.int64).pin_memory() for _ in range(2)]
+        self.h_new = [torch.zeros(self.max_reads, dtype=torch.int64).pin_memory() for _ in range(2)]
+        self.done = [torch.cuda.Event(), torch.cuda.Event()]
         self.use_graph = use_graph
         if use_graph:
             if bucketed_fits(graph, self.max_kmers, getattr(graph, "_bucket_bits", 0)):
@@ -103,24 +106,39 @@ class BatchedInserter:
                              self.max_reads, n_kmers=self.max_kmers,
                              n_new_ptr=self.d_new.data_ptr(), stream=self.stream.cuda_stream)
 
-    def _stage(self, batch):
+    def _fill(self, batch, s):
+        """Host side: the batch into pinned staging set s."""
         nw, nr = batch.packed.size, batch.n_reads
         if nr > self.max_reads or batch.n_bases > self.max_bases:
             raise ValueError("batch exceeds the inserter's capacity")
-        self.h_packed[:nw].numpy()[:] = batch.packed.view(np.int32)
-        off = self.h_off.numpy()
+        self.h_packed[s][:nw].numpy()[:] = batch.packed.view(np.int32)
+        off = self.h_off[s].numpy()
         off[:nr + 1] = batch.offsets.view(np.int64)
         off[nr + 1:] = off[nr]          # padding: empty reads
+
+    def _submit(self, batch, s):
+        """Stream side: copy staging set s in, insert, copy the new counts out
+        into set s; done[s] marks the end."""
         torch = self.torch
+        nw, nr = batch.packed.size, batch.n_reads
         with torch.cuda.stream(self.stream):
-            self.d_packed[:nw].copy_(self.h_packed[:nw], non_blocking=True)
-            self.d_off.copy_(self.h_off, non_blocking=True)
+            self.d_packed[:nw].copy_(self.h_packed[s][:nw], non_blocking=True)
+            self.d_off.copy_(self.h_off[s], non_blocking=True)
+            if self.cuda_graph is not None:
+                self.cuda_graph.replay()
+            else:
+                self._launch()
+            if nr:
+                self.h_new[s][:nr].copy_(self.d_new[:nr], non_blocking=True)
+            self.done[s].record(self.stream)
+        self.launches += 1
 
     def prepare(self):
         """Grow the graph's scratch to the capacity with one empty batch and,
         when requested, capture the insert as a CUDA graph."""
         torch = self.torch
-        self.h_off.zero_()
+        for h in self.h_off:
+            h.zero_()
         with torch.cuda.stream(self.stream):
             self.d_off.zero_()
         # scratch sized for the capacity: one insert with the full hint
@@ -136,29 +154,35 @@ class BatchedInserter:
 
     def insert(self, batch, wait=True):
         """Insert one batch; returns its per-read new-k-mer counts (numpy) when
-        wait, else None (results stay in self.d_new until the next call)."""
-        torch = self.torch
-        self._stage(batch)
-        if self.cuda_graph is not None:
-            with torch.cuda.stream(self.stream):
-                self.cuda_graph.replay()
-        else:
-            self._launch()
-        self.launches += 1
+        wait, else None (the counts land in staging set 0 when done[0] fires)."""
+        self.done[1].synchronize()     # a pipelined call may still use the GPU
+        self.done[0].synchronize()
+        self._fill(batch, 0)
+        self._submit(batch, 0)
         if not wait:
             return None
-        nr = batch.n_reads
-        with torch.cuda.stream(self.stream):
-            self.h_new[:nr].copy_(self.d_new[:nr], non_blocking=True)
-        self.stream.synchronize()
-        return self.h_new[:nr].numpy().view(np.uint64).copy()
+        self.done[0].synchronize()
+        return self.h_new[0][:batch.n_reads].numpy().view(np.uint64).copy()
 
     def insert_stream(self, reads):
-        """Insert a whole PackedReads in capacity-sized batches; returns the
-        per-read new counts for all reads."""
+        """Insert a whole PackedReads in capacity-sized batches, in order;
+        returns the per-read new counts for all reads.  The host fills the
+        next batch's staging set while the current batch is on the GPU."""
         out = np.zeros(reads.n_reads, np.uint64)
-        for r0, b in split_batches(reads, self.max_reads, self.max_bases):
-            out[r0:r0 + b.n_reads] = self.insert(b)
+        bats = split_batches(reads, self.max_reads, self.max_bases)
+        if not bats:
+            return out
+        self.done[0].synchronize()
+        self.done[1].synchronize()
+        self._fill(bats[0][1], 0)
+        for i, (r0, b) in enumerate(bats):
+            s = i & 1
+            self._submit(b, s)
+            if i + 1 < len(bats):
+                # set s^1 was last used by batch i-1, finished below last round
+                self._fill(bats[i + 1][1], s ^ 1)
+            self.done[s].synchronize()
+            out[r0:r0 + b.n_reads] = self.h_new[s][:b.n_reads].numpy().view(np.uint64)
         return out
 
 
