@@ -623,7 +623,7 @@ int run_insert_bucketed(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cuda
                 return set_error_launch(e, "bucket scatter");
         }
         std::swap(src, dst);
-        g->launches += 5;   // histogram, 3 scan kernels, scatter
+        g->launches += 4;   // histogram, 2 scan kernels, scatter
     }
     if ((e = launch_bucket_starts_fix(st, bp, g->bstart.p)) != cudaSuccess)
         return set_error_launch(e, "bucket starts");
@@ -724,7 +724,7 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
         if ((e = launch_sp_part(false, st, sp, g->rec_a.p, g->rec_b.p)) != cudaSuccess)
             return set_error_launch(e, "segment partition");
     }
-    g->launches += 5;   // emit, 3 scan kernels, partition
+    g->launches += 4;   // emit, 2 scan kernels, partition
     const uint64_t* fin = g->rec_b.p;
     if (sp.bins2 > 1) {
         GDBG_CUDA(cudaMemsetAsync(sp.hist2, 0, h2 * sizeof(uint32_t), st));
@@ -745,7 +745,7 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
                 return set_error_launch(e, "segment partition");
         }
         fin = g->rec_a.p;
-        g->launches += 6;   // plan, counts, 3 scan kernels, partition
+        g->launches += 5;   // plan, counts, 2 scan kernels, partition
     }
     if ((e = launch_sp_starts(st, sp, g->bstart.p)) != cudaSuccess)
         return set_error_launch(e, "bucket starts");

@@ -68,35 +68,30 @@ k_prefix_partials(const uint64_t* __restrict__ off, uint64_t n, uint32_t K, uint
     }
 }
 
-// Exclusive scan of the (k-mer, task) block partials in place, one block.
-__global__ void __launch_bounds__(SCAN_BLOCK)
-k_prefix_partials_scan(uint64_t* __restrict__ partials, uint64_t nb) {
-    __shared__ uint64_t ws[32];
-    __shared__ uint64_t chunk_total;
-    for (int c = 0; c < 2; ++c) {
-        uint64_t carry = 0;
-        for (uint64_t base = 0; base < nb; base += SCAN_BLOCK) {
-            uint64_t i = base + threadIdx.x;
-            uint64_t v = i < nb ? partials[2 * i + c] : 0;
-            uint64_t s = block_inclusive_scan(v, ws);
-            if (i < nb) partials[2 * i + c] = carry + s - v;
-            if (threadIdx.x == SCAN_BLOCK - 1) chunk_total = s;
-            __syncthreads();
-            carry += chunk_total;
-            __syncthreads();
-        }
-    }
-}
-
+// Each block first sums the (k-mer, task) totals of the blocks before it,
+// so no separate pass scans the partials.
 __global__ void __launch_bounds__(SCAN_BLOCK)
 k_prefix_final(const uint64_t* __restrict__ off, uint64_t n, uint32_t K, uint64_t max_bases,
                const uint64_t* __restrict__ partials, uint64_t* __restrict__ kofs,
                uint64_t* __restrict__ tofs) {
     __shared__ uint64_t ws[32], wt[32];
+    __shared__ uint64_t before_s[2];
+    uint64_t pk = 0, pt = 0;
+    for (uint32_t i = threadIdx.x; i < blockIdx.x; i += SCAN_BLOCK) {
+        pk += partials[2 * i];
+        pt += partials[2 * i + 1];
+    }
+    pk = block_inclusive_scan(pk, ws);
+    pt = block_inclusive_scan(pt, wt);
+    if (threadIdx.x == SCAN_BLOCK - 1) {
+        before_s[0] = pk;
+        before_s[1] = pt;
+    }
+    __syncthreads();
     uint64_t r = (uint64_t)blockIdx.x * SCAN_BLOCK + threadIdx.x;
     ulonglong2 v = r < n ? read_counts(off, r, K, max_bases, nullptr) : make_ulonglong2(0, 0);
-    uint64_t s = block_inclusive_scan(v.x, ws) + partials[2 * blockIdx.x];
-    uint64_t t = block_inclusive_scan(v.y, wt) + partials[2 * blockIdx.x + 1];
+    uint64_t s = block_inclusive_scan(v.x, ws) + before_s[0];
+    uint64_t t = block_inclusive_scan(v.y, wt) + before_s[1];
     if (r < n) {
         kofs[r] = s - v.x;
         tofs[r] = t - v.y;
@@ -142,10 +137,9 @@ cudaError_t launch_kmer_prefix(const uint64_t* offsets, uint64_t n_reads, uint32
     uint64_t nb = (n_reads + SCAN_BLOCK - 1) / SCAN_BLOCK;
     k_prefix_partials<<<(unsigned)nb, SCAN_BLOCK, 0, st>>>(offsets, n_reads, K, max_bases,
                                                            partials, err);
-    k_prefix_partials_scan<<<1, SCAN_BLOCK, 0, st>>>(partials, nb);
     k_prefix_final<<<(unsigned)nb, SCAN_BLOCK, 0, st>>>(offsets, n_reads, K, max_bases, partials,
                                                         kofs, tofs);
-    *launches = 3;
+    *launches = 2;
     return cudaGetLastError();
 }
 

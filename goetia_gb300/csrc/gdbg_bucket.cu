@@ -131,27 +131,19 @@ k_scan32_partials(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restr
     if (threadIdx.x == SCAN32_BLOCK - 1) partials[blockIdx.x] = s;
 }
 
-__global__ void __launch_bounds__(SCAN32_BLOCK)
-k_scan32_partials_scan(uint32_t* __restrict__ partials, uint64_t nb) {
-    __shared__ uint32_t ws[32];
-    __shared__ uint32_t chunk_total;
-    uint32_t carry = 0;
-    for (uint64_t base = 0; base < nb; base += SCAN32_BLOCK) {
-        const uint64_t i = base + threadIdx.x;
-        const uint32_t v = i < nb ? partials[i] : 0;
-        const uint32_t s = block_scan32(v, ws);
-        if (i < nb) partials[i] = carry + s - v;
-        if (threadIdx.x == SCAN32_BLOCK - 1) chunk_total = s;
-        __syncthreads();
-        carry += chunk_total;
-        __syncthreads();
-    }
-}
-
+// Each block first sums the totals of the blocks before it (a few thousand at
+// most), so no separate pass scans the partials.
 __global__ void __launch_bounds__(SCAN32_BLOCK)
 k_scan32_final(const uint32_t* __restrict__ in, uint64_t n, const uint32_t* __restrict__ partials,
                uint32_t* __restrict__ out) {
     __shared__ uint32_t ws[32];
+    __shared__ uint32_t before_s;
+    uint32_t pre = 0;
+    for (uint32_t i = threadIdx.x; i < blockIdx.x; i += SCAN32_BLOCK) pre += partials[i];
+    pre = block_scan32(pre, ws);
+    if (threadIdx.x == SCAN32_BLOCK - 1) before_s = pre;
+    __syncthreads();
+    const uint32_t before = before_s;
     const uint64_t base = ((uint64_t)blockIdx.x * SCAN32_BLOCK + threadIdx.x) * SCAN32_ITEMS;
     uint32_t v[SCAN32_ITEMS], s = 0;
 #pragma unroll
@@ -159,7 +151,7 @@ k_scan32_final(const uint32_t* __restrict__ in, uint64_t n, const uint32_t* __re
         v[j] = base + j < n ? in[base + j] : 0;
         s += v[j];
     }
-    uint32_t run = block_scan32(s, ws) - s + partials[blockIdx.x];
+    uint32_t run = block_scan32(s, ws) - s + before;
 #pragma unroll
     for (int j = 0; j < SCAN32_ITEMS; ++j) {
         if (base + j < n) out[base + j] = run;
@@ -176,7 +168,6 @@ cudaError_t launch_scan32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_
     if (n == 0) return cudaSuccess;
     const uint64_t nb = (n + SCAN32_BLOCK * SCAN32_ITEMS - 1) / (SCAN32_BLOCK * SCAN32_ITEMS);
     k_scan32_partials<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials);
-    k_scan32_partials_scan<<<1, SCAN32_BLOCK, 0, st>>>(partials, nb);
     k_scan32_final<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials, out);
     return cudaGetLastError();
 }
