@@ -339,6 +339,8 @@ def run_batched(args, check_reads=300):
     return {"kmers_per_s": nk / dt, "kmers": nk, "reads": reads.n_reads, "seconds": dt,
             "batches": len(bat), "capacity_reads_bases": list(cap),
             "schedule": tuned["schedule"], "cuda_graph": ins.cuda_graph is not None,
+            "autotune_trials_ms": [{**t["schedule"], "ms": round(1e3 * t["seconds"], 3)}
+                                   for t in tuned.get("trials", [])],
             "plain_kmers_per_s": plain, "batched_over_plain": (nk / dt) / plain,
             "exact_vs_oracle_first_reads": exact, "oracle_checked_reads": sub.n_reads,
             "workload": f"{reads.n_reads} of the 2M uneven reads (median 4 kb, 200 bp-60 kb), "

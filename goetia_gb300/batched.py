@@ -65,8 +65,10 @@ class BatchedInserter:
     max_reads  reads per batch (short batches are padded with empty reads)
     max_bases  bases per batch
     use_graph  capture the insert once and replay it per batch.  Replay needs
-               an insert path that keeps no per-batch state on the host, so
-               the graph is switched to the bucketed path (and replay is
+               an insert path that keeps no per-batch state on the host: the
+               persistent fused kernel (one cooperative launch per batch,
+               its claims epoch kept on the device) or a bucketed path; any
+               other path is switched to the bucketed one (and replay is
                turned off when the tables do not fit it).
     """
 
@@ -92,7 +94,7 @@ class BatchedInserter:
         self.h_new = [torch.zeros(self.max_reads, dtype=torch.int64).pin_memory() for _ in range(2)]
         self.done = [torch.cuda.Event(), torch.cuda.Event()]
         self.use_graph = use_graph
-        if use_graph:
+        if use_graph and str(graph.insert_path()) != "persistent":
             if bucketed_fits(graph, self.max_kmers, getattr(graph, "_bucket_bits", 0)):
                 if not str(graph.insert_path()).startswith("bucketed"):
                     graph.set_insert_path("bucketed")
@@ -205,12 +207,14 @@ def _key(graph, max_reads, max_bases):
 def candidates(storage_type, use_graph=True):
     """Schedules tried by the autotuner: the segmented bucketed path at its
     adaptive bucket size, the ordered bucketed path at three bucket sizes,
-    and -- without graph replay -- the windowed path at two windows and two
-    k-mers per thread."""
+    the persistent fused hash+insert kernel at two claim windows, and --
+    without graph replay -- the windowed path at two windows and two k-mers
+    per thread."""
     from . import dbg as D
     fs0 = {D.BitStorage: 19, D.ByteStorage: 16, D.NibbleStorage: 17}[storage_type]
     out = [{"path": "bucketed", "bucket_bits": 0}]
     out += [{"path": "bucketed_ordered", "bucket_bits": fs} for fs in (fs0 - 1, fs0, fs0 + 1)]
+    out += [{"path": "persistent", "window": w, "kpt": 4} for w in (262144, 1048576)]
     if not use_graph:
         out += [{"path": "windowed", "window": w, "kpt": k}
                 for w in (262144, 1048576) for k in (4, 8)]
@@ -253,7 +257,10 @@ def autotune(graph, sample, max_reads, max_bases, repeats=2, use_cache=True, ver
             if sched["path"].startswith("bucketed") and not bucketed_fits(
                     g, max(max_bases - g.K + 1, 1), sched["bucket_bits"]):
                 continue
-            ins = BatchedInserter(g, max_reads, max_bases, use_graph=use_graph).prepare()
+            try:
+                ins = BatchedInserter(g, max_reads, max_bases, use_graph=use_graph).prepare()
+            except RuntimeError:
+                continue                             # a launch the capture does not take
             ins.insert(sample)                       # warm state
             t = []
             for _ in range(repeats):
