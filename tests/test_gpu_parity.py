@@ -242,6 +242,37 @@ def test_device_pointer_api(cuda_ready):
     assert np.array_equal(d_cnt.cpu().numpy(), st.query_reads(True, 31, pr.packed, pr.offsets))
 
 
+@pytest.mark.parametrize("path", ["bucketed", "bucketed_ordered", "persistent", "windowed"])
+def test_device_batch_ending_on_a_word_boundary(cuda_ready, path):
+    """A device batch whose packed stream has no slack word: its bases end
+    exactly at a 16-base word boundary and its last reads are exactly K long
+    (their k-mer is the last one of the stream); results equal the oracle's."""
+    import torch
+    K = 31
+    gen = synth.genome(100_000, 21)
+    rows = list(synth.sample_reads(gen, 600, 90, 0.01, 22))
+    rows += [rows[0][:K].copy(), rows[1][:K].copy()]
+    pad = (-sum(len(r) for r in rows)) % 16
+    rows[-3] = np.concatenate([rows[-3], rows[-3][:pad]])   # the stream ends on a word boundary
+    pr = G.from_codes(rows)
+    assert int(pr.offsets[-1]) % 16 == 0
+    words = int(pr.offsets[-1]) // 16
+    sizes = oracle.primes(4, 200_003)
+    g = graph_for("byte", True, K, sizes)
+    g.set_insert_path(path)
+    d_packed = torch.from_numpy(pr.packed[:words].view(np.int32).copy()).cuda()
+    d_off = torch.from_numpy(pr.offsets.view(np.int64)).cuda()
+    d_new = torch.zeros(pr.n_reads, dtype=torch.int64, device="cuda")
+    g.insert_device(d_packed.data_ptr(), words, d_off.data_ptr(), pr.n_reads,
+                    n_new_ptr=d_new.data_ptr())
+    g.synchronize()
+    ref = oracle.Storage("byte", sizes)
+    _, want = ref.insert_reads(True, K, pr.packed, pr.offsets)
+    assert np.array_equal(d_new.cpu().numpy().view(np.uint64), want)
+    for a, t in zip(g.get_raw(), ref.tables()):
+        assert np.array_equal(a, t)
+
+
 def test_device_offsets_validated(cuda_ready):
     """Offsets that decrease or run past the packed stream are rejected on
     the device (counted as zero k-mers) and reported, without reading past
