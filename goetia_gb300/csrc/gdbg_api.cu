@@ -149,6 +149,17 @@ struct gdbg_graph {
         uint32_t err, pad;
         uint64_t v[7];
     }* h_ret = nullptr;
+    // host batch inserts: the packed reads move in chunks of whole reads on
+    // copy_stream (chunk_ev[c] after chunk c) while the segmented emit runs on
+    // the segments of the chunks already in; plan.kmer_end[c] is the k-mer
+    // count of chunks 0..c (plan.n chunks, 0 when no plan is pending)
+    static constexpr int N_CHUNKS = 4;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t chunk_ev[N_CHUNKS] = {}, prior_ev = nullptr;
+    struct ChunkPlan {
+        int n = 0;
+        uint64_t kmer_end[N_CHUNKS];
+    } plan;
     // staging for host-pointer calls
     DevBuf<uint32_t> st_packed;
     DevBuf<uint64_t> st_offsets, st_out64, st_out64b, st_out64c;
@@ -356,9 +367,13 @@ int insert_maps(const gdbg_graph* g, uint64_t n_total);
 // checked: the offsets came from a host batch and are validated by the prefix
 // kernel into their own status word; with hint UINT64_MAX that word comes back
 // with the total, so a bad batch fails before any table is touched.
+// probe_reads: reads whose k-mer prefix kofs[r] comes back with the total
+// (into probe_kofs; only with hint UINT64_MAX).
 int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
                   const uint64_t* offsets, uint64_t n_reads, uint64_t hint, cudaStream_t st,
-                  BatchView* view, int maps = MAP_TILES | MAP_TASKS, bool checked = false) {
+                  BatchView* view, int maps = MAP_TILES | MAP_TASKS, bool checked = false,
+                  const uint64_t* probe_reads = nullptr, uint64_t* probe_kofs = nullptr,
+                  int n_probe = 0) {
     GDBG_TRY(g->kofs.ensure(n_reads + 1));
     GDBG_TRY(g->tofs.ensure(n_reads + 1));
     GDBG_TRY(g->partials.ensure(2 * (n_reads / 1024 + 2)));
@@ -371,19 +386,27 @@ int prepare_batch(gdbg_graph* g, const uint32_t* packed, uint64_t packed_words,
     g->launches += nl;
     uint64_t total = hint, tasks = 0;
     if (total == UINT64_MAX) {
-        uint64_t tt[3] = {0, 0, 0};
+        // read back through the pinned block: [0] total, [1] tasks, [2] the
+        // offset check, [3..] the probed prefixes
+        uint64_t* tt = g->h_ret->v;
+        if (n_probe > 4) n_probe = 4;
+        tt[2] = 0;
         GDBG_CUDA(cudaMemcpyAsync(&tt[0], g->kofs.p + n_reads, sizeof(uint64_t),
                                   cudaMemcpyDeviceToHost, st));
         GDBG_CUDA(cudaMemcpyAsync(&tt[1], g->tofs.p + n_reads, sizeof(uint64_t),
                                   cudaMemcpyDeviceToHost, st));
         if (checked)
             GDBG_CUDA(cudaMemcpyAsync(&tt[2], perr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        for (int i = 0; i < n_probe; ++i)
+            GDBG_CUDA(cudaMemcpyAsync(&tt[3 + i], g->kofs.p + probe_reads[i], sizeof(uint64_t),
+                                      cudaMemcpyDeviceToHost, st));
         GDBG_CUDA(cudaStreamSynchronize(st));
         if (tt[2])
             return fail(GDBG_ERR_INVALID_ARG,
                         "offsets must be non-decreasing and end within the packed stream");
         total = tt[0];
         tasks = tt[1];
+        for (int i = 0; i < n_probe; ++i) probe_kofs[i] = tt[3 + i];
     } else {
         // every read adds at most one partly filled task
         tasks = total / TASK_KMERS + std::min<uint64_t>(n_reads, total);
@@ -711,8 +734,30 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
     cudaError_t e;
     {
         Stage sg(g, "k_sp_emit", st);
-        if ((e = launch_sp_emit(canon, st, b, g->hp, g->ts->tp, sp, g->rec_a.p)) != cudaSuccess)
+        if (g->plan.n > 0) {
+            // a host batch still arriving in chunks: each piece covers the
+            // segments whose reads are all in, after its chunk's copy
+            uint32_t s0 = 0;
+            for (int c = 0; c < g->plan.n; ++c) {
+                uint32_t s1 = sp.nseg1;
+                if (c + 1 < g->plan.n)
+                    s1 = (uint32_t)std::min<uint64_t>(sp.nseg1, g->plan.kmer_end[c] / SP_SEGK);
+                if (s1 < s0) s1 = s0;
+                GDBG_CUDA(cudaStreamWaitEvent(st, g->chunk_ev[c], 0));
+                if (s1 > s0) {
+                    if ((e = launch_sp_emit(canon, st, b, g->hp, g->ts->tp, sp, g->rec_a.p, s0,
+                                            s1 - s0)) != cudaSuccess)
+                        return set_error_launch(e, "segment emit");
+                    g->launches += 1;
+                }
+                s0 = s1;
+            }
+            g->plan.n = 0;
+            g->launches -= 1;   // counted with the scans below
+        } else if ((e = launch_sp_emit(canon, st, b, g->hp, g->ts->tp, sp, g->rec_a.p, 0,
+                                       sp.nseg1)) != cudaSuccess) {
             return set_error_launch(e, "segment emit");
+        }
     }
     {
         Stage sg(g, "k_scan32", st);
@@ -955,6 +1000,62 @@ int stage_host_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                          view, maps, total == UINT64_MAX);
 }
 
+// A host batch for an insert.  The offsets move first and the device prefix
+// checks and counts them (with the k-mer prefix at the chunk boundaries); the
+// packed reads then move in N_CHUNKS chunks of whole reads, split by bases,
+// on copy_stream, and g->plan lets the segmented emit start on each chunk's
+// segments as soon as it is in.  Other insert paths wait for the last chunk.
+int stage_host_insert(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
+                      const uint64_t* offsets, uint64_t n_reads, BatchView* view) {
+    constexpr int C = gdbg_graph::N_CHUNKS;
+    if (!offsets || (n_reads && !packed && n_words))
+        return fail(GDBG_ERR_INVALID_ARG, "NULL batch buffers");
+    GDBG_TRY(g->st_packed.ensure(n_words + 1));
+    GDBG_TRY(g->st_offsets.ensure(n_reads + 1));
+    if (!g->copy_stream) {
+        if (cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(GDBG_ERR_CUDA, "cudaStreamCreate failed");
+        for (int c = 0; c < C; ++c)
+            GDBG_CUDA(cudaEventCreateWithFlags(&g->chunk_ev[c], cudaEventDisableTiming));
+        GDBG_CUDA(cudaEventCreateWithFlags(&g->prior_ev, cudaEventDisableTiming));
+    }
+    GDBG_CUDA(cudaMemcpyAsync(g->st_offsets.p, offsets, (n_reads + 1) * sizeof(uint64_t),
+                              cudaMemcpyHostToDevice, g->stream));
+    // chunk c holds reads [rb[c], rb[c+1]); the host offsets only choose the
+    // split (the device checks them), so any answer here is safe
+    uint64_t rb[C + 1];
+    rb[0] = 0;
+    rb[C] = n_reads;
+    const uint64_t b0 = offsets[0], bn = offsets[n_reads];
+    for (int c = 1; c < C; ++c) {
+        const uint64_t target = bn > b0 ? b0 + (bn - b0) / C * c : b0;
+        uint64_t r = (uint64_t)(std::upper_bound(offsets, offsets + n_reads + 1, target) - offsets);
+        r = r ? r - 1 : 0;
+        rb[c] = std::min(std::max(r, rb[c - 1]), (uint64_t)n_reads);
+    }
+    uint64_t kb[C - 1];
+    GDBG_TRY(prepare_batch(g, g->st_packed.p, n_words, g->st_offsets.p, n_reads, UINT64_MAX,
+                           g->stream, view, MAP_FOR_INSERT, true, rb + 1, kb, C - 1));
+    // the offsets are valid from here on: chunk c's words end at the word of
+    // its last base (the word a chunk boundary falls in goes with the earlier
+    // chunk, so every chunk's reads are in once its copy and those before are)
+    GDBG_CUDA(cudaEventRecord(g->prior_ev, g->stream));
+    GDBG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->prior_ev, 0));
+    uint64_t w0 = 0;
+    for (int c = 0; c < C; ++c) {
+        uint64_t w1 = c + 1 < C ? std::min<uint64_t>(n_words, (offsets[rb[c + 1]] + 15) / 16) : n_words;
+        if (w1 < w0) w1 = w0;
+        if (w1 > w0)
+            GDBG_CUDA(cudaMemcpyAsync(g->st_packed.p + w0, packed + w0, (w1 - w0) * sizeof(uint32_t),
+                                      cudaMemcpyHostToDevice, g->copy_stream));
+        GDBG_CUDA(cudaEventRecord(g->chunk_ev[c], g->copy_stream));
+        w0 = w1;
+    }
+    g->plan.n = C;
+    for (int c = 0; c + 1 < C; ++c) g->plan.kmer_end[c] = kb[c];
+    return GDBG_OK;
+}
+
 // One read of len >= K bases as a batch: offsets {0, len}, k-mer prefix
 // {0, n}, task prefix {0, ceil(n / TASK_KMERS)}, zero tile and task maps, a
 // zero n_new slot and the packed bases, written into the pinned block and
@@ -1093,6 +1194,13 @@ int gdbg_destroy(gdbg_graph* g) {
     if (g->h_single) cudaFreeHost(g->h_single);
     if (g->h_ret) cudaFreeHost(g->h_ret);
     if (g->single_done) cudaEventDestroy(g->single_done);
+    if (g->copy_stream) {
+        cudaStreamSynchronize(g->copy_stream);
+        cudaStreamDestroy(g->copy_stream);
+    }
+    for (auto& ev : g->chunk_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (g->prior_ev) cudaEventDestroy(g->prior_ev);
     g->d_single.release();
     g->fresh.release(); g->words_seen.release(); g->claims.release();
     g->kofs.release(); g->tofs.release(); g->partials.release(); g->tile_read.release();
@@ -1630,10 +1738,28 @@ int gdbg_insert_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
     GDBG_TRY(set_device(g));
     BatchView b;
-    GDBG_TRY(stage_host_batch(g, packed, n_words, offsets, n_reads, &b, true));
-    GDBG_TRY(g->st_out64.ensure(n_reads + 1));
-    if (n_new) GDBG_CUDA(cudaMemsetAsync(g->st_out64.p, 0, n_reads * sizeof(uint64_t), g->stream));
-    GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, n_new ? g->st_out64.p : nullptr, g->stream));
+    GDBG_TRY(stage_host_insert(g, packed, n_words, offsets, n_reads, &b));
+    const cudaEvent_t all_in = g->chunk_ev[gdbg_graph::N_CHUNKS - 1];   // chunks copy in order
+    if (insert_kind(g, b.n_kmers) != INS_SORTED) {
+        // only the segmented emit starts before the whole batch is in
+        GDBG_CUDA(cudaStreamWaitEvent(g->stream, all_in, 0));
+        g->plan.n = 0;
+    }
+    int rc = g->st_out64.ensure(n_reads + 1);
+    if (rc == GDBG_OK && n_new && cudaMemsetAsync(g->st_out64.p, 0, n_reads * sizeof(uint64_t),
+                                                  g->stream) != cudaSuccess)
+        rc = fail(GDBG_ERR_CUDA, "cudaMemsetAsync failed");
+    if (rc == GDBG_OK)
+        rc = run_insert(g, b, nullptr, b.n_kmers, n_new ? g->st_out64.p : nullptr, g->stream);
+    if (g->plan.n) {
+        // the plan was not used (an empty batch, or an error before the emit)
+        cudaStreamWaitEvent(g->stream, all_in, 0);
+        g->plan.n = 0;
+    }
+    if (rc != GDBG_OK) {
+        cudaStreamSynchronize(g->copy_stream);   // the caller's buffer is read until then
+        return rc;
+    }
     if (n_new && n_reads)
         GDBG_CUDA(cudaMemcpyAsync(n_new, g->st_out64.p, n_reads * sizeof(uint64_t),
                                   cudaMemcpyDeviceToHost, g->stream));

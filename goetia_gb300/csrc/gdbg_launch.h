@@ -86,8 +86,10 @@ cudaError_t launch_tile_map(const uint64_t* kofs, uint64_t n_reads, uint64_t n_t
                             uint32_t* tile_read, cudaStream_t st);
 
 // Segmented bucketed insert (gdbg_sort.cu / gdbg_sort.cuh).
+// segments [seg0, seg0 + n_seg) of the batch (clipped to sp.nseg1)
 cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
-                           const TableParams& tp, const SortParams& sp, uint64_t* rout);
+                           const TableParams& tp, const SortParams& sp, uint64_t* rout,
+                           uint32_t seg0, uint32_t n_seg);
 cudaError_t launch_sp_part(bool pass2, cudaStream_t st, const SortParams& sp, const uint64_t* rin,
                            uint64_t* rout);
 cudaError_t launch_sp_plan(cudaStream_t st, const SortParams& sp);

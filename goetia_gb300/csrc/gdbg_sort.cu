@@ -5,13 +5,15 @@
 namespace gdbg {
 
 cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
-                           const TableParams& tp, const SortParams& sp, uint64_t* rout) {
-    if (sp.nseg1 == 0) return cudaSuccess;
+                           const TableParams& tp, const SortParams& sp, uint64_t* rout,
+                           uint32_t seg0, uint32_t n_seg) {
+    if (n_seg == 0 || seg0 >= sp.nseg1) return cudaSuccess;
+    if (n_seg > sp.nseg1 - seg0) n_seg = sp.nseg1 - seg0;
     const bool t4 = sp.n_tables == 4;
     bool small = true;   // every table below 2^31 cells: 32-bit remainders
     for (int i = 0; i < tp.n; ++i) small = small && tp.p[i] < (1ull << 31);
-    const unsigned g = sp.nseg1;
-#define GDBG_EMIT(C, N, S) k_sp_emit<C, N, S><<<g, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout)
+    const unsigned g = n_seg;
+#define GDBG_EMIT(C, N, S) k_sp_emit<C, N, S><<<g, SP_EMIT_BLOCK, 0, st>>>(b, hp, tp, sp, rout, seg0)
     if (canonical) {
         if (t4) small ? GDBG_EMIT(true, 4, true) : GDBG_EMIT(true, 4, false);
         else small ? GDBG_EMIT(true, 0, true) : GDBG_EMIT(true, 0, false);

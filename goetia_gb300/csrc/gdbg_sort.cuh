@@ -121,13 +121,14 @@ struct EmitCursor {
 // run per step.
 template <bool CANON, int NT, bool SMALLP>
 __global__ void __launch_bounds__(SP_EMIT_BLOCK)
-k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* __restrict__ rout) {
+k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* __restrict__ rout,
+          uint32_t seg0) {
     __shared__ __align__(16) uint64_t stage[NT == 4 ? 1 : SP_EMIT_BLOCK / 32][32 * BK_MAXNT];
     __shared__ uint32_t hist[256];
     // roll terms by (out, in): fw ^= symk(out) ^ sym(in), rc ^= symk(3-in) ^ sym(3-out)
     __shared__ uint64_t roll_fw[16], roll_rc[16];
     const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const uint32_t s = blockIdx.x;
+    const uint32_t s = seg0 + blockIdx.x;   // launches may cover a range of segments
     for (uint32_t k = tid; k < sp.bins1; k += SP_EMIT_BLOCK) hist[k] = 0;
     if (tid < 16) {
         const uint32_t out = tid >> 2, in = tid & 3u;
