@@ -1019,6 +1019,9 @@ int stage_host_insert(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
             GDBG_CUDA(cudaEventCreateWithFlags(&g->chunk_ev[c], cudaEventDisableTiming));
         GDBG_CUDA(cudaEventCreateWithFlags(&g->prior_ev, cudaEventDisableTiming));
     }
+    // the chunks below wait only for the work the graph's stream holds so far
+    // (an earlier batch may still read the staging buffer)
+    GDBG_CUDA(cudaEventRecord(g->prior_ev, g->stream));
     GDBG_CUDA(cudaMemcpyAsync(g->st_offsets.p, offsets, (n_reads + 1) * sizeof(uint64_t),
                               cudaMemcpyHostToDevice, g->stream));
     // chunk c holds reads [rb[c], rb[c+1]); the host offsets only choose the
@@ -1033,23 +1036,29 @@ int stage_host_insert(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
         r = r ? r - 1 : 0;
         rb[c] = std::min(std::max(r, rb[c - 1]), (uint64_t)n_reads);
     }
-    uint64_t kb[C - 1];
-    GDBG_TRY(prepare_batch(g, g->st_packed.p, n_words, g->st_offsets.p, n_reads, UINT64_MAX,
-                           g->stream, view, MAP_FOR_INSERT, true, rb + 1, kb, C - 1));
-    // the offsets are valid from here on: chunk c's words end at the word of
-    // its last base (the word a chunk boundary falls in goes with the earlier
-    // chunk, so every chunk's reads are in once its copy and those before are)
-    GDBG_CUDA(cudaEventRecord(g->prior_ev, g->stream));
+    // the chunks go out at once and overlap the offsets' copy and check; each
+    // chunk's words end at the word of its last base (the word a chunk
+    // boundary falls in goes with the earlier chunk, so every chunk's reads
+    // are in once its copy and those before it are), all within the packed
+    // stream whatever the offsets say
     GDBG_CUDA(cudaStreamWaitEvent(g->copy_stream, g->prior_ev, 0));
     uint64_t w0 = 0;
     for (int c = 0; c < C; ++c) {
-        uint64_t w1 = c + 1 < C ? std::min<uint64_t>(n_words, (offsets[rb[c + 1]] + 15) / 16) : n_words;
+        uint64_t w1 = n_words;
+        if (c + 1 < C) w1 = std::min<uint64_t>(n_words, (offsets[rb[c + 1]] + 15) / 16);
         if (w1 < w0) w1 = w0;
         if (w1 > w0)
             GDBG_CUDA(cudaMemcpyAsync(g->st_packed.p + w0, packed + w0, (w1 - w0) * sizeof(uint32_t),
                                       cudaMemcpyHostToDevice, g->copy_stream));
         GDBG_CUDA(cudaEventRecord(g->chunk_ev[c], g->copy_stream));
         w0 = w1;
+    }
+    uint64_t kb[C - 1];
+    const int rc = prepare_batch(g, g->st_packed.p, n_words, g->st_offsets.p, n_reads, UINT64_MAX,
+                                 g->stream, view, MAP_FOR_INSERT, true, rb + 1, kb, C - 1);
+    if (rc != GDBG_OK) {
+        cudaStreamSynchronize(g->copy_stream);   // the caller's buffer is read until then
+        return rc;
     }
     g->plan.n = C;
     for (int c = 0; c + 1 < C; ++c) g->plan.kmer_end[c] = kb[c];
