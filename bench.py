@@ -220,6 +220,51 @@ def run_serving(args, check_streams=3):
     }
 
 
+def masks_setup(n_reads):
+    """Tables and query reads of the decision-mask workload: 4 x ~2^28-bit
+    BitStorage (K=31) built from a 20 Mbp genome with 2,000 inserted 1-5 kb
+    repeats and its 0.1% SNP haplotype; n_reads query reads of 150 bp sampled
+    from both haplotypes, resident on cuda:0 with a mask buffer."""
+    import numpy as np
+    import torch
+    import goetia_gb300 as G
+    from goetia_gb300 import synth
+    K = 31
+    a, b = synth.repeat_genome(20_000_000, 2000, 1000, 5000, 0.001, 11)
+    storage = G.BitStorage.build(1 << 28, 4)
+    g = G.dBG[G.BitStorage, G.CanLemireShifter].build(storage, K)
+    for hap in (a, b):
+        g.insert_packed(synth.tiles_of(hap, 100_000, K))
+    half = n_reads // 2
+    q = np.concatenate([synth.sample_reads(a, half, 150, 0.0, 12),
+                        synth.sample_reads(b, n_reads - half, 150, 0.0, 13)])
+    pr = synth.rows_to_packed(q)
+    dev = torch.device("cuda", 0)
+    s = torch.cuda.Stream(dev)
+    g.set_stream(s.cuda_stream)
+    d_p = torch.from_numpy(pr.packed.view(np.int32)).to(dev)
+    d_o = torch.from_numpy(pr.offsets.view(np.int64)).to(dev)
+    d_m = torch.empty(pr.n_kmers(K), dtype=torch.uint8, device=dev)
+    return (a, b), storage, g, pr, s, d_p, d_o, d_m
+
+
+def run_profile_masks(args):
+    """The small case the decision-mask ncu captures run: the mask workload's
+    own tables (4 x ~2^28 bits, 128 MiB) and args.mask_reads query reads,
+    three mask passes."""
+    from goetia_gb300 import build as gbuild
+    gbuild.build()
+    _, _, g, pr, s, d_p, d_o, d_m = masks_setup(args.mask_reads)
+    nk = pr.n_kmers(31)
+    for rep in range(3):
+        g.neighbor_masks_device(d_p.data_ptr(), d_p.numel(), d_o.data_ptr(), pr.n_reads,
+                                d_m.data_ptr(), n_kmers=nk, stream=s.cuda_stream)
+        s.synchronize()
+        print(json.dumps({"profile_masks_pass": rep, "kmers": nk}), flush=True)
+    g.synchronize()
+    return 0
+
+
 def run_masks(args, check_reads=2000):
     """Config 4 shape: decision-node masks against a resident BitStorage, K=31.
     Tables (4 x ~2^28 bits) are built from a 20 Mbp genome with 2,000 inserted
@@ -228,27 +273,12 @@ def run_masks(args, check_reads=2000):
     args.mask_reads query reads (the configuration's 5M by default)."""
     import numpy as np
     import torch
-    import goetia_gb300 as G
     import oracle
     from goetia_gb300 import synth
     K = 31
-    a, b = synth.repeat_genome(20_000_000, 2000, 1000, 5000, 0.001, 11)
-    storage = G.BitStorage.build(1 << 28, 4)
-    g = G.dBG[G.BitStorage, G.CanLemireShifter].build(storage, K)
-    for hap in (a, b):
-        g.insert_packed(synth.tiles_of(hap, 100_000, K))
     n = args.mask_reads
-    half = n // 2
-    q = np.concatenate([synth.sample_reads(a, half, 150, 0.0, 12),
-                        synth.sample_reads(b, n - half, 150, 0.0, 13)])
-    pr = synth.rows_to_packed(q)
+    (a, b), storage, g, pr, s, d_p, d_o, d_m = masks_setup(n)
     nk = pr.n_kmers(K)
-    dev = torch.device("cuda", 0)
-    s = torch.cuda.Stream(dev)
-    g.set_stream(s.cuda_stream)
-    d_p = torch.from_numpy(pr.packed.view(np.int32)).to(dev)
-    d_o = torch.from_numpy(pr.offsets.view(np.int64)).to(dev)
-    d_m = torch.empty(nk, dtype=torch.uint8, device=dev)
     for _ in range(2):
         g.neighbor_masks_device(d_p.data_ptr(), d_p.numel(), d_o.data_ptr(), pr.n_reads,
                                 d_m.data_ptr(), n_kmers=nk, stream=s.cuda_stream)
@@ -642,9 +672,14 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)
     ap.add_argument("--profile-case", action="store_true",
                     help="run only the small insert case the ncu captures profile")
+    ap.add_argument("--profile-masks", action="store_true",
+                    help="run only the decision-mask case the ncu captures profile "
+                         "(--mask-reads query reads)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)
+    if args.profile_masks:
+        return run_profile_masks(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

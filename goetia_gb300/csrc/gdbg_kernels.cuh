@@ -388,6 +388,55 @@ __device__ __forceinline__ bool present(const TableParams& tp, uint64_t h) {
     return ok;
 }
 
+// Presence of 8 neighbour hashes as a bit mask (bit k = nh[k] present), for
+// NT > 1 tables, in two rounds of independent loads: table 0 for every
+// neighbour, then tables 1 .. NT-1 only for the neighbours whose table-0
+// cell is set.  A neighbour is present iff all its cells are non-zero, as
+// in present(); most absent neighbours are settled by their table-0 cell,
+// and no neighbour's probes wait for another neighbour's.
+template <int STORAGE, int NT, bool SMALLP>
+__device__ __forceinline__ uint32_t neighbor_mask(const TableParams& tp, const uint64_t (&nh)[8]) {
+    auto bin = [&](int i, uint64_t h) -> uint64_t {
+        return SMALLP ? (uint64_t)fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
+                      : fastmod(h, tp.p[i], tp.m[i]);
+    };
+    uint32_t cand = 0;
+    {
+        uint32_t w0[8], s0[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const Cell c = cell_of<STORAGE>(tp, 0, bin(0, nh[k]));
+            w0[k] = __ldcg(c.word);
+            s0[k] = c.shift;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+            if (cell_value<STORAGE>(w0[k], s0[k]) != 0) cand |= 1u << k;
+    }
+    // the candidates' other cells, all loads issued before any is tested
+    uint32_t w[8][NT - 1], s[8][NT - 1];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+#pragma unroll
+        for (int i = 1; i < NT; ++i) {
+            w[k][i - 1] = 0;
+            s[k][i - 1] = 0;
+            if ((cand >> k) & 1u) {
+                const Cell c = cell_of<STORAGE>(tp, i, bin(i, nh[k]));
+                w[k][i - 1] = __ldcg(c.word);
+                s[k][i - 1] = c.shift;
+            }
+        }
+    }
+    uint32_t m = cand;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+#pragma unroll
+        for (int i = 1; i < NT; ++i)
+            if (cell_value<STORAGE>(w[k][i - 1], s[k][i - 1]) == 0) m &= ~(1u << k);
+    return m;
+}
+
 template <int STORAGE, bool CANON, int H, int NT, bool SMALLP>
 __global__ void __launch_bounds__(BLOCK)
 k_masks(BatchView b, HashParams hp, TableParams tp, uint8_t* __restrict__ masks) {
@@ -411,9 +460,13 @@ k_masks(BatchView b, HashParams hp, TableParams tp, uint8_t* __restrict__ masks)
             nh[4 + c] = hash_value<CANON>(rf, rr);
         }
         uint32_t m = 0;
+        if constexpr (NT > 1) {
+            m = neighbor_mask<STORAGE, NT, SMALLP>(tp, nh);
+        } else {
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (present<STORAGE, CANON, NT, SMALLP>(tp, nh[k])) m |= 1u << k;
+            for (int k = 0; k < 8; ++k)
+                if (present<STORAGE, CANON, NT, SMALLP>(tp, nh[k])) m |= 1u << k;
+        }
         masks[g0 + j] = (uint8_t)m;
     }
 }
