@@ -664,7 +664,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-masks", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--batched-reads", type=int, default=32_000)
+    ap.add_argument("--batched-reads", type=int, default=131_072)
     ap.add_argument("--mask-reads", type=int, default=5_000_000)
     ap.add_argument("--serve-streams", type=int, default=64)
     ap.add_argument("--serve-scale", type=float, default=0.02)
