@@ -160,6 +160,17 @@ struct gdbg_graph {
         int n = 0;
         uint64_t kmer_end[N_CHUNKS];
     } plan;
+    // asynchronous host-buffer inserts of large batches: two staging slots
+    // used in turn, each filled on copy_stream while the batch before it
+    // runs; `released` follows the last work that reads the slot
+    static constexpr uint64_t ASYNC_SLOT_WORDS = 1u << 20;   // packed words (16 Mbp) and up
+    struct AsyncSlot {
+        DevBuf<uint32_t> packed;
+        DevBuf<uint64_t> offsets, out;
+        cudaEvent_t copied = nullptr, released = nullptr;
+        bool pending = false;
+    } aslot[2];
+    int aslot_next = 0;
     // staging for host-pointer calls
     DevBuf<uint32_t> st_packed;
     DevBuf<uint64_t> st_offsets, st_out64, st_out64b, st_out64c;
@@ -1000,6 +1011,23 @@ int stage_host_batch(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                          view, maps, total == UINT64_MAX);
 }
 
+// The handle's second stream for host-to-device copies, with its events.
+int ensure_copy_stream(gdbg_graph* g) {
+    if (g->copy_stream) return GDBG_OK;
+    if (cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g->copy_stream = nullptr;
+        return fail(GDBG_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    for (auto& ev : g->chunk_ev)
+        GDBG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    GDBG_CUDA(cudaEventCreateWithFlags(&g->prior_ev, cudaEventDisableTiming));
+    for (auto& s : g->aslot) {
+        GDBG_CUDA(cudaEventCreateWithFlags(&s.copied, cudaEventDisableTiming));
+        GDBG_CUDA(cudaEventCreateWithFlags(&s.released, cudaEventDisableTiming));
+    }
+    return GDBG_OK;
+}
+
 // A host batch for an insert.  The offsets move first and the device prefix
 // checks and counts them (with the k-mer prefix at the chunk boundaries); the
 // packed reads then move in N_CHUNKS chunks of whole reads, split by bases,
@@ -1012,13 +1040,7 @@ int stage_host_insert(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
         return fail(GDBG_ERR_INVALID_ARG, "NULL batch buffers");
     GDBG_TRY(g->st_packed.ensure(n_words + 1));
     GDBG_TRY(g->st_offsets.ensure(n_reads + 1));
-    if (!g->copy_stream) {
-        if (cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
-            return fail(GDBG_ERR_CUDA, "cudaStreamCreate failed");
-        for (int c = 0; c < C; ++c)
-            GDBG_CUDA(cudaEventCreateWithFlags(&g->chunk_ev[c], cudaEventDisableTiming));
-        GDBG_CUDA(cudaEventCreateWithFlags(&g->prior_ev, cudaEventDisableTiming));
-    }
+    GDBG_TRY(ensure_copy_stream(g));
     // the chunks below wait only for the work the graph's stream holds so far
     // (an earlier batch may still read the staging buffer)
     GDBG_CUDA(cudaEventRecord(g->prior_ev, g->stream));
@@ -1210,6 +1232,11 @@ int gdbg_destroy(gdbg_graph* g) {
     for (auto& ev : g->chunk_ev)
         if (ev) cudaEventDestroy(ev);
     if (g->prior_ev) cudaEventDestroy(g->prior_ev);
+    for (auto& s : g->aslot) {
+        if (s.copied) cudaEventDestroy(s.copied);
+        if (s.released) cudaEventDestroy(s.released);
+        s.packed.release(); s.offsets.release(); s.out.release();
+    }
     g->d_single.release();
     g->fresh.release(); g->words_seen.release(); g->claims.release();
     g->kofs.release(); g->tofs.release(); g->partials.release(); g->tile_read.release();
@@ -1915,6 +1942,57 @@ int gdbg_insert_batch_async(gdbg_graph* g, const uint32_t* packed, uint64_t n_wo
     if (!g || !offsets || (n_words && !packed)) return fail(GDBG_ERR_INVALID_ARG, "NULL argument");
     GDBG_TRY(set_device(g));
     cudaStream_t st = pick_stream(g, stream);
+    if (n_kmers == UINT64_MAX) {
+        // counted here from the host offsets (a read whose end lies before
+        // its start counts zero, as on the device, which checks them)
+        n_kmers = 0;
+        for (uint64_t r = 0; r < n_reads; ++r) {
+            const uint64_t a = offsets[r], e = offsets[r + 1];
+            if (e > a && e - a >= g->K) n_kmers += e - a - g->K + 1;
+        }
+    }
+    if (n_words >= gdbg_graph::ASYNC_SLOT_WORDS) {
+        // large batch: its copies go to the next staging slot on copy_stream
+        // as soon as the batch two calls back is done with that slot, so they
+        // overlap the previous batch's kernels
+        GDBG_TRY(ensure_copy_stream(g));
+        gdbg_graph::AsyncSlot& s = g->aslot[g->aslot_next];
+        if (s.pending && (s.packed.cap < n_words + 1 || s.offsets.cap < n_reads + 1 ||
+                          s.out.cap < n_reads + 1))
+            GDBG_CUDA(cudaEventSynchronize(s.released));   // regrown below
+        GDBG_TRY(s.packed.ensure(n_words + 1));
+        GDBG_TRY(s.offsets.ensure(n_reads + 1));
+        GDBG_TRY(s.out.ensure(n_reads + 1));
+        if (s.pending) GDBG_CUDA(cudaStreamWaitEvent(g->copy_stream, s.released, 0));
+        GDBG_CUDA(cudaMemcpyAsync(s.packed.p, packed, n_words * sizeof(uint32_t),
+                                  cudaMemcpyHostToDevice, g->copy_stream));
+        GDBG_CUDA(cudaMemcpyAsync(s.offsets.p, offsets, (n_reads + 1) * sizeof(uint64_t),
+                                  cudaMemcpyHostToDevice, g->copy_stream));
+        GDBG_CUDA(cudaEventRecord(s.copied, g->copy_stream));
+        g->aslot_next ^= 1;
+        GDBG_CUDA(cudaStreamWaitEvent(st, s.copied, 0));
+        BatchView b;
+        int rc = prepare_batch(g, s.packed.p, n_words, s.offsets.p, n_reads, n_kmers, st, &b,
+                               insert_maps(g, n_kmers));
+        if (rc == GDBG_OK && n_reads &&
+            cudaMemsetAsync(s.out.p, 0, n_reads * sizeof(uint64_t), st) != cudaSuccess)
+            rc = fail(GDBG_ERR_CUDA, "cudaMemsetAsync failed");
+        if (rc == GDBG_OK) rc = run_insert(g, b, nullptr, b.n_kmers, s.out.p, st);
+        if (rc == GDBG_OK && n_new && n_reads &&
+            cudaMemcpyAsync(n_new, s.out.p, n_reads * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess)
+            rc = fail(GDBG_ERR_CUDA, "cudaMemcpyAsync failed");
+        // the slot is free again once the work queued on `st` so far is done
+        const bool rec = cudaEventRecord(s.released, st) == cudaSuccess;
+        s.pending = rec;
+        if (rc != GDBG_OK || !rec) {
+            cudaStreamSynchronize(g->copy_stream);   // the caller's buffers are read until then
+            cudaStreamSynchronize(st);
+            s.pending = false;
+            return rc != GDBG_OK ? rc : fail(GDBG_ERR_CUDA, "cudaEventRecord failed");
+        }
+        return GDBG_OK;
+    }
     GDBG_TRY(g->st_packed.ensure(n_words + 1));
     GDBG_TRY(g->st_offsets.ensure(n_reads + 1));
     GDBG_TRY(g->st_out64.ensure(n_reads + 1));

@@ -661,9 +661,11 @@ class dBGBase:
     def insert_async(self, packed_ptr, packed_words, offsets_ptr, n_reads, n_kmers, n_new_ptr,
                      stream=None):
         """gdbg_insert_batch_async: host (pinned) buffers in and out, all work
-        queued on `stream`; returns at once."""
+        queued on `stream`; returns at once.  n_kmers None: the call counts
+        the k-mers from the host offsets."""
+        hint = (1 << 64) - 1 if n_kmers is None else int(n_kmers)
         _lib.call("gdbg_insert_batch_async", self._h, packed_ptr, int(packed_words), offsets_ptr,
-                  int(n_reads), int(n_kmers), n_new_ptr, _stream(stream))
+                  int(n_reads), hint, n_new_ptr, _stream(stream))
 
     def reserve_staging(self, max_words, max_reads):
         _lib.call("gdbg_reserve_staging", self._h, int(max_words), int(max_reads))

@@ -240,8 +240,11 @@ int gdbg_insert_batch_device(gdbg_graph* g, const uint32_t* packed, uint64_t pac
  * `stream`; the call returns at once.  The host buffers must stay untouched
  * until the stream has passed this call (record an event after it); with
  * pinned buffers the copies overlap other streams' work.  n_kmers is the
- * batch's k-mer count (or an upper bound).  Calls on one handle reuse its
- * staging buffers in stream order. */
+ * batch's k-mer count (or an upper bound), or UINT64_MAX to have the call
+ * count it from the host offsets.  Calls on one handle reuse its staging
+ * buffers in stream order; the copies of a batch of 2^20 packed words or
+ * more go to one of two staging slots on the handle's copy stream, so they
+ * overlap the kernels of the batch queued before it. */
 int gdbg_insert_batch_async(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
                             const uint64_t* offsets, uint64_t n_reads, uint64_t n_kmers,
                             uint64_t* n_new, void* stream);

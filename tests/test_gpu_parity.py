@@ -290,6 +290,42 @@ def test_device_offsets_validated(cuda_ready):
 
 
 @pytest.mark.parametrize("path", ["bucketed", "windowed"])
+def test_async_host_batches_in_flight(cuda_ready, path):
+    """Large host batches through gdbg_insert_batch_async, queued back to back:
+    their copies go to two staging slots in turn on the handle's second stream
+    (the third call refills the first slot, regrown for a larger batch, while
+    the second batch may still run; the second call counts its k-mers from the
+    host offsets).  Per-read new counts, tables and counters equal those of the
+    same batches through the synchronous host call."""
+    import torch
+    K = 31
+    gen = synth.genome(2_000_000, 31)
+    sizes = oracle.primes(4, 1 << 26)
+    g = graph_for("byte", True, K, sizes)
+    twin = graph_for("byte", True, K, sizes)
+    g.set_insert_path(path)
+    twin.set_insert_path(path)
+    batches, held = [], []
+    for b, n in enumerate((115_000, 120_000, 150_000)):
+        pr = synth.rows_to_packed(synth.sample_reads(gen, n, 150, 0.005, 40 + b))
+        assert pr.packed.size >= 1 << 20   # the two-slot path
+        hp = torch.from_numpy(pr.packed.view(np.int32)).pin_memory()
+        ho = torch.from_numpy(pr.offsets.view(np.int64)).pin_memory()
+        hn = torch.zeros(max(pr.n_reads, 1), dtype=torch.int64).pin_memory()
+        nk = None if b == 1 else pr.n_kmers(K)   # None: the call counts them itself
+        g.insert_async(hp.data_ptr(), pr.packed.size, ho.data_ptr(), pr.n_reads, nk, hn.data_ptr())
+        batches.append(pr)
+        held.append((hp, ho, hn))
+    g.synchronize()
+    for pr, (_, _, hn) in zip(batches, held):
+        want = twin.insert_packed(pr)
+        assert np.array_equal(hn.numpy()[:pr.n_reads].view(np.uint64), want)
+    for a, t in zip(g.get_raw(), twin.get_raw()):
+        assert np.array_equal(a, t)
+    assert (g.n_unique(), g.n_occupied()) == (twin.n_unique(), twin.n_occupied())
+
+
+@pytest.mark.parametrize("path", ["bucketed", "windowed"])
 def test_host_offsets_rejected_before_tables_change(cuda_ready, path):
     """A host batch whose offsets decrease or run past the packed stream is
     refused with INVALID_ARG by the device's offset check, before any table
