@@ -904,6 +904,12 @@ int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64
         w.n_new = (unsigned long long*)n_new;
         w.counters = g->ts->d_counters;
         w.err = g->d_err;
+        if (end - start <= (uint64_t)SMALL_BLOCK) {
+            // a single read or a small chunk: probe and commit in one block,
+            // one k-mer per thread, so no thread updates tables in a chain
+            GDBG_TRY(launch_pass(g, 3, s, end - start, st, b, hashes, w));
+            continue;
+        }
         uint64_t n_threads = (end - start + kpt - 1) / kpt;
         if (n_threads <= (uint64_t)SMALL_BLOCK) {
             // a small window: probe and commit in one block, one launch

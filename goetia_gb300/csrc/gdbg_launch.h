@@ -19,8 +19,9 @@ struct LaunchShape {
     int n_tables;           // 4 uses the unrolled kernels, others the generic ones
 };
 
-// pass 0 = probe, 1 = commit, 2 = both in one block (n_threads <= SMALL_BLOCK);
-// hashes != nullptr selects the hash-array source
+// pass 0 = probe, 1 = commit, 2 = both in one block (n_threads <= SMALL_BLOCK),
+// 3 = both in one block with one k-mer per thread (n_threads = the window's
+// k-mers <= SMALL_BLOCK); hashes != nullptr selects the hash-array source
 template <int STORAGE>
 cudaError_t launch_insert_pass(int pass, const LaunchShape& s, uint64_t n_threads,
                                cudaStream_t st, const BatchView& b, const uint64_t* hashes,

@@ -27,6 +27,18 @@ cudaError_t insert_pass_one(int pass, uint64_t n_threads, cudaStream_t st, const
     return cudaGetLastError();
 }
 
+// Probe and commit of at most SMALL_BLOCK k-mers in one block, one k-mer per
+// thread: each thread's chain of dependent table updates is one k-mer long.
+template <int ST, bool C, int NT, bool FH>
+cudaError_t insert_small_one(uint64_t n_kmers, cudaStream_t st, const BatchView& b,
+                             const uint64_t* hashes, const HashParams& hp, const TableParams& tp,
+                             const WindowParams& w) {
+    if (n_kmers == 0) return cudaSuccess;
+    if (n_kmers > (uint64_t)SMALL_BLOCK) return cudaErrorInvalidValue;
+    k_insert_small<ST, C, 1, NT, FH><<<1, SMALL_BLOCK, 0, st>>>(b, hashes, hp, tp, w);
+    return cudaGetLastError();
+}
+
 template <int ST>
 cudaError_t launch_insert_pass(int pass, const LaunchShape& s, uint64_t n_threads,
                                cudaStream_t st, const BatchView& b, const uint64_t* hashes,
@@ -34,6 +46,16 @@ cudaError_t launch_insert_pass(int pass, const LaunchShape& s, uint64_t n_thread
                                const WindowParams& w) {
     const bool fh = hashes != nullptr;
     const bool t4 = s.n_tables == 4;
+    if (pass == 3) {   // n_threads = k-mers of the window
+        if (fh)
+            return t4 ? insert_small_one<ST, false, 4, true>(n_threads, st, b, hashes, hp, tp, w)
+                      : insert_small_one<ST, false, 0, true>(n_threads, st, b, hashes, hp, tp, w);
+        if (s.canonical)
+            return t4 ? insert_small_one<ST, true, 4, false>(n_threads, st, b, hashes, hp, tp, w)
+                      : insert_small_one<ST, true, 0, false>(n_threads, st, b, hashes, hp, tp, w);
+        return t4 ? insert_small_one<ST, false, 4, false>(n_threads, st, b, hashes, hp, tp, w)
+                  : insert_small_one<ST, false, 0, false>(n_threads, st, b, hashes, hp, tp, w);
+    }
 #define GDBG_PASS(C, H, NT, FH)                                                              \
     if (s.canonical == C && s.kmers_per_thread == H && (NT == 4) == t4 && fh == FH)          \
         return insert_pass_one<ST, C, H, NT, FH>(pass, n_threads, st, b, hashes, hp, tp, w);
