@@ -626,7 +626,7 @@ def run_gpu(args):
         mask_stats = run_masks(args)
     serving_stats = None
     if not args.no_serving:
-        del g, g2, g3
+        del g, g3
         torch.cuda.empty_cache()
         serving_stats = run_serving(args)
 
