@@ -110,3 +110,34 @@ def test_pack_policy():
     assert skipped == 2
     assert list(off) == [0, 4, 8, 8, 12]
     assert packed[0] & 0xFF == 0b11100100  # A C G T -> 0 1 2 3
+
+
+def _packed_reads(rng, genome_len, n_reads, read_len):
+    genome = rng.integers(0, 4, genome_len, dtype=np.uint8)
+    starts = rng.integers(0, genome_len - read_len, n_reads)
+    codes = np.concatenate([genome[s:s + read_len] for s in starts]).astype(np.uint32)
+    idx = np.arange(len(codes), dtype=np.uint64)
+    packed = np.zeros(len(codes) // 16 + 1, np.uint32)
+    np.bitwise_or.at(packed, idx >> 4, codes << (2 * (idx & 15)).astype(np.uint32))
+    offsets = np.arange(0, len(codes) + 1, read_len, dtype=np.uint64)
+    return packed, offsets
+
+
+@pytest.mark.parametrize("kind", ["bit", "byte", "nibble"])
+def test_multithreaded_insert_equals_sequential(kind):
+    """The reference arm's insert on several threads over one shared storage:
+    cell updates are atomic and saturating increments commute, so the tables
+    equal one sequential pass over the same reads.  Small tables saturate
+    many Byte and Nibble cells while the threads race on them."""
+    packed, offsets = _packed_reads(np.random.default_rng(7), 20_000, 3000, 150)
+    sizes = oracle.primes(4, 2003)
+    seq = oracle.Storage(kind, sizes)
+    total, _ = seq.insert_reads(True, 31, packed, offsets)
+    par = oracle.Storage(kind, sizes)
+    assert par.insert_reads_mt(True, 31, packed, offsets, 4) == total == 3000 * 120
+    for a, b in zip(seq.tables(), par.tables()):
+        assert np.array_equal(a, b)
+    if kind == "byte":
+        assert any((t == 255).any() for t in seq.tables())          # saturated cells
+    elif kind == "nibble":
+        assert any(((t >> 4) == 15).any() for t in seq.tables())
