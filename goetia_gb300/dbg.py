@@ -16,6 +16,7 @@ Differences from the reference, all deliberate:
 """
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -103,6 +104,7 @@ class _Storage:
             self.tablesizes = [int(v) for v in out[:got.value]]
         self.build_params = (max_table, N)
         self._anchor = None      # a handle on the device tables, once built
+        self._graphs = weakref.WeakSet()   # the graphs built on it
 
     def _attach(self, h, shifter_kind, K):
         """Keep the tables of handle h alive with this storage object."""
@@ -119,6 +121,29 @@ class _Storage:
 
     def get_tablesizes(self):
         return list(self.tablesizes)
+
+    def _stats(self):
+        # after the work queued on every graph built on the storage; empty
+        # tables before the first one
+        if self._anchor is None:
+            return 0, 0
+        for g in list(self._graphs):
+            g.synchronize()
+        u, o = _lib.c_u64(), _lib.c_u64()
+        _lib.call("gdbg_stats", self._anchor.h, _c.byref(u), _c.byref(o))
+        return int(u.value), int(o.value)
+
+    def n_unique_kmers(self):
+        """k-mers that found a zero cell when inserted (bitstorage.hh:178-181)."""
+        return self._stats()[0]
+
+    def n_occupied(self):
+        """Non-zero cells of table 0 (bitstorage.hh:173-176)."""
+        return self._stats()[1]
+
+    def estimated_fp(self):
+        """(n_occupied / size_0) ^ n_tables (bitstorage.hh:183-187)."""
+        return (self.n_occupied() / self.tablesizes[0]) ** len(self.tablesizes)
 
     def n_tables(self):
         return len(self.tablesizes)
@@ -195,6 +220,7 @@ class dBGBase:
         self._h = handle
         self.K = int(K)
         self.storage = storage
+        storage._graphs.add(self)
         self._cursor = None
         self._stream = None
 

@@ -248,3 +248,27 @@ def test_graphs_on_one_storage_share_tables(cuda_ready, tmp_path):
     g4.load(str(f))
     assert st.get_tablesizes() == [1009, 1013, 1019]
     assert g5.query_sequence(c.reads[0]) == other.query_sequence(c.reads[0])
+
+
+@pytest.mark.parametrize("kind", ["bit", "byte", "nibble"])
+def test_storage_counters_follow_its_graphs(cuda_ready, kind):
+    """Storage-level n_unique_kmers / n_occupied / estimated_fp
+    (bitstorage.hh:173-187) read the tables shared by every graph built on
+    the storage: zero before the first graph, then the oracle's counts after
+    inserts through two graphs on it."""
+    sizes = oracle.primes(4, 40009)
+    st = STORAGES[kind](tablesizes=sizes)
+    assert (st.n_unique_kmers(), st.n_occupied()) == (0, 0)
+    a = G.dBG[STORAGES[kind], G.CanLemireShifter].build(st, 31)
+    b = G.dBG[STORAGES[kind], G.CanLemireShifter].build(st, 31)
+    gen = synth.genome(30_000, 5)
+    first = synth.rows_to_packed(synth.sample_reads(gen, 300, 150, 0.01, 6))
+    second = synth.rows_to_packed(synth.sample_reads(gen, 300, 150, 0.01, 7))
+    a.insert_packed(first)
+    b.insert_packed(second)
+    ref = oracle.Storage(kind, sizes)
+    for pr in (first, second):
+        ref.insert_reads(True, 31, pr.packed, pr.offsets)
+    assert (st.n_unique_kmers(), st.n_occupied()) == ref.stats()
+    assert (a.n_unique(), a.n_occupied()) == (b.n_unique(), b.n_occupied()) == ref.stats()
+    assert st.estimated_fp() == a.estimated_fp() > 0
