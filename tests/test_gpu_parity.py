@@ -452,3 +452,30 @@ def test_pack_reads_device_matches_host_policy(cuda_ready):
         assert np.array_equal(packed.cpu().numpy().view(np.uint32)[:nw], host.packed[:nw])
         p2, o2, sk = oracle.pack_ascii(seqs, min_len)
         assert np.array_equal(o2, host.offsets) and sk == skipped
+
+
+@pytest.mark.parametrize("kind", ["bit", "byte", "nibble"])
+def test_fork_degrees(cuda_ready, kind):
+    """A right fork, as in the reference's tests/test_traversal.py:123-151: a
+    core path and a branch that shares its first 50 bases.  The k-mer ending
+    at the divergence has out-degree 2 and in-degree 1 (left_degree /
+    right_degree, and in_degree / out_degree on the cursor), and it is the
+    decision k-mer find_decision_kmers reports on the core."""
+    K, pivot = 21, 50
+    rng = np.random.default_rng(12)
+    core = "".join(rng.choice(list("ACGT"), 80))
+    alt = "ACGT"[("ACGT".index(core[pivot]) + 1) % 4]
+    branch = core[:pivot] + alt + "".join(rng.choice(list("ACGT"), 29))
+    g = graph_for(kind, True, K, oracle.primes(4, 100_003))
+    g.insert_sequence(core)
+    g.insert_sequence(branch)
+    fork = core[pivot - K:pivot]
+    assert g.right_degree(fork) == 2
+    assert g.left_degree(fork) == 1
+    g.set_cursor(fork)
+    assert (g.in_degree(), g.out_degree(), g.degree()) == (1, 2, 3)
+    pos, hs = g.find_decision_kmers(core)
+    assert pos == [pivot - K]
+    assert int(hs[0]) == int(g.hash(fork))
+    # a k-mer inside the core path away from the fork: one in, one out
+    assert (g.left_degree(core[10:10 + K]), g.right_degree(core[10:10 + K])) == (1, 1)
