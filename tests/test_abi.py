@@ -85,6 +85,22 @@ def test_pack_codes_layout():
     assert np.array_equal((p[j >> 4] >> (2 * (j & 15)).astype(np.uint32)) & 3, c)
 
 
+def test_from_codes_and_kmer_count():
+    rng = np.random.default_rng(9)
+    rows = [rng.integers(0, 4, L, dtype=np.uint8) for L in (0, 5, 31, 32, 150)]
+    pr = reads.from_codes(rows)
+    assert pr.n_reads == 5 and pr.n_bases == 218
+    assert pr.n_kmers(31) == 0 + 0 + 1 + 2 + 120   # short and empty reads count zero
+    flat = np.concatenate(rows)
+    j = np.arange(len(flat))
+    assert np.array_equal((pr.packed[j >> 4] >> (2 * (j & 15)).astype(np.uint32)) & 3, flat)
+    grid = rng.integers(0, 4, (7, 40), dtype=np.uint8)
+    pg = reads.from_codes(grid)
+    assert [int(v) for v in pg.offsets] == [40 * i for i in range(8)]
+    assert pg.n_kmers(21) == 7 * 20
+    assert reads.codes_to_str(reads.str_to_codes("GATTACA")) == "GATTACA"
+
+
 def test_storage_params_mirror():
     from goetia_gb300 import BitStorage, ByteStorage, NibbleStorage
     s = BitStorage.build(4194304, 4)
