@@ -8,6 +8,12 @@
 //
 // Usage:
 //   ref_driver <bit|byte|nibble> <can|fwd> <K> <n_tables> <max_table> <reads.txt> <outdir>
+//   ref_driver time <bit|byte|nibble> <can|fwd> <K> <n_tables> <max_table> <reads.txt>
+//
+// The second form only times dBG::insert_sequence(seq, n_new) over the reads
+// in file order on one thread (steady clock around the loop) and prints
+// "<k-mers> <new k-mers> <seconds>", for comparing the C restatement's speed
+// with the reference's own code on the same host.
 //
 // reads.txt holds one read per line.  For every read, in file order, the
 // driver calls dBG::insert_sequence(seq, n_new) (dbg.hh:296-305), catching the
@@ -32,6 +38,7 @@
 #include "goetia/storage/nibblestorage.hh"
 #include "goetia/hashing/shifter_types.hh"
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -208,7 +215,55 @@ static int run(uint16_t K, uint16_t n_tables, uint64_t max_table,
     return 0;
 }
 
+template <class Storage, class Shifter>
+static int time_insert(uint16_t K, uint16_t n_tables, uint64_t max_table,
+                       const std::vector<std::string>& reads) {
+    auto storage = Storage::build(max_table, n_tables);
+    auto graph = dBG<Storage, Shifter>::build(storage, K);
+    uint64_t total = 0, new_total = 0;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (const auto& s : reads) {
+        try {
+            uint64_t nn = 0;
+            total += graph->insert_sequence(s, nn);
+            new_total += nn;
+        } catch (SequenceLengthException&) {
+        }
+    }
+    const double dt =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::printf("%llu %llu %.6f\n", (unsigned long long)total, (unsigned long long)new_total, dt);
+    return 0;
+}
+
+static std::vector<std::string> read_lines(const char* path) {
+    std::vector<std::string> reads;
+    std::ifstream in(path);
+    std::string line;
+    while (std::getline(in, line)) reads.push_back(line);
+    return reads;
+}
+
 int main(int argc, char** argv) {
+    if (argc == 8 && std::string(argv[1]) == "time") {
+        const std::string kind = argv[2];
+        const bool can = std::string(argv[3]) == "can";
+        const uint16_t K = (uint16_t)std::atoi(argv[4]);
+        const uint16_t N = (uint16_t)std::atoi(argv[5]);
+        const uint64_t max_table = std::strtoull(argv[6], nullptr, 10);
+        const auto reads = read_lines(argv[7]);
+        if (kind == "bit")
+            return can ? time_insert<BitStorage, CanLemireShifter>(K, N, max_table, reads)
+                       : time_insert<BitStorage, FwdLemireShifter>(K, N, max_table, reads);
+        if (kind == "byte")
+            return can ? time_insert<ByteStorage, CanLemireShifter>(K, N, max_table, reads)
+                       : time_insert<ByteStorage, FwdLemireShifter>(K, N, max_table, reads);
+        if (kind == "nibble")
+            return can ? time_insert<NibbleStorage, CanLemireShifter>(K, N, max_table, reads)
+                       : time_insert<NibbleStorage, FwdLemireShifter>(K, N, max_table, reads);
+        std::fprintf(stderr, "unknown storage %s\n", kind.c_str());
+        return 1;
+    }
     if (argc != 8) {
         std::fprintf(stderr, "usage: %s <bit|byte|nibble> <can|fwd> <K> <n_tables> <max_table> <reads.txt> <outdir>\n", argv[0]);
         return 1;
