@@ -298,6 +298,7 @@ static void walk_reads(int canonical, uint16_t K, const uint32_t* packed,
 
 typedef struct { uint64_t* val; uint64_t* fw; uint64_t* rc; uint64_t k; } hash_ctx;
 static void hash_cb(void* c, uint64_t r, uint64_t p, const shifter* s) {
+    (void)r; (void)p;   /* the read walker's callback signature */
     hash_ctx* h = (hash_ctx*)c;
     if (h->val) h->val[h->k] = sh_value(s);
     if (h->fw) h->fw[h->k] = s->fw.h;
@@ -313,6 +314,7 @@ void orc_hash_reads(int canonical, uint16_t K, const uint32_t* packed,
 
 typedef struct { orc_storage* s; uint64_t* n_new; uint64_t total; } ins_ctx;
 static void ins_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    (void)r; (void)p;   /* the read walker's callback signature */
     ins_ctx* x = (ins_ctx*)c;
     int nw = orc_insert(x->s, sh_value(sh));
     if (x->n_new) x->n_new[r] += (uint64_t)nw;
@@ -330,6 +332,7 @@ uint64_t orc_insert_reads(orc_storage* s, int canonical, uint16_t K, const uint3
 
 typedef struct { orc_storage* s; int16_t* counts; uint64_t k; } iq_ctx;
 static void iq_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    (void)r; (void)p;   /* the read walker's callback signature */
     iq_ctx* x = (iq_ctx*)c;
     x->counts[x->k++] = orc_insert_and_query(x->s, sh_value(sh));
 }
@@ -343,6 +346,7 @@ void orc_insert_and_query_reads(orc_storage* s, int canonical, uint16_t K, const
 
 typedef struct { const orc_storage* s; int16_t* counts; uint64_t k; } q_ctx;
 static void q_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    (void)r; (void)p;   /* the read walker's callback signature */
     q_ctx* x = (q_ctx*)c;
     x->counts[x->k++] = orc_query(x->s, sh_value(sh));
 }
@@ -405,6 +409,7 @@ static int cmp_hp(const void* a, const void* b) {
 }
 typedef struct { uint64_t* h; uint64_t k; } collect_ctx;
 static void collect_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    (void)r; (void)p;   /* the read walker's callback signature */
     collect_ctx* x = (collect_ctx*)c;
     x->h[x->k++] = sh_value(sh);
 }
@@ -496,6 +501,7 @@ static void atomic_insert(orc_storage* s, uint64_t h) {
 
 typedef struct { orc_storage* s; uint64_t total; } mt_ctx;
 static void mt_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    (void)r; (void)p;   /* the read walker's callback signature */
     mt_ctx* x = (mt_ctx*)c;
     atomic_insert(x->s, sh_value(sh));
     x->total++;
