@@ -67,17 +67,58 @@ def over_ranks(dt, kmers, dev, world):
     return float(t.item()), float(k.item())
 
 
-def make_batches(n_batches, reads_per_step, seed0=4):
-    """Seeded batches of packed reads (N-reads already dropped)."""
+def make_batches(n_batches, reads_per_step, seed0=4, native=True):
+    """Seeded batches of packed reads (N-reads already dropped).  native=False
+    packs with numpy alone, so the reference arm never loads the GPU library;
+    both give the same words."""
     from goetia_gb300 import synth
     g = synth.genome(GENOME_LEN, 3)
     out = []
     for b in range(n_batches):
         rows = synth.sample_reads(g, reads_per_step, READ_LEN, SUB_RATE, seed0 + 1000 * b)
         keep = ~synth.n_read_mask(reads_per_step, N_READ_FRAC, seed0 + 1000 * b + 1)
-        pr = synth.rows_to_packed(rows[keep])
+        pr = synth.rows_to_packed(rows[keep], native=native)
         pr.n_skipped = int((~keep).sum())
         out.append(pr)
+    return out
+
+
+def oracle_check_headline(batches, sizes, gpu_tables, gpu_last_new, gpu_occupied, threads):
+    """Bit-exact check of the timed run's end state against the oracle at the
+    full benchmark shape (4 x ~2^30 Byte cells, every batch of the run).  The
+    final table bytes do not depend on insertion order (a cell ends at
+    min(255, its touches)), so all batches but the last go in with the
+    oracle's multi-threaded insert; the last batch goes in sequentially, in
+    batch order, which gives the reference's per-read new counts for it.
+    Compared: those counts, all table bytes, and n_occupied (the non-zero
+    cells of table 0)."""
+    import oracle
+    t0 = time.perf_counter()
+    st = oracle.Storage("byte", sizes)
+    for pr in batches[:-1]:
+        st.insert_reads_mt(True, K, pr.packed, pr.offsets, threads)
+    last = batches[-1]
+    _, want_new = st.insert_reads(True, K, last.packed, last.offsets)
+    new_ok = bool(np.array_equal(gpu_last_new, want_new))
+    tables_ok = True
+    step = 1 << 26
+    for i, gt in enumerate(gpu_tables):
+        ot = st.table_view(i)
+        tables_ok &= len(ot) == len(gt)
+        for a in range(0, len(gt), step):
+            if not tables_ok:
+                break
+            tables_ok &= bool(np.array_equal(ot[a:a + step], gt[a:a + step]))
+    occ_ok = int(np.count_nonzero(st.table_view(0))) == int(gpu_occupied)
+    out = {"exact_vs_oracle": bool(new_ok and tables_ok and occ_ok),
+           "last_batch_new_counts_equal": new_ok, "table_bytes_equal": bool(tables_ok),
+           "n_occupied_equal": occ_ok,
+           "checked": f"all {len(batches)} batches of the run ({sum(b.n_reads for b in batches)} "
+                      f"reads) into 4 x ~2^30 oracle cells; per-read new counts of the last "
+                      f"batch ({last.n_reads} reads, sequential oracle insert), all "
+                      f"{sum(len(t) for t in gpu_tables)} table bytes, n_occupied",
+           "seconds": time.perf_counter() - t0}
+    del st
     return out
 
 
@@ -146,10 +187,10 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic_per_kmer():
-    """DRAM bytes per k-mer of the insert kernels from the committed ncu
-    summary (profiles/insert_byte_k31_traffic.txt), or None."""
-    p = os.path.join(HERE, "profiles", "insert_byte_k31_traffic.txt")
+def profile_traffic_per_kmer(name="insert_byte_k31_traffic.txt"):
+    """DRAM bytes per k-mer from a committed ncu summary under profiles/ (its
+    `dram_bytes_per_kmer=` line), or None."""
+    p = os.path.join(HERE, "profiles", name)
     try:
         for ln in open(p):
             if ln.startswith("dram_bytes_per_kmer="):
@@ -305,9 +346,19 @@ def run_masks(args, check_reads=2000):
         ref.insert_reads(True, K, t.packed, t.offsets)
     want = ref.decision_masks(True, K, pr.packed, sub_off)
     exact = bool(np.array_equal(masks[:len(want)], want))
+    peak, peak_kind = measured_peak()
+    tpk = profile_traffic_per_kmer("decision_masks_bit_k31_ncu.md")
+    roof = None
+    if tpk:
+        roof = {"bound": "hbm", "achieved": nk / dt * tpk / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": nk / dt * tpk / 1e9 / peak, "dram_bytes_per_kmer": tpk,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "bytes_source": "DRAM read + write bytes per k-mer of an ncu capture of k_masks "
+                                "on 500,000 of this leg's query reads and its tables "
+                                "(profiles/decision_masks_bit_k31_ncu.md), times k-mers/s",
+                "probes_per_kmer": "32 counted (8 neighbours x 4 tables); 15.6 sectors loaded"}
     return {"kmers_per_s": nk / dt, "ms_per_pass": dt * 1e3, "kmers": nk,
-            "decision_kmers": int(((lo > 1) | (hi > 1)).sum()),
-            "probe_bytes_per_kmer": 1024, "achieved_GBs_at_1024B": nk / dt * 1024 / 1e9,
+            "decision_kmers": int(((lo > 1) | (hi > 1)).sum()), "roofline": roof,
             "exact_vs_oracle_sample": exact, "oracle_sample_reads": check_reads,
             "workload": f"{n} reads x 150 bp vs Bit 4 x ~2^28 bits built from a 20 Mbp "
                         "genome + 2,000 1-5 kb repeats + 0.1% SNP haplotype"}
@@ -401,36 +452,41 @@ def run_profile_case(args):
 
 
 def run_reference(args):
+    """The reference's insert algorithm on the host cores: the oracle's C
+    restatement (the reference's own objects are x86 builds that do not run
+    on the Arm GPU host), all threads sharing one storage, over the same
+    warm-up + timed batches the GPU arm inserts (same seeds, generated and
+    packed with numpy alone), into the same 4 x ~2^30-cell Byte tables."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     import oracle
     threads = os.cpu_count() or 1
-    batches = make_batches(1 + 0, args.reads_per_step)
+    batches = make_batches(args.warmup + args.steps, args.reads_per_step, native=False)
     sizes = oracle.primes(N_TABLES, MAX_TABLE)
     st = oracle.Storage("byte", sizes)
-    pr = batches[0]
-    n = min(args.reference_sample_reads, pr.n_reads)
-    off = pr.offsets[:n + 1].copy()
-    for _ in range(args.warmup):
-        st.insert_reads_mt(True, K, pr.packed, off, threads)
+    for pr in batches[:args.warmup]:
+        st.insert_reads_mt(True, K, pr.packed, pr.offsets, threads)
     t0 = time.perf_counter()
     total = 0
-    for _ in range(args.steps):
-        total += st.insert_reads_mt(True, K, pr.packed, off, threads)
+    for pr in batches[args.warmup:]:
+        total += st.insert_reads_mt(True, K, pr.packed, pr.offsets, threads)
     dt = time.perf_counter() - t0
     v = total / dt
+    n = batches[0].n_reads
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "k-mers/s", "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64/u8",
-        "data": "synthetic (seeded)",
+        "data": "synthetic (seeded genome and reads)",
         "config": {"workload": WORKLOAD, "reads_per_step": int(n), "read_len": READ_LEN,
-                   "table_cells": sizes},
+                   "table_cells": sizes, "genome_bp": GENOME_LEN, "substitution_rate": SUB_RATE,
+                   "batches": f"the GPU arm's {args.warmup} warm-up + {args.steps} timed "
+                              "batches, same seeds"},
         "cpu_baseline": {"value": v, "unit": "k-mers/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} reads x {READ_LEN} bp per step of the same workload, "
-                                   f"C restatement of the reference insert, {threads} threads "
-                                   "on one shared storage"},
+                         "sample": f"{args.steps} distinct batches of ~{n} reads x {READ_LEN} bp "
+                                   f"({total} k-mers), C restatement of the reference insert, "
+                                   f"{threads} threads on one shared storage"},
         "e2e": {"value": v, "unit": "k-mers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -600,6 +656,24 @@ def run_gpu(args):
     plain_dt = time.perf_counter() - t0
     plain_value = pk / plain_dt
 
+    # bit-exact check of the timed run's end state against the oracle at the
+    # full shape, on the host cores while the other legs use the GPU
+    exact = {}
+    checker = None
+    if rank == 0 and not args.no_oracle_check:
+        gpu_state = (g.get_raw(), d_batches[-1][2].cpu().numpy().view(np.uint64)[:batches[-1].n_reads],
+                     g.n_occupied())
+
+        def _check():
+            try:
+                exact.update(oracle_check_headline(batches, storage.get_tablesizes(), *gpu_state,
+                                                   max(1, (os.cpu_count() or 2) - 2)))
+            except Exception as e:   # reported in the line, never hidden
+                exact.update({"exact_vs_oracle": False, "error": repr(e)})
+
+        checker = threading.Thread(target=_check, daemon=True)
+        checker.start()
+
     peak, peak_kind = measured_peak()
     achieved = value / world * BYTES_PER_KMER / 1e9
     tpk = profile_traffic_per_kmer()
@@ -624,6 +698,9 @@ def run_gpu(args):
     mask_stats = None
     if not args.no_masks:
         mask_stats = run_masks(args)
+    if checker is not None:
+        checker.join()
+        del gpu_state
     serving_stats = None
     if not args.no_serving:
         del g, g3
@@ -654,6 +731,7 @@ def run_gpu(args):
                                        "bucketed (ordered)" if "k_bkt_apply" in stages else
                                        "windowed"),
                        "l2": "inputs larger than L2: 4 GiB of tables, random cells",
+                       "exact_vs_oracle": exact.get("exact_vs_oracle"),
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": "k-mers/s", "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps, "same_new_counts_as_value_arm": same,
@@ -668,6 +746,7 @@ def run_gpu(args):
             "decision_masks": mask_stats,
             "batched_uneven": batched_stats,
             "roofline": roofline,
+            "oracle_check": exact or None,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
         }
@@ -688,11 +767,12 @@ def main():
     ap.add_argument("--kpt", type=int, default=0)
     ap.add_argument("--plain-reads", type=int, default=2000)
     ap.add_argument("--cpu-sample-reads", type=int, default=300_000)
-    ap.add_argument("--reference-sample-reads", type=int, default=1_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-masks", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-oracle-check", action="store_true",
+                    help="skip the oracle check of the timed run's end state")
     ap.add_argument("--batched-reads", type=int, default=131_072)
     ap.add_argument("--mask-reads", type=int, default=5_000_000)
     ap.add_argument("--serve-streams", type=int, default=64)

@@ -86,6 +86,7 @@ SIGNATURES = {
     "gdbg_set_insert_path": [c_vp, c_int],
     "gdbg_set_bucket_bits": [c_vp, c_u32],
     "gdbg_device_status": [c_vp, u32p],
+    "gdbg_set_wait_limits": [c_vp, c_u32, c_u32],
     "gdbg_noalloc_table_layout": [c_int, u64p, c_u16, u64p],
     "gdbg_insert_batch_noalloc": [c_int, c_int, c_u16, u64p, c_u16, c_vp, c_vp, c_u64, c_vp,
                                   c_u64, c_vp, c_vp, c_vp],

@@ -15,6 +15,7 @@
 
 #include <cuda_runtime.h>
 
+#include "gdbg_device.cuh"
 #include "gdbg_launch.h"
 #include "goetia_gb300.h"
 
@@ -42,14 +43,6 @@ int fail(int code, const std::string& msg) {
         int rc_ = (call);                    \
         if (rc_ != GDBG_OK) return rc_;      \
     } while (0)
-
-uint64_t host_rotl(uint64_t x, unsigned r) {
-    r &= 63u;
-    return r ? (x << r) | (x >> (64u - r)) : x;
-}
-
-constexpr uint64_t HSYM[4] = {16664410744025174816ull, 15956807086001210932ull,
-                              9404339731978646439ull, 836480985777824379ull};
 
 template <class T>
 struct DevBuf {
@@ -132,6 +125,8 @@ struct gdbg_graph {
     DevBuf<uint32_t> cq_min, cq_ones;
     uint32_t* d_epoch = nullptr;
     unsigned int* d_bar = nullptr;
+    // poll limits of the bounded device waits (0: the kernels' default)
+    uint32_t barrier_polls = 0, copy_polls = 0;
     bool epoch_on_device = false;
     uint32_t epoch_staging = 0;
     // batch scratch
@@ -304,8 +299,7 @@ int init_handle(gdbg_graph* g, int storage, int shifter, uint16_t K) {
     if (cudaHostAlloc((void**)&g->h_ret, sizeof(gdbg_graph::Ret), cudaHostAllocDefault) != cudaSuccess ||
         cudaEventCreateWithFlags(&g->single_done, cudaEventDisableTiming) != cudaSuccess)
         return fail(GDBG_ERR_OOM, "pinned status allocation failed");
-    g->hp.K = K;
-    for (int c = 0; c < 4; ++c) g->hp.tk[c] = host_rotl(HSYM[c], K % 64u);
+    g->hp = make_hash_params(K);
     return GDBG_OK;
 }
 
@@ -740,6 +734,7 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
     sp.off2 = h2 ? g->sp_off2.p : nullptr;
     sp.plan = g->sp_plan.p;
     sp.err = g->d_err;
+    sp.wait_cap = g->copy_polls;
     GDBG_CUDA(cudaMemsetAsync(g->new_bits.p, 0, (nk / 32 + 2) * sizeof(uint32_t), st));
     const bool canon = g->shifter == GDBG_CAN_LEMIRE;
     cudaError_t e;
@@ -839,7 +834,8 @@ int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cu
         g->epoch_on_device = true;
     }
     GDBG_CUDA(cudaMemsetAsync(g->d_bar, 0, 2 * sizeof(unsigned int), st));
-    PersistParams pp;
+    PersistParams pp{};
+    pp.spin_cap = g->barrier_polls;
     pp.window_tasks = (uint32_t)(W / TASK_KMERS);
     pp.fresh = g->fresh.p;
     pp.words = g->words_seen.p;
@@ -2102,6 +2098,13 @@ int gdbg_set_bucket_bits(gdbg_graph* g, uint32_t log2_cells) {
         if (smem > 200 * 1024) return fail(GDBG_ERR_INVALID_ARG, "bucket does not fit shared memory");
     }
     g->bucket_fs = log2_cells;
+    return GDBG_OK;
+}
+
+int gdbg_set_wait_limits(gdbg_graph* g, uint32_t barrier_polls, uint32_t copy_polls) {
+    if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
+    g->barrier_polls = barrier_polls;
+    g->copy_polls = copy_polls;
     return GDBG_OK;
 }
 

@@ -29,6 +29,16 @@ __host__ __device__ __forceinline__ uint64_t rotl64(uint64_t x, unsigned r) {
 __host__ __device__ __forceinline__ uint64_t rotl1(uint64_t x) { return (x << 1) | (x >> 63); }
 __host__ __device__ __forceinline__ uint64_t rotr1(uint64_t x) { return (x >> 1) | (x << 63); }
 
+// Host side: the kernels' hash constants for K, the four symbol words rotated
+// by K mod 64 (the term CyclicHash::update removes, cyclichash.h:85-92).
+inline HashParams make_hash_params(uint32_t K) {
+    const uint64_t words[4] = {SYM_A, SYM_C, SYM_G, SYM_T};
+    HashParams hp{};
+    hp.K = K;
+    for (int c = 0; c < 4; ++c) hp.tk[c] = rotl64(words[c], K % 64u);
+    return hp;
+}
+
 // Symbol word for a 2-bit code, selected in registers (no indexed memory).
 __device__ __forceinline__ uint64_t sym(uint32_t c) {
     uint64_t lo = (c & 1u) ? SYM_C : SYM_A;

@@ -127,16 +127,15 @@ template <int ST, bool C, int NT>
 cudaError_t persist_one(uint64_t max_tasks, cudaStream_t st, const BatchView& b,
                         const HashParams& hp, const TableParams& tp, const PersistParams& pp,
                         int* grid_used) {
-    static int per_sm = -1, n_sm = 0;
     auto kern = k_insert_persistent<ST, C, NT>;
-    if (per_sm < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PBLOCK, 0);
-        if (e != cudaSuccess) return e;
-    }
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    // co-resident blocks of the current device (occupancy queries are cheap
+    // and per device, so nothing is cached across calls or devices)
+    int dev = 0, n_sm = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PBLOCK, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1 || n_sm < 1) return cudaErrorInvalidConfiguration;
     uint64_t want = (max_tasks * 32 + PBLOCK - 1) / PBLOCK;
     uint64_t grid = (uint64_t)per_sm * n_sm;
     if (want < grid) grid = want ? want : 1;

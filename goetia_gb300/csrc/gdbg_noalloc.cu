@@ -20,12 +20,14 @@
 // barrier are cleared at the start of every call.  Two calls whose work
 // overlaps on the GPU (different streams, or different host threads) race on
 // the array; serialise them.
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
 
+#include "gdbg_device.cuh"
 #include "gdbg_launch.h"
 #include "goetia_gb300.h"
 
@@ -175,14 +177,7 @@ extern "C" int gdbg_insert_batch_noalloc(int storage, int shifter, uint16_t K, c
             off += ((table_bytes(storage, sizes[i]) + 3) / 4 + 63) / 64 * 64;
         }
         tp.n = n_tables;
-        HashParams hp{};
-        hp.K = K;
-        static const uint64_t sym[4] = {16664410744025174816ull, 15956807086001210932ull,
-                                        9404339731978646439ull, 836480985777824379ull};
-        for (int c = 0; c < 4; ++c) {
-            const unsigned r = K % 64u;
-            hp.tk[c] = r ? (sym[c] << r) | (sym[c] >> (64u - r)) : sym[c];
-        }
+        const HashParams hp = make_hash_params(K);
         BatchView b{};
         b.packed = packed;
         b.offsets = offsets;
@@ -217,6 +212,20 @@ extern "C" int gdbg_insert_batch_noalloc(int storage, int shifter, uint16_t K, c
             (e = cudaMemsetAsync(stats + 2, 0, 8, st)) != cudaSuccess ||
             (e = cudaMemcpyAsync(stats + 2, &hdr->err, 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
             return na_fail(GDBG_ERR_CUDA, cudaGetErrorString(e));
+        return GDBG_OK;
     }
+    // no stats buffer to carry the device status: wait for the insert and
+    // report a failed device-side check here, before the next call clears it
+    uint32_t err = 0;
+    if ((e = cudaMemcpyAsync(&err, &hdr->err, sizeof err, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return na_fail(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    if (err)
+        return na_fail(GDBG_ERR_DEVICE,
+                       "device status 0x" + [&] {
+                           char b[16];
+                           std::snprintf(b, sizeof b, "%x", err);
+                           return std::string(b);
+                       }() + " (1=CAS cap, 2=claims map full, 4=barrier timeout, 8=bad read offsets)");
     return GDBG_OK;
 }

@@ -15,8 +15,10 @@
 // first-touch map), waits at a grid barrier, runs the commit phase (apply the
 // inserts, decide which k-mers are new), and waits again.  A window's table
 // sectors stay in L2 between the two phases.  The barrier spins with an
-// iteration cap: when it runs out the kernel records GDBG_ERR_BARRIER_TIMEOUT
-// and every block returns.
+// iteration cap (PersistParams::spin_cap, WAIT_CAP by default): when it runs
+// out the kernel records GDBG_ERR_BARRIER_TIMEOUT and every block returns.
+// The claims of an aborted run are never trusted again: the kernel leaves the
+// epoch at 127, so the next run starts by clearing the claims map.
 #pragma once
 #include "gdbg_kernels.cuh"
 
@@ -24,12 +26,9 @@ namespace gdbg {
 
 constexpr int PBLOCK = 512;
 
-
-constexpr uint32_t BARRIER_SPIN_CAP = 1u << 24;   // ~1-2 s of polling
-
 // Grid-wide barrier for a cooperative launch.  Returns false (for every
-// thread of the block) when the wait ran past its cap.
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, uint32_t* err) {
+// thread of the block) when the wait ran past `cap` polls.
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, uint32_t* err, uint32_t cap) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -45,7 +44,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, uint32_t* err) {
         } else {
             uint32_t spins = 0;
             while (*vgen == gen) {
-                if (++spins > BARRIER_SPIN_CAP) {
+                if (++spins > cap) {
                     atomicOr(err, GDBG_ERR_BARRIER_TIMEOUT);
                     ok = 0;
                     break;
@@ -247,23 +246,24 @@ k_insert_persistent(BatchView b, HashParams hp, TableParams tp, PersistParams pp
     if (n_tasks > b.task_cap) n_tasks = b.task_cap;
     const uint64_t WT = pp.window_tasks;
     uint32_t epoch = *(volatile uint32_t*)pp.epoch_state;
+    const uint32_t cap = pp.spin_cap ? pp.spin_cap : WAIT_CAP;
     unsigned long long uniq = 0, occ = 0;
     bool ok = true;
     for (uint64_t t0 = 0; t0 < n_tasks && ok; t0 += WT) {
         const uint64_t t1 = min(n_tasks, t0 + WT);
         if (++epoch > 127) {
             for (uint64_t i = tid; i <= pp.claims_mask; i += n_threads) pp.claims[i] = 0;
-            if (!grid_barrier(pp.bar, pp.err)) { ok = false; break; }
+            if (!grid_barrier(pp.bar, pp.err, cap)) { ok = false; break; }
             epoch = 1;
         }
         const uint64_t r0 = __ldg(b.task_read + t0);
         const uint64_t gws = __ldg(b.kofs + r0) + (t0 - __ldg(b.tofs + r0)) * TASK_KMERS;
         for (uint64_t t = t0 + warp; t < t1; t += n_warps)
             probe_task<STORAGE, CANON, NT>(b, hp, tp, pp, t, gws, epoch, occ);
-        if (!grid_barrier(pp.bar, pp.err)) { ok = false; break; }
+        if (!grid_barrier(pp.bar, pp.err, cap)) { ok = false; break; }
         for (uint64_t t = t0 + warp; t < t1; t += n_warps)
             commit_task<STORAGE, CANON, NT>(b, hp, tp, pp, t, gws, epoch, uniq);
-        if (!grid_barrier(pp.bar, pp.err)) { ok = false; break; }
+        if (!grid_barrier(pp.bar, pp.err, cap)) { ok = false; break; }
     }
     uniq = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)uniq);
     occ = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)occ);
@@ -271,7 +271,12 @@ k_insert_persistent(BatchView b, HashParams hp, TableParams tp, PersistParams pp
         if (uniq) atomicAdd(pp.counters + 0, uniq);
         if (occ) atomicAdd(pp.counters + 1, occ);
     }
-    if (ok && blockIdx.x == 0 && threadIdx.x == 0) *pp.epoch_state = epoch;
+    if (threadIdx.x == 0) {
+        // an aborted run leaves claims of epochs the next run would reuse:
+        // epoch 127 makes the next run clear the map before its first window
+        if (!ok) atomicExch(pp.epoch_state, 127u);
+        else if (blockIdx.x == 0) atomicExch(pp.epoch_state, epoch);
+    }
 }
 
 }  // namespace gdbg

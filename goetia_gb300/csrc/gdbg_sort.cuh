@@ -68,10 +68,32 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for a barrier phase; false when the poll limit runs out.
+// Bounded wait for a barrier phase; false when WAIT_CAP polls run out.  The
+// last wait for copies still in flight before a block gives up always takes
+// this limit, so no block leaves with a copy still writing its shared memory.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t it = 0; it < (1u << 24); ++it)
+    for (uint32_t it = 0; it < WAIT_CAP; ++it)
         if (mbar_try(bar, parity)) return true;
+    return false;
+}
+// Non-blocking test of a barrier phase.
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// First wait on a bulk copy: WAIT_CAP blocking polls, or, when the handle set
+// a limit (SortParams::wait_cap), that many non-blocking tests, so a small
+// limit runs out within nanoseconds of the copy's issue.
+__device__ __forceinline__ bool copy_wait(const SortParams& sp, uint64_t* bar, uint32_t parity) {
+    if (sp.wait_cap == 0) return mbar_wait(bar, parity);
+    for (uint32_t it = 0; it < sp.wait_cap; ++it)
+        if (mbar_test(bar, parity)) return true;
     return false;
 }
 // Global -> shared bulk copy; both addresses 16-byte aligned, bytes a
@@ -442,7 +464,7 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
         const uint32_t ts = rs + i * SP_TILE;
         const uint32_t nt = re - ts < SP_TILE ? re - ts : SP_TILE;
         const uint64_t* src = inbuf + (i % SP_NBUF) * SP_BUF + (ts & 1u);
-        if (!mbar_wait(&bars[i % SP_NBUF], (i / SP_NBUF) & 1u)) atomicExch(&abort_s, 1u);
+        if (!copy_wait(sp, &bars[i % SP_NBUF], (i / SP_NBUF) & 1u)) atomicExch(&abort_s, 1u);
         // also orders the previous tile's reads of stage / delta before this
         // tile's writes
         __syncthreads();
@@ -686,7 +708,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
     for (uint32_t k = threadIdx.x; k < SP_MAPCAP / 32; k += SP_APPLY_BLOCK) used[k] = 0;
     __syncthreads();   // the barrier is initialised before anyone waits on it
-    if (!mbar_wait(&bar, phase & 1u)) atomicExch(&abort_s, 1u);
+    if (!copy_wait(sp, &bar, phase & 1u)) atomicExch(&abort_s, 1u);
     ++phase;
     __syncthreads();
     if (abort_s) {
@@ -758,7 +780,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 chunk_copy(c, false);
             }
-            if (!mbar_wait(&bar, phase & 1u)) atomicExch(&abort_s, 1u);
+            if (!copy_wait(sp, &bar, phase & 1u)) atomicExch(&abort_s, 1u);
             ++phase;
             __syncthreads();
             loaded = c;

@@ -8,6 +8,10 @@ namespace gdbg {
 
 constexpr int MAX_TABLES = 32;
 
+// Default poll limit of every bounded device wait (grid barrier, bulk-copy
+// mbarrier): about a second or two of polling.
+constexpr uint32_t WAIT_CAP = 1u << 24;
+
 // Error bits accumulated in a device status word and surfaced by the C ABI.
 enum : uint32_t {
     GDBG_ERR_CAS_LIMIT = 1u,      // a saturating compare-and-swap loop hit its cap
@@ -115,6 +119,7 @@ struct SortParams {
     uint32_t* off2;               // its exclusive scan
     uint32_t* plan;               // s0[bins1 + 1] then G[bins1 + 1]
     uint32_t* err;                // device status word
+    uint32_t wait_cap;            // polls of a bulk-copy wait before giving up (0: WAIT_CAP)
 };
 
 // Persistent batch insert (gdbg_persist.cuh).
@@ -129,6 +134,7 @@ struct PersistParams {
     unsigned long long* counters; // [0] n_unique, [1] n_occupied
     uint32_t* err;
     unsigned int* bar;            // [0] arrivals, [1] generation
+    uint32_t spin_cap;            // polls of a grid-barrier wait before giving up (0: WAIT_CAP)
 };
 
 }  // namespace gdbg

@@ -748,6 +748,13 @@ class dBGBase:
         _lib.call("gdbg_device_status", self._h, _c.byref(s))
         return int(s.value)
 
+    def set_wait_limits(self, barrier_polls=0, copy_polls=0):
+        """Poll limits of the bounded device waits (0 = default, 2^24): the
+        persistent insert's grid barrier and the bucketed insert's first wait
+        on each bulk copy.  A wait that runs out ends its kernel early and the
+        next synchronising call raises GoetiaError (GDBG_ERR_DEVICE)."""
+        _lib.call("gdbg_set_wait_limits", self._h, int(barrier_polls), int(copy_polls))
+
     def reserve(self, max_reads, max_kmers):
         """Grow the insert scratch for batches up to this size now."""
         _lib.call("gdbg_reserve", self._h, int(max_reads), int(max_kmers))

@@ -42,11 +42,28 @@ def sample_reads(g, n_reads, length, sub_rate, seed, rc_frac=0.5):
     return rows
 
 
-def rows_to_packed(rows):
+def pack_codes_np(codes):
+    """uint8 codes (A=0 C=1 G=2 T=3) -> uint32 packed stream in numpy alone
+    (the same words as reads.pack_codes: base j in bits 2*(j%16) of word
+    j/16, len(codes)//16 + 1 words, zero-padded).  Four codes make a byte,
+    four bytes a little-endian word."""
+    codes = np.ascontiguousarray(codes, np.uint8)
+    n = len(codes)
+    buf = np.zeros((n // 16 + 1) * 16, np.uint8)
+    buf[:n] = codes
+    q = buf.reshape(-1, 4)
+    b = q[:, 0] | (q[:, 1] << 2) | (q[:, 2] << 4) | (q[:, 3] << 6)
+    return b.view("<u4").astype(np.uint32, copy=False)
+
+
+def rows_to_packed(rows, native=True):
+    """Equal-length code rows -> PackedReads.  native=False packs with numpy
+    alone, so the caller never loads the GPU library."""
     rows = np.ascontiguousarray(rows, np.uint8)
     n, L = rows.shape
     offsets = np.arange(n + 1, dtype=np.uint64) * np.uint64(L)
-    return PackedReads(pack_codes(rows.reshape(-1)), offsets, 0)
+    flat = rows.reshape(-1)
+    return PackedReads(pack_codes(flat) if native else pack_codes_np(flat), offsets, 0)
 
 
 def n_read_mask(n_reads, frac, seed):

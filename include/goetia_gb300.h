@@ -299,6 +299,17 @@ int gdbg_get_insert_schedule(const gdbg_graph* g, uint32_t* window_kmers,
                              uint32_t* kmers_per_thread);
 /* Device status word (GDBG_ERR_* device bits); cleared by reading. */
 int gdbg_device_status(gdbg_graph* g, uint32_t* status);
+/* Poll limits of the bounded device waits on this handle: barrier_polls for
+ * a grid-barrier wait of the PERSISTENT insert, copy_polls for the first wait
+ * on each shared-memory bulk copy of the BUCKETED insert (0 = the default,
+ * 2^24 polls, a second or two).  A wait that runs out sets a device status
+ * bit (4 = barrier timeout, 16 = bulk-copy timeout), its kernel returns
+ * without finishing the batch, and the next synchronising call reports
+ * GDBG_ERR_DEVICE; the tables are then partly updated (gdbg_reset clears
+ * them).  Before a block gives up it still waits, with the default limit,
+ * for its own copies in flight.  A diagnostic with no counterpart in the
+ * reference: it lets a test drive those error paths without a GPU fault. */
+int gdbg_set_wait_limits(gdbg_graph* g, uint32_t barrier_polls, uint32_t copy_polls);
 /* Grow the graph's batch and windowed-insert scratch for batches of up to
  * max_reads reads and max_kmers k-mers now, so later inserts within that
  * size allocate nothing. */
@@ -346,9 +357,17 @@ int gdbg_noalloc_table_layout(int storage, const uint64_t* sizes, uint16_t n_tab
  * The first call on a device looks the array up and clears it: make that
  * call before any stream capture.  Calls share the array; calls that overlap
  * on the GPU race and must be serialised by the caller.  n_new (device, one
- * uint64 per read) may be NULL.  stats (device, 3 x uint64) may be NULL; it
- * receives the call's n_unique and n_occupied increments and the device
- * status bits (non-zero = a device-side check failed). */
+ * uint64 per read) may be NULL.  stats (device, 3 x uint64) receives the
+ * call's n_unique and n_occupied increments and the device status bits
+ * (non-zero = a device-side check failed: 1 CAS cap, 2 claims map full,
+ * 4 barrier timeout, 8 bad read offsets); the call then returns at once.
+ * With stats NULL the call waits for the insert on `stream` and returns
+ * GDBG_ERR_DEVICE when a device-side check failed, so no failure goes
+ * unreported.  Offsets are checked on the device, as by
+ * gdbg_insert_batch_device: a read whose offsets decrease or run past
+ * 16*packed_words counts as zero k-mers, the batch's other reads are still
+ * inserted, and status bit 8 reports it (gdbg_insert_batch, with host
+ * buffers, rejects such a batch before touching any table). */
 int gdbg_insert_batch_noalloc(int storage, int shifter, uint16_t K, const uint64_t* sizes,
                               uint16_t n_tables, uint32_t* tables, const uint32_t* packed,
                               uint64_t packed_words, const uint64_t* offsets, uint64_t n_reads,

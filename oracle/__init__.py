@@ -133,6 +133,12 @@ class Storage:
             out.append(np.ctypeslib.as_array(L.orc_table(self.h, i), shape=(n,)).copy())
         return out
 
+    def table_view(self, i):
+        """Table i's bytes without a copy (valid while the storage lives)."""
+        L = lib()
+        n = L.orc_table_bytes(self.h, i)
+        return np.ctypeslib.as_array(L.orc_table(self.h, i), shape=(n,))
+
     def stats(self):
         u, o = ctypes.c_uint64(), ctypes.c_uint64()
         lib().orc_stats(self.h, ctypes.byref(u), ctypes.byref(o))

@@ -85,6 +85,20 @@ def test_pack_codes_layout():
     assert np.array_equal((p[j >> 4] >> (2 * (j & 15)).astype(np.uint32)) & 3, c)
 
 
+def test_numpy_packer_equals_library_packer():
+    """synth.pack_codes_np (numpy alone, for runs that must not load the GPU
+    library) gives the library packer's words, padding included."""
+    from goetia_gb300 import synth
+    rng = np.random.default_rng(5)
+    for n in (0, 1, 15, 16, 17, 33, 1000, 150 * 1001):
+        c = rng.integers(0, 4, n, dtype=np.uint8)
+        a, b = synth.pack_codes_np(c), reads.pack_codes(c)
+        assert a.dtype == np.uint32 and np.array_equal(a, b)
+    rows = rng.integers(0, 4, (300, 150), dtype=np.uint8)
+    pa, pb = synth.rows_to_packed(rows, native=False), synth.rows_to_packed(rows)
+    assert np.array_equal(pa.packed, pb.packed) and np.array_equal(pa.offsets, pb.offsets)
+
+
 def test_from_codes_and_kmer_count():
     rng = np.random.default_rng(9)
     rows = [rng.integers(0, 4, L, dtype=np.uint8) for L in (0, 5, 31, 32, 150)]
