@@ -222,45 +222,94 @@ def cpu_baseline_port(batches, sample_reads, threads):
 
 
 def run_serving(args, check_streams=3):
-    """Config 5 shape: 64 streams, each its own dBG<BitStorage, CanLemireShifter>
-    (K=31, 4 tables of 2^24-2^28 bits, log-uniform per stream), 150 bp reads
-    with 1% errors arriving as 8-4096-read chunks on Poisson timing.  Stream
-    sizes are the configuration's 10k-5M reads scaled by args.serve_scale to
-    bound the run.  Per-chunk new counts of a few streams are checked against
-    a sequential replay."""
-    import numpy as np
+    """Config 5: 64 streams, each its own dBG<BitStorage, CanLemireShifter>
+    (K=31, 4 tables of 2^24-2^28 bits, log-uniform per stream), stream sizes
+    log-uniform in 10k-5M reads of 150 bp (times args.serve_scale, 1 by
+    default) with 1% substitutions, arriving as 8-4096-read chunks on Poisson
+    timing.  One full run at a mean gap of args.serve_gap per stream, then a
+    sweep of arrival rates over a time window of the same streams
+    (args.serve_window seconds of arrivals per rate), reporting p50/p99 chunk
+    latency and aggregate k-mers/s at each; the capacity point is the highest
+    swept rate whose p99 stays under 5 ms.  The check (run later) replays
+    streams of the full run sequentially on the GPU and the smallest one on
+    the oracle, chunk by chunk."""
     import goetia_gb300 as G
     from goetia_gb300 import serving
     sc = args.serve_scale
-    specs = serving.make_streams(args.serve_streams, 17, reads_lo=max(8, int(10_000 * sc)),
-                                 reads_hi=max(16, int(5_000_000 * sc)), chunk_lo=8, chunk_hi=4096,
-                                 table_lo_bits=24, table_hi_bits=28, mean_gap_s=args.serve_gap,
-                                 genome_len=2_000_000)
-    srv = serving.Server(G.BitStorage, G.CanLemireShifter, K=31, n_tables=4,
-                         hbm_budget=int(args.serve_budget_gb * (1 << 30)), depth=4)
-    results, stats = srv.run(specs)
-    exact = True
-    for spec in specs[:check_streams]:
-        want = serving.replay(spec)
-        exact &= all(np.array_equal(r.n_new, w) for r, w in zip(results[spec.sid], want))
-    offered = sum(s.n_kmers(31) for s in specs)
-    return {
+    cache = {}
+
+    def specs_for(gap, window=None):
+        return serving.make_streams(args.serve_streams, 17, reads_lo=max(8, int(10_000 * sc)),
+                                    reads_hi=max(16, int(5_000_000 * sc)), chunk_lo=8,
+                                    chunk_hi=4096, table_lo_bits=24, table_hi_bits=28,
+                                    mean_gap_s=gap, genome_len=2_000_000, max_arrival_s=window,
+                                    reads_cache=cache)
+
+    def serve(specs):
+        srv = serving.Server(G.BitStorage, G.CanLemireShifter, K=31, n_tables=4,
+                             hbm_budget=int(args.serve_budget_gb * (1 << 30)), depth=4)
+        return srv.run(specs)
+
+    t0 = time.perf_counter()
+    specs = specs_for(args.serve_gap)
+    gen_s = time.perf_counter() - t0
+    results, stats = serve(specs)
+    offered = sum(sp.n_kmers(31) for sp in specs)
+    sweep = []
+    for gap in args.serve_sweep_gaps:
+        sw_specs = specs_for(gap, args.serve_window)
+        _, st = serve(sw_specs)
+        sweep.append({"mean_gap_ms": gap * 1e3,
+                      "offered_kmers_per_s": sum(sp.n_kmers(31) for sp in sw_specs) / args.serve_window,
+                      "kmers_per_s": st["kmers_per_s"], "p50_ms": st["p50_ms"],
+                      "p99_ms": st["p99_ms"], "chunks": st["chunks"]})
+        del sw_specs
+    ok = [x for x in sweep if x["p99_ms"] < 5.0]
+    capacity = max(ok, key=lambda x: x["kmers_per_s"]) if ok else None
+    out = {
         "streams": len(specs), "chunks": stats["chunks"],
+        "reads": sum(sum(c.n_reads for c in sp.chunks) for sp in specs),
         "p50_chunk_latency_ms": stats["p50_ms"], "p99_chunk_latency_ms": stats["p99_ms"],
         "max_chunk_latency_ms": stats["max_ms"],
         "kmers_per_s": stats["kmers_per_s"], "kmers": stats["kmers"],
         "wall_s": stats["wall_s"], "offered_kmers": offered,
         "peak_hbm_GB": stats["peak_hbm_bytes"] / (1 << 30),
-        "admission_waits": stats["admission_waits"],
-        "lazy_frees": stats["lazy_frees"],
+        "admission_waits": stats["admission_waits"], "lazy_frees": stats["lazy_frees"],
         "host": {k: stats[k] for k in ("admit_ms_max", "admit_ms_total", "dispatch_ms_p99",
                                        "dispatch_delay_ms_p99")},
         "hbm_budget_GB": args.serve_budget_gb,
-        "exact_vs_sequential_replay": bool(exact), "replay_checked_streams": check_streams,
+        "rate_sweep": sweep,
+        "capacity_at_p99_under_5ms": capacity,
+        "generator_seconds": gen_s,
         "workload": (f"64 streams, reads 10k-5M x {sc} log-uniform, chunks 8-4096 reads, "
                      f"Poisson mean gap {args.serve_gap * 1e3:.1f} ms per stream, "
-                     "Bit 4 x 2^24-2^28 bits per stream"),
+                     "Bit 4 x 2^24-2^28 bits per stream; sweep: "
+                     f"{args.serve_window:.1f} s of arrivals per rate"),
     }
+    by_size = sorted(specs, key=lambda sp: sum(c.n_reads for c in sp.chunks))
+    replay_specs = [by_size[0], by_size[len(by_size) // 2], by_size[-1]][:check_streams]
+    oracle_spec = by_size[0]
+    served = {sp.sid: results[sp.sid] for sp in replay_specs + [oracle_spec]}
+    del results, specs
+
+    def check(threads):
+        import oracle
+        exact = True
+        for sp in replay_specs:
+            want = serving.replay(sp)
+            exact &= all(np.array_equal(r.n_new, w) for r, w in zip(served[sp.sid], want))
+        sizes = G.BitStorage.build(oracle_spec.max_table, 4).get_tablesizes()
+        ref = oracle.Storage("bit", sizes)
+        ok_or = True
+        for r, c in zip(served[oracle_spec.sid], oracle_spec.chunks):
+            _, want = ref.insert_reads(True, 31, c.packed, c.offsets)
+            ok_or &= bool(np.array_equal(r.n_new, want))
+        return {"exact_vs_sequential_replay": bool(exact),
+                "replay_streams": [sum(c.n_reads for c in sp.chunks) for sp in replay_specs],
+                "exact_vs_oracle": bool(ok_or),
+                "oracle_stream_reads": sum(c.n_reads for c in oracle_spec.chunks)}
+
+    return out, check
 
 
 def masks_setup(n_reads):
@@ -338,14 +387,33 @@ def run_masks(args, check_reads=2000):
     masks = d_m.cpu().numpy()
     lo = np.unpackbits((masks & 15)[:, None], axis=1).sum(1)
     hi = np.unpackbits((masks >> 4)[:, None], axis=1).sum(1)
-    # bit-exact check of a sample against the oracle's walker on the same tables
-    ref = oracle.Storage("bit", storage.get_tablesizes())
-    sub_off = pr.offsets[:check_reads + 1].copy()
-    for hap in (a, b):
-        t = synth.tiles_of(hap, 100_000, K)
-        ref.insert_reads(True, K, t.packed, t.offsets)
-    want = ref.decision_masks(True, K, pr.packed, sub_off)
-    exact = bool(np.array_equal(masks[:len(want)], want))
+    sizes = storage.get_tablesizes()
+    # the query reads are spread over the two haplotypes: check the first
+    # reads of each half
+    half = pr.n_reads // 2
+    kofs = np.zeros(pr.n_reads + 1, np.int64)
+    kofs[1:] = np.cumsum(np.maximum(np.diff(pr.offsets.astype(np.int64)) - (K - 1), 0))
+    picks = [(0, min(check_reads // 2, half)), (half, half + min(check_reads // 2, pr.n_reads - half))]
+    got = [masks[kofs[r0]:kofs[r1]].copy() for r0, r1 in picks]
+    del d_m, d_p, d_o, g
+
+    def check(threads):
+        # bit-exact check of samples against the oracle's walker on tables
+        # built from the same tiles
+        ref = oracle.Storage("bit", sizes)
+        for hap in (a, b):
+            t = synth.tiles_of(hap, 100_000, K)
+            ref.insert_reads(True, K, t.packed, t.offsets)
+        ok = True
+        for (r0, r1), gm in zip(picks, got):
+            b0 = int(pr.offsets[r0])
+            w0 = b0 // 16
+            sub_off = (pr.offsets[r0:r1 + 1] - np.uint64(16 * w0)).astype(np.uint64)
+            want = ref.decision_masks(True, K, np.ascontiguousarray(pr.packed[w0:]), sub_off)
+            ok &= bool(np.array_equal(gm, want))
+        return {"exact_vs_oracle": ok,
+                "checked": f"neighbour masks of {sum(r1 - r0 for r0, r1 in picks)} query reads "
+                           "(the first of each haplotype's half) against the oracle's walker"}
     peak, peak_kind = measured_peak()
     tpk = profile_traffic_per_kmer("decision_masks_bit_k31_ncu.md")
     roof = None
@@ -359,75 +427,132 @@ def run_masks(args, check_reads=2000):
                 "probes_per_kmer": "32 counted (8 neighbours x 4 tables); 15.6 sectors loaded"}
     return {"kmers_per_s": nk / dt, "ms_per_pass": dt * 1e3, "kmers": nk,
             "decision_kmers": int(((lo > 1) | (hi > 1)).sum()), "roofline": roof,
-            "exact_vs_oracle_sample": exact, "oracle_sample_reads": check_reads,
             "workload": f"{n} reads x 150 bp vs Bit 4 x ~2^28 bits built from a 20 Mbp "
-                        "genome + 2,000 1-5 kb repeats + 0.1% SNP haplotype"}
+                        "genome + 2,000 1-5 kb repeats + 0.1% SNP haplotype"}, check
 
 
-def run_batched(args, check_reads=300):
-    """Config 3 shape: uneven-length batched insert into
+def run_batched(args, check_reads=2000, later_batch=4, cell_width=1 << 20):
+    """Config 3: uneven-length batched insert into
     dBG<NibbleStorage, FwdLemireShifter>, K=21, 4 tables of ~2^28 cells.
-    Reads: log-normal lengths (median 4 kb, clipped 200 bp-60 kb) from 5
+    Reads: args.batched_reads (the configuration's 2M by default) with
+    log-normal lengths (median 4 kb, sigma 1, clipped 200 bp-60 kb) from 5
     random 10 Mbp genomes at abundances 1:2:4:8:16, 4% substitutions, 2%
-    insertions, 2% deletions; args.batched_reads of the configuration's 2M
-    reads.  Batches are replayed through a CUDA graph with the autotuned
-    capacity and schedule; the plain per-read call is timed on a sample of
-    the same reads."""
-    import numpy as np
+    insertions, 2% deletions, made by the multi-threaded generator before the
+    timed region.  The whole stream goes through BatchedInserter.insert_stream:
+    capacity-sized batches replayed from one captured CUDA graph with the
+    autotuned capacity and schedule, the host staging of the next batch
+    overlapped with the current one; wall clock around the whole stream.  The
+    plain per-read call is timed on 40 of the same reads.
+
+    Returns (stats, check): `check` runs the oracle comparisons later (they
+    take the host cores): the first check_reads reads from empty tables, the
+    first check_reads reads of batch `later_batch` after an oracle fed the
+    batches before it, and the final value of cell_width cells of tables 0
+    and 3 after the whole stream (min(15, the oracle's touch count))."""
     import goetia_gb300 as G
-    import oracle
     from goetia_gb300 import batched, synth
+    import torch
     K = 21
     gens = [synth.genome(10_000_000, 5 + i) for i in range(5)]
-    parts = []
-    per = 8000
-    for i in range(0, args.batched_reads, per):
-        parts.append(synth.uneven_batch(gens, [1, 2, 4, 8, 16], min(per, args.batched_reads - i),
-                                        4000, 1.0, 200, 60_000, 0.04, 0.02, 0.02, 10 + i))
-    from goetia_gb300.reads import concat
-    reads = concat(parts)
+    t0 = time.perf_counter()
+    reads = synth.uneven_stream(gens, [1, 2, 4, 8, 16], args.batched_reads, 4000, 1.0, 200, 60_000,
+                                0.04, 0.02, 0.02, 10)
+    gen_s = time.perf_counter() - t0
     nk = reads.n_kmers(K)
     storage = G.NibbleStorage.build(1 << 28, 4)
     g = G.dBG[G.NibbleStorage, G.FwdLemireShifter].build(storage, K)
-    caps = [(2048, 16 << 20), (8192, 64 << 20), (16384, 128 << 20)]
+    caps = [(8192, 64 << 20), (16384, 128 << 20), (32768, 256 << 20)]
     cap, tuned = batched.autotune_capacity(g, reads, caps)
     ins = batched.BatchedInserter(g, cap[0], cap[1], use_graph=True).prepare()
     bat = batched.split_batches(reads, cap[0], cap[1])
-    import torch
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    n_new = ins.insert_stream(reads)   # the same batches, host staging overlapped
+    n_new = ins.insert_stream(reads)   # host staging of the next batch overlapped
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    # exactness: the first reads against the oracle from empty tables
-    first = bat[0][1]
-    sub = G.PackedReads(first.packed, first.offsets[:min(check_reads, first.n_reads) + 1].copy())
-    ref = oracle.Storage("nibble", storage.get_tablesizes())
-    _, want = ref.insert_reads(False, K, sub.packed, sub.offsets)
-    exact = bool(np.array_equal(n_new[:sub.n_reads], want))
+    g.synchronize()
+    sizes = storage.get_tablesizes()
+    # the GPU's final cells of tables 0 and 3 in the checked ranges
+    raw = g.get_raw()
+    lo = [sizes[0] // 2, sizes[3] // 3]
+    gpu_cells = []
+    for ti, l in zip((0, 3), lo):
+        c = np.arange(l, l + cell_width, dtype=np.int64)
+        b = raw[ti][c // 2]
+        gpu_cells.append(np.where(c % 2 == 0, b >> 4, b & 15).astype(np.uint8))
+    del raw
+    lb = min(later_batch, len(bat) - 1)
+
     # plain: one insert_sequence call per read on a fresh graph
     gp = g.clone()
     from goetia_gb300.reads import codes_to_str
-    sample = []
-    j_all = np.arange(int(first.offsets[min(40, first.n_reads)]))
+    first = bat[0][1]
+    n_plain = min(40, first.n_reads)
+    j_all = np.arange(int(first.offsets[n_plain]))
     codes = ((first.packed[j_all >> 4] >> (2 * (j_all & 15)).astype(np.uint32)) & 3).astype(np.uint8)
-    for r in range(min(40, first.n_reads)):
-        sample.append(codes_to_str(codes[int(first.offsets[r]):int(first.offsets[r + 1])]).encode())
+    sample = [codes_to_str(codes[int(first.offsets[r]):int(first.offsets[r + 1])]).encode()
+              for r in range(n_plain)]
     gp.insert_sequence(sample[0])
-    t0 = time.perf_counter()
+    t1 = time.perf_counter()
     pk = 0
     for sq in sample[1:]:
         pk += gp.insert_sequence(sq)
-    plain = pk / (time.perf_counter() - t0)
-    return {"kmers_per_s": nk / dt, "kmers": nk, "reads": reads.n_reads, "seconds": dt,
-            "batches": len(bat), "capacity_reads_bases": list(cap),
-            "schedule": tuned["schedule"], "cuda_graph": ins.cuda_graph is not None,
-            "autotune_trials_ms": [{**t["schedule"], "ms": round(1e3 * t["seconds"], 3)}
-                                   for t in tuned.get("trials", [])],
-            "plain_kmers_per_s": plain, "batched_over_plain": (nk / dt) / plain,
-            "exact_vs_oracle_first_reads": exact, "oracle_checked_reads": sub.n_reads,
-            "workload": f"{reads.n_reads} of the 2M uneven reads (median 4 kb, 200 bp-60 kb), "
-                        "5 x 10 Mbp genomes 1:2:4:8:16, 8% errors; Nibble 4 x ~2^28 cells, K=21"}
+    plain = pk / (time.perf_counter() - t1)
+    del gp
+    peak, peak_kind = measured_peak()
+    achieved = nk / dt * BYTES_PER_KMER / 1e9
+    stats = {"kmers_per_s": nk / dt, "kmers": nk, "reads": reads.n_reads, "bases": reads.n_bases,
+             "seconds": dt, "batches": len(bat), "capacity_reads_bases": list(cap),
+             "schedule": tuned["schedule"], "cuda_graph": ins.cuda_graph is not None,
+             "autotune_trials_ms": [{**t["schedule"], "ms": round(1e3 * t["seconds"], 3)}
+                                    for t in tuned.get("trials", [])],
+             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                          "frac": achieved / peak, "algorithmic_bytes_per_kmer": BYTES_PER_KMER,
+                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+             "generator_seconds": gen_s,
+             "plain_kmers_per_s": plain, "batched_over_plain": (nk / dt) / plain,
+             "workload": f"{reads.n_reads} uneven reads (log-normal, median 4 kb, sigma 1, "
+                         "200 bp-60 kb), 5 x 10 Mbp genomes 1:2:4:8:16, 4% sub / 2% ins / 2% del; "
+                         "Nibble 4 x ~2^28 cells, FwdLemireShifter, K=21"}
+    del ins, g
+
+    def check(threads):
+        import oracle
+        t = time.perf_counter()
+        out = {}
+        # (1) the first reads from empty tables, in batch order
+        b0 = bat[0][1]
+        sub = G.PackedReads(b0.packed, b0.offsets[:min(check_reads, b0.n_reads) + 1].copy())
+        ref = oracle.Storage("nibble", sizes)
+        _, want = ref.insert_reads(False, K, sub.packed, sub.offsets)
+        out["first_reads_new_counts_equal"] = bool(np.array_equal(n_new[:sub.n_reads], want))
+        # (2) reads of a later batch after the oracle took the batches before it
+        #     (final cells do not depend on order: multi-threaded), then the
+        #     checked reads in order
+        ref = oracle.Storage("nibble", sizes)
+        for r0, b in bat[:lb]:
+            ref.insert_reads_mt(False, K, b.packed, b.offsets, threads)
+        r0, b = bat[lb]
+        sub = G.PackedReads(b.packed, b.offsets[:min(check_reads, b.n_reads) + 1].copy())
+        _, want = ref.insert_reads(False, K, sub.packed, sub.offsets)
+        out["later_batch_new_counts_equal"] = bool(np.array_equal(n_new[r0:r0 + sub.n_reads], want))
+        del ref
+        # (3) final cells after the whole stream
+        cnt = oracle.count_cells(False, K, reads.packed, reads.offsets, sizes, [0, 3], lo,
+                                 cell_width, threads=threads)
+        out["final_cells_equal"] = bool(all(np.array_equal(gpu_cells[j], np.minimum(cnt[j], 15))
+                                            for j in range(2)))
+        out["exact_vs_oracle"] = bool(out["first_reads_new_counts_equal"] and
+                                      out["later_batch_new_counts_equal"] and
+                                      out["final_cells_equal"])
+        out["checked"] = (f"per-read new counts of the first {check_reads} reads (empty tables) "
+                          f"and of the first {check_reads} reads of batch {lb} (oracle fed "
+                          f"batches 0-{lb - 1}); final values of {cell_width} cells of tables "
+                          f"0 and 3 after all {reads.n_reads} reads")
+        out["seconds"] = time.perf_counter() - t
+        return out
+
+    return stats, check
 
 
 def run_profile_case(args):
@@ -491,6 +616,30 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_checks(checks):
+    """Run the legs' oracle checks side by side on the host cores (ctypes
+    releases the GIL); each gets a share of the threads.  Returns
+    {leg: result}; a check that raises reports the error, never hides it."""
+    out = {}
+    if not checks:
+        return out
+    cores = max(1, (os.cpu_count() or 2) - 1)
+    share = max(1, cores // len(checks))
+
+    def run(name, fn):
+        try:
+            out[name] = fn(share)
+        except Exception as e:
+            out[name] = {"exact_vs_oracle": False, "error": repr(e)}
+
+    th = [threading.Thread(target=run, args=kv, daemon=True) for kv in checks.items()]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    return out
 
 
 def run_gpu(args):
@@ -656,23 +805,11 @@ def run_gpu(args):
     plain_dt = time.perf_counter() - t0
     plain_value = pk / plain_dt
 
-    # bit-exact check of the timed run's end state against the oracle at the
-    # full shape, on the host cores while the other legs use the GPU
-    exact = {}
-    checker = None
+    # the timed run's end state, for the oracle check after the timed legs
+    gpu_state = None
     if rank == 0 and not args.no_oracle_check:
         gpu_state = (g.get_raw(), d_batches[-1][2].cpu().numpy().view(np.uint64)[:batches[-1].n_reads],
                      g.n_occupied())
-
-        def _check():
-            try:
-                exact.update(oracle_check_headline(batches, storage.get_tablesizes(), *gpu_state,
-                                                   max(1, (os.cpu_count() or 2) - 2)))
-            except Exception as e:   # reported in the line, never hidden
-                exact.update({"exact_vs_oracle": False, "error": repr(e)})
-
-        checker = threading.Thread(target=_check, daemon=True)
-        checker.start()
 
     peak, peak_kind = measured_peak()
     achieved = value / world * BYTES_PER_KMER / 1e9
@@ -692,30 +829,41 @@ def run_gpu(args):
         "stages_ms_per_step": {k: v[0] / max(args.steps, 1) for k, v in stages.items()},
     }
 
+    # the other configurations' legs; each returns its stats and a check that
+    # runs the oracle comparisons after every timed leg is done
+    checks = {}
     batched_stats = None
     if not args.no_batched:
-        batched_stats = run_batched(args)
+        batched_stats, checks["batched_uneven"] = run_batched(args)
     mask_stats = None
     if not args.no_masks:
-        mask_stats = run_masks(args)
-    if checker is not None:
-        checker.join()
-        del gpu_state
+        mask_stats, checks["decision_masks"] = run_masks(args)
     serving_stats = None
     if not args.no_serving:
         del g, g3
         torch.cuda.empty_cache()
-        serving_stats = run_serving(args)
-
+        serving_stats, checks["serving"] = run_serving(args)
+    if gpu_state is not None:
+        checks["headline"] = lambda threads: oracle_check_headline(
+            batches, storage.get_tablesizes(), *gpu_state, threads)
     line = None
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
+            # timed alone, before the checks take the host cores
             v, tot, cdt = cpu_baseline_port(batches, args.cpu_sample_reads, 1)
             cpu = {"value": v, "unit": "k-mers/s", "cores": 1, "kind": "port",
                    "sample": f"{min(args.cpu_sample_reads, batches[0].n_reads)} reads x "
                              f"{READ_LEN} bp of step 0 ({tot} k-mers, {cdt:.1f} s), one thread, "
                              "4 x ~2^30-cell Byte tables"}
+        exact = run_checks(checks)
+        if batched_stats is not None:
+            batched_stats["oracle_check"] = exact.get("batched_uneven")
+        if mask_stats is not None:
+            mask_stats["oracle_check"] = exact.get("decision_masks")
+        if serving_stats is not None:
+            serving_stats["oracle_check"] = exact.get("serving")
+        exact = exact.get("headline", {})
         line = {
             "metric": METRIC, "value": value, "unit": "k-mers/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
@@ -773,10 +921,15 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-oracle-check", action="store_true",
                     help="skip the oracle check of the timed run's end state")
-    ap.add_argument("--batched-reads", type=int, default=131_072)
+    ap.add_argument("--batched-reads", type=int, default=2_000_000)
     ap.add_argument("--mask-reads", type=int, default=5_000_000)
     ap.add_argument("--serve-streams", type=int, default=64)
-    ap.add_argument("--serve-scale", type=float, default=0.02)
+    ap.add_argument("--serve-scale", type=float, default=1.0)
+    ap.add_argument("--serve-window", type=float, default=3.0,
+                    help="seconds of arrivals per point of the rate sweep")
+    ap.add_argument("--serve-sweep-gaps", type=lambda v: [float(x) for x in v.split(",")],
+                    default=[0.008, 0.004, 0.002, 0.001, 0.0005],
+                    help="mean chunk gaps per stream (s) of the rate sweep")
     ap.add_argument("--serve-gap", type=float, default=0.002)
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)
     ap.add_argument("--profile-case", action="store_true",

@@ -54,8 +54,28 @@ def _compile(src, verbose):
     return obj
 
 
+WORKLOAD_SRC = os.path.join(HERE, "workload", "gen_reads.cc")
+WORKLOAD_LIB = os.path.join(HERE, "libgoetia_workload.so")
+
+
+def build_workload(verbose=False):
+    """The host-only synthetic read generator the benchmark and tests use
+    (g++, no CUDA): goetia_gb300/libgoetia_workload.so."""
+    if os.path.exists(WORKLOAD_LIB) and os.path.getmtime(WORKLOAD_LIB) >= os.path.getmtime(WORKLOAD_SRC):
+        return WORKLOAD_LIB
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O3", "-fPIC", "-shared", "-pthread",
+           "-o", WORKLOAD_LIB + ".tmp", WORKLOAD_SRC]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.check_call(cmd)
+    os.replace(WORKLOAD_LIB + ".tmp", WORKLOAD_LIB)
+    return WORKLOAD_LIB
+
+
 def build(verbose=False, jobs=None):
-    """Compile every CUDA/C++ unit for sm_103a and link the shared library."""
+    """Compile every CUDA/C++ unit for sm_103a and link the shared library
+    (and the host-only workload generator)."""
+    build_workload(verbose)
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
     with ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:

@@ -30,6 +30,16 @@ class PackedReads:
         lens = np.diff(self.offsets.astype(np.int64))
         return int(np.maximum(lens - K + 1, 0).sum())
 
+    def slice(self, r0, r1):
+        """Reads r0 .. r1-1 as a PackedReads over the same words (no copy of
+        the bases): the words from the one holding read r0's first base, the
+        offsets shifted to match."""
+        b0 = int(self.offsets[r0])
+        w0 = b0 // 16
+        w1 = (int(self.offsets[r1]) + 15) // 16 + 1
+        off = (self.offsets[r0:r1 + 1] - np.uint64(16 * w0)).astype(np.uint64)
+        return PackedReads(self.packed[w0:min(w1, len(self.packed))], off, 0)
+
 
 def _p(a, t):
     return a.ctypes.data_as(t)

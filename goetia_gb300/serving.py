@@ -295,11 +295,17 @@ def replay(spec, storage_type=D.BitStorage, shifter_type=D.CanLemireShifter, K=3
 
 def make_streams(n_streams, seed, reads_lo, reads_hi, chunk_lo, chunk_hi, table_lo_bits,
                  table_hi_bits, mean_gap_s, genome_len=2_000_000, read_len=150, sub_rate=0.01,
-                 start_spread_s=1.0):
+                 start_spread_s=1.0, max_arrival_s=None, threads=None, reads_cache=None):
     """Seeded serving workload: stream sizes log-uniform in [reads_lo, reads_hi],
     chunk sizes log-uniform in [chunk_lo, chunk_hi], table sizes log-uniform
     in [2^table_lo_bits, 2^table_hi_bits] per table, Poisson chunk arrivals
-    with mean gap mean_gap_s, stream starts uniform over start_spread_s."""
+    with mean gap mean_gap_s, stream starts uniform over start_spread_s.
+    Each stream samples its reads (either strand, i.i.d. substitutions) from
+    its own random genome with the multi-threaded generator; a chunk is a
+    view of the stream's packed reads.  max_arrival_s keeps only the chunks
+    that arrive before it (a time window of the same streams).  reads_cache
+    (a dict) keeps each stream's generated reads for later calls with the
+    same seed and sizes."""
     from . import synth
     rng = np.random.default_rng(seed)
     specs = []
@@ -308,16 +314,25 @@ def make_streams(n_streams, seed, reads_lo, reads_hi, chunk_lo, chunk_hi, table_
         n_reads = int(np.exp(rng.uniform(np.log(reads_lo), np.log(reads_hi))))
         bits = rng.uniform(table_lo_bits, table_hi_bits)
         max_table = int(2 ** bits)
-        rows = synth.sample_reads(g, n_reads, read_len, sub_rate, seed * 7919 + s)
+        key = (seed, s, n_reads, read_len, sub_rate, genome_len)
+        reads = reads_cache.get(key) if reads_cache is not None else None
+        if reads is None:
+            reads = synth.sample_reads_packed(g, n_reads, read_len, sub_rate, seed * 7919 + s,
+                                              threads=threads)
+            if reads_cache is not None:
+                reads_cache[key] = reads
         chunks, arrivals = [], []
         t = rng.uniform(0.0, start_spread_s)
         pos = 0
         while pos < n_reads:
             n = int(np.exp(rng.uniform(np.log(chunk_lo), np.log(chunk_hi))))
             n = max(1, min(n, n_reads - pos))
-            chunks.append(synth.rows_to_packed(rows[pos:pos + n]))
+            if max_arrival_s is not None and t >= max_arrival_s:
+                break
+            chunks.append(reads.slice(pos, pos + n))
             arrivals.append(t)
             t += rng.exponential(mean_gap_s)
             pos += n
-        specs.append(StreamSpec(s, max_table, chunks, arrivals))
+        if chunks:
+            specs.append(StreamSpec(s, max_table, chunks, arrivals))
     return specs

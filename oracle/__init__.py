@@ -78,6 +78,10 @@ def lib():
         L.orc_pack_ascii.argtypes = [ctypes.c_char_p, u64p, ctypes.c_uint64, ctypes.c_uint32,
                                      u32p, u64p, u64p]
         L.orc_symbol_table.argtypes = [u64p]
+        L.orc_count_cells.restype = ctypes.c_int
+        L.orc_count_cells.argtypes = [ctypes.c_int, ctypes.c_uint16, u32p, u64p, ctypes.c_uint64,
+                                      u64p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, u64p,
+                                      ctypes.c_uint64, u8p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -202,6 +206,24 @@ def hash_reads(canonical, K, packed, offsets):
     lib().orc_hash_reads(int(canonical), K, _p(packed, u32p), _p(offsets, u64p),
                          len(offsets) - 1, _p(val, u64p), _p(fw, u64p), _p(rc, u64p))
     return val[:nk], fw[:nk], rc[:nk]
+
+
+def count_cells(canonical, K, packed, offsets, sizes, tables, lo, width, out=None, threads=1):
+    """Touch counts (min 255) of cells [lo[j], lo[j] + width) of tables[j]
+    over every k-mer of the batch, added to `out` (n_sel x width uint8,
+    created when None): the final value of those cells is min(max, count)."""
+    sizes = np.ascontiguousarray(sizes, np.uint64)
+    sel = np.ascontiguousarray(tables, np.int32)
+    lo = np.ascontiguousarray(lo, np.uint64)
+    if out is None:
+        out = np.zeros((len(sel), width), np.uint8)
+    rc = lib().orc_count_cells(int(canonical), K, _p(packed, u32p), _p(offsets, u64p),
+                               len(offsets) - 1, _p(sizes, u64p),
+                               sel.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(sel),
+                               _p(lo, u64p), width, _p(out, u8p), int(threads))
+    if rc:
+        raise MemoryError("orc_count_cells failed")
+    return out
 
 
 def pack_ascii(seqs, min_length=0):

@@ -536,6 +536,72 @@ uint64_t orc_insert_reads_mt(orc_storage* s, int canonical, uint16_t K, const ui
     return total;
 }
 
+/* ---- touch counts of a cell range (the final-state check of long runs) --
+ * The final value of a cell of a saturating table is min(max, the number of
+ * k-mer inserts that hit it), whatever their order (bytestorage.cc:60-113,
+ * nibblestorage.cc:60-100 each add one up to the maximum).  This counts, for
+ * the tables listed in `tables`, the inserts that hit cells [lo[j],
+ * lo[j] + width) -- min(255, count) per cell into out[j * width + cell - lo[j]]
+ * -- over every k-mer of the batch, on n_threads threads. */
+typedef struct {
+    const uint64_t* sizes; const int* tables; int n_sel; const uint64_t* lo; uint64_t width;
+    uint8_t* cnt;
+} cc_ctx;
+static void cc_cb(void* c, uint64_t r, uint64_t p, const shifter* sh) {
+    (void)r; (void)p;   /* the read walker's callback signature */
+    cc_ctx* x = (cc_ctx*)c;
+    const uint64_t h = sh_value(sh);
+    for (int j = 0; j < x->n_sel; ++j) {
+        const uint64_t cell = h % x->sizes[x->tables[j]];
+        if (cell >= x->lo[j] && cell - x->lo[j] < x->width) {
+            uint8_t* q = &x->cnt[(uint64_t)j * x->width + (cell - x->lo[j])];
+            if (*q < 255) ++*q;
+        }
+    }
+}
+typedef struct {
+    cc_ctx c; int canonical; uint16_t K; const uint32_t* packed; const uint64_t* off;
+    uint64_t n, r0, stride;
+} cc_job;
+static void* cc_run(void* arg) {
+    cc_job* j = (cc_job*)arg;
+    walk_reads(j->canonical, j->K, j->packed, j->off, j->n, j->r0, j->stride, cc_cb, &j->c);
+    return NULL;
+}
+
+int orc_count_cells(int canonical, uint16_t K, const uint32_t* packed, const uint64_t* off,
+                    uint64_t n, const uint64_t* sizes, const int* tables, int n_sel,
+                    const uint64_t* lo, uint64_t width, uint8_t* out, int n_threads) {
+    if (n_threads < 1) n_threads = 1;
+    if (n_sel < 1 || width == 0) return 1;
+    const uint64_t cells = (uint64_t)n_sel * width;
+    pthread_t* th = (pthread_t*)calloc((size_t)n_threads, sizeof(pthread_t));
+    cc_job* jobs = (cc_job*)calloc((size_t)n_threads, sizeof(cc_job));
+    int ok = th && jobs;
+    for (int t = 0; ok && t < n_threads; ++t) {
+        uint8_t* cnt = (uint8_t*)calloc(cells, 1);
+        cc_job j = {{sizes, tables, n_sel, lo, width, cnt}, canonical, K, packed, off, n,
+                    (uint64_t)t, (uint64_t)n_threads};
+        jobs[t] = j;
+        ok = cnt != NULL;
+    }
+    if (!ok) {   /* nothing started: free what was allocated */
+        for (int t = 0; jobs && t < n_threads; ++t) free(jobs[t].c.cnt);
+        free(th); free(jobs);
+        return 2;
+    }
+    for (int t = 0; t < n_threads; ++t) pthread_create(&th[t], NULL, cc_run, &jobs[t]);
+    for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+    for (uint64_t i = 0; i < cells; ++i) {
+        unsigned v = out[i];
+        for (int t = 0; t < n_threads && v < 255; ++t) v += jobs[t].c.cnt[i];
+        out[i] = (uint8_t)(v < 255 ? v : 255);
+    }
+    for (int t = 0; t < n_threads; ++t) free(jobs[t].c.cnt);
+    free(th); free(jobs);
+    return 0;
+}
+
 /* ---- FASTX parser policy (readers.hh:150-219, alphabets.hh:41-56,107-130) */
 
 int64_t orc_pack_ascii(const char* seqs, const uint64_t* so, uint64_t n, uint32_t min_length,

@@ -76,6 +76,15 @@ uint64_t orc_insert_reads_mt(orc_storage* s, int canonical, uint16_t K,
                              const uint32_t* packed, const uint64_t* offsets,
                              uint64_t n_reads, int n_threads);
 
+/* min(255, number of inserts hitting each cell [lo[j], lo[j] + width) of
+ * table tables[j]) over every k-mer of the batch, ADDED to out (n_sel x
+ * width bytes, saturating at 255), so calls over consecutive batches
+ * accumulate.  Order independent: the final value of a saturating cell. */
+int      orc_count_cells(int canonical, uint16_t K, const uint32_t* packed,
+                         const uint64_t* offsets, uint64_t n_reads, const uint64_t* sizes,
+                         const int* tables, int n_sel, const uint64_t* lo, uint64_t width,
+                         uint8_t* out, int n_threads);
+
 /* FASTX parser policy for DNA_SIMPLE: uppercase acgt, drop any read holding
  * another symbol, drop reads shorter than min_length. */
 int64_t  orc_pack_ascii(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
