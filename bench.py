@@ -613,9 +613,20 @@ def run_reference(args):
                                    f"({total} k-mers), C restatement of the reference insert, "
                                    f"{threads} threads on one shared storage"},
         "e2e": {"value": v, "unit": "k-mers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "repo_libraries_loaded": repo_libraries_loaded(),
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def repo_libraries_loaded():
+    """Shared objects of this repository mapped into the process (Linux)."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")}
+    except OSError:
+        return []
+    return sorted(os.path.relpath(p, HERE) for p in paths if p.startswith(HERE + os.sep))
 
 
 def run_checks(checks):
