@@ -91,12 +91,14 @@ def oracle_check_headline(batches, sizes, gpu_tables, gpu_last_new, gpu_occupied
     oracle's multi-threaded insert; the last batch goes in sequentially, in
     batch order, which gives the reference's per-read new counts for it.
     Compared: those counts, all table bytes, and n_occupied (the non-zero
-    cells of table 0)."""
+    cells of table 0).  A generator: the multi-threaded insert runs up to its
+    yield, the rest when it is resumed (see run_checks)."""
     import oracle
     t0 = time.perf_counter()
     st = oracle.Storage("byte", sizes)
     for pr in batches[:-1]:
         st.insert_reads_mt(True, K, pr.packed, pr.offsets, threads)
+    yield   # the multi-threaded part is done; the rest runs on one thread
     last = batches[-1]
     _, want_new = st.insert_reads(True, K, last.packed, last.offsets)
     new_ok = bool(np.array_equal(gpu_last_new, want_new))
@@ -294,6 +296,7 @@ def run_serving(args, check_streams=3):
 
     def check(threads):
         import oracle
+        yield
         exact = True
         for sp in replay_specs:
             want = serving.replay(sp)
@@ -399,11 +402,12 @@ def run_masks(args, check_reads=2000):
 
     def check(threads):
         # bit-exact check of samples against the oracle's walker on tables
-        # built from the same tiles
+        # built from the same tiles (final Bit tables do not depend on order)
         ref = oracle.Storage("bit", sizes)
         for hap in (a, b):
             t = synth.tiles_of(hap, 100_000, K)
-            ref.insert_reads(True, K, t.packed, t.offsets)
+            ref.insert_reads_mt(True, K, t.packed, t.offsets, threads)
+        yield
         ok = True
         for (r0, r1), gm in zip(picks, got):
             b0 = int(pr.offsets[r0])
@@ -520,26 +524,29 @@ def run_batched(args, check_reads=2000, later_batch=4, cell_width=1 << 20):
         import oracle
         t = time.perf_counter()
         out = {}
+        # multi-threaded part: the batches before the later batch (final
+        # cells do not depend on order), and the touch counts of the checked
+        # cells over the whole stream
+        ref_later = oracle.Storage("nibble", sizes)
+        for r0, b in bat[:lb]:
+            ref_later.insert_reads_mt(False, K, b.packed, b.offsets, threads)
+        cnt = oracle.count_cells(False, K, reads.packed, reads.offsets, sizes, [0, 3], lo,
+                                 cell_width, threads=threads)
+        yield
         # (1) the first reads from empty tables, in batch order
         b0 = bat[0][1]
         sub = G.PackedReads(b0.packed, b0.offsets[:min(check_reads, b0.n_reads) + 1].copy())
         ref = oracle.Storage("nibble", sizes)
         _, want = ref.insert_reads(False, K, sub.packed, sub.offsets)
         out["first_reads_new_counts_equal"] = bool(np.array_equal(n_new[:sub.n_reads], want))
-        # (2) reads of a later batch after the oracle took the batches before it
-        #     (final cells do not depend on order: multi-threaded), then the
-        #     checked reads in order
-        ref = oracle.Storage("nibble", sizes)
-        for r0, b in bat[:lb]:
-            ref.insert_reads_mt(False, K, b.packed, b.offsets, threads)
+        del ref
+        # (2) the first reads of the later batch, in order, after its prefix
         r0, b = bat[lb]
         sub = G.PackedReads(b.packed, b.offsets[:min(check_reads, b.n_reads) + 1].copy())
-        _, want = ref.insert_reads(False, K, sub.packed, sub.offsets)
+        _, want = ref_later.insert_reads(False, K, sub.packed, sub.offsets)
         out["later_batch_new_counts_equal"] = bool(np.array_equal(n_new[r0:r0 + sub.n_reads], want))
-        del ref
+        del ref_later
         # (3) final cells after the whole stream
-        cnt = oracle.count_cells(False, K, reads.packed, reads.offsets, sizes, [0, 3], lo,
-                                 cell_width, threads=threads)
         out["final_cells_equal"] = bool(all(np.array_equal(gpu_cells[j], np.minimum(cnt[j], 15))
                                             for j in range(2)))
         out["exact_vs_oracle"] = bool(out["first_reads_new_counts_equal"] and
@@ -630,22 +637,34 @@ def repo_libraries_loaded():
 
 
 def run_checks(checks):
-    """Run the legs' oracle checks side by side on the host cores (ctypes
-    releases the GIL); each gets a share of the threads.  Returns
-    {leg: result}; a check that raises reports the error, never hides it."""
-    out = {}
-    if not checks:
-        return out
+    """Run the legs' oracle checks on the host cores.  Each check is a
+    generator function of a thread count: its multi-threaded part runs up to
+    its yield (one check after another, each with all cores), then the
+    single-threaded remainders run side by side (ctypes releases the GIL).
+    Returns {leg: result}; a check that raises reports the error, never hides
+    it."""
+    out, pending = {}, {}
     cores = max(1, (os.cpu_count() or 2) - 1)
-    share = max(1, cores // len(checks))
-
-    def run(name, fn):
+    for name, fn in checks.items():
         try:
-            out[name] = fn(share)
+            gen = fn(cores)
+            next(gen)
+            pending[name] = gen
+        except StopIteration as e:
+            out[name] = e.value
         except Exception as e:
             out[name] = {"exact_vs_oracle": False, "error": repr(e)}
 
-    th = [threading.Thread(target=run, args=kv, daemon=True) for kv in checks.items()]
+    def finish(name, gen):
+        try:
+            next(gen)
+            out[name] = {"exact_vs_oracle": False, "error": "check did not finish"}
+        except StopIteration as e:
+            out[name] = e.value
+        except Exception as e:
+            out[name] = {"exact_vs_oracle": False, "error": repr(e)}
+
+    th = [threading.Thread(target=finish, args=kv, daemon=True) for kv in pending.items()]
     for t in th:
         t.start()
     for t in th:

@@ -563,9 +563,38 @@ typedef struct {
     cc_ctx c; int canonical; uint16_t K; const uint32_t* packed; const uint64_t* off;
     uint64_t n, r0, stride;
 } cc_job;
+/* The same walk as walk_reads + cc_cb (hash_base, then shift_right per
+ * step), with the base reads and the roll inlined: this check hashes every
+ * k-mer of a multi-gigabase stream. */
 static void* cc_run(void* arg) {
     cc_job* j = (cc_job*)arg;
-    walk_reads(j->canonical, j->K, j->packed, j->off, j->n, j->r0, j->stride, cc_cb, &j->c);
+    const uint16_t K = j->K;
+    const unsigned myr = K % 64u;
+    uint64_t outw[4];
+    for (int c = 0; c < 4; ++c) outw[c] = rotl64(SYM[c], myr);
+    const uint32_t* pk = j->packed;
+    for (uint64_t r = j->r0; r < j->n; r += j->stride) {
+        const uint64_t b = j->off[r], L = j->off[r + 1] - j->off[r];
+        if (L < K) continue;
+        uint64_t fw = 0, rc = 0;
+        for (uint16_t i = 0; i < K; ++i) {
+            const unsigned c = (pk[(b + i) >> 4] >> (((b + i) & 15u) << 1)) & 3u;
+            fw = rotl64(fw, 1) ^ SYM[c];
+            const unsigned d = (pk[(b + K - 1 - i) >> 4] >> (((b + K - 1 - i) & 15u) << 1)) & 3u;
+            rc = rotl64(rc, 1) ^ SYM[comp((int)d)];
+        }
+        for (uint64_t i = 0;; ++i) {
+            shifter s;   /* value() of the current k-mer, as sh_value */
+            s.canonical = j->canonical; s.fw.h = fw; s.rc.h = rc;
+            cc_cb(&j->c, r, i, &s);
+            if (i + K >= L) break;
+            const unsigned out = (pk[(b + i) >> 4] >> (((b + i) & 15u) << 1)) & 3u;
+            const unsigned in = (pk[(b + i + K) >> 4] >> (((b + i + K) & 15u) << 1)) & 3u;
+            fw = rotl64(fw, 1) ^ outw[out] ^ SYM[in];                       /* update */
+            const uint64_t x = rc ^ outw[comp((int)in)] ^ SYM[comp((int)out)]; /* reverse_update */
+            rc = (x >> 1) | (x << 63);
+        }
+    }
     return NULL;
 }
 

@@ -13,7 +13,7 @@ K = 21, 27, 31, 64 (rotation by K mod 64 == 0) and 101 (K > 64), short
 reads, duplicate reads, reverse-complement reads, tiny tables (collisions)
 and homopolymers (Byte saturation at 255, Nibble at 15).
 
-    python tests/golden/make_golden.py [REF=/root/reference]
+    GOETIA_REF=<goetia checkout> python tests/golden/make_golden.py
 
 Needs the reference checkout, so it runs in the build container only; the
 fixtures it writes are committed and are all the tests read.
