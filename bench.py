@@ -248,8 +248,14 @@ def run_serving(args, check_streams=3):
                                     reads_cache=cache)
 
     def serve(specs):
-        srv = serving.Server(G.BitStorage, G.CanLemireShifter, K=31, n_tables=4,
-                             hbm_budget=int(args.serve_budget_gb * (1 << 30)), depth=4)
+        budget = int(args.serve_budget_gb * (1 << 30))
+        if args.serve_loop == "python":
+            srv = serving.Server(G.BitStorage, G.CanLemireShifter, K=31, n_tables=4,
+                                 hbm_budget=budget, depth=4)
+        else:
+            srv = serving.NativeServer(G.BitStorage, G.CanLemireShifter, K=31, n_tables=4,
+                                       hbm_budget=budget, depth=4,
+                                       dispatch_threads=args.serve_dispatch_threads)
         return srv.run(specs)
 
     t0 = time.perf_counter()
@@ -277,8 +283,9 @@ def run_serving(args, check_streams=3):
         "wall_s": stats["wall_s"], "offered_kmers": offered,
         "peak_hbm_GB": stats["peak_hbm_bytes"] / (1 << 30),
         "admission_waits": stats["admission_waits"], "lazy_frees": stats["lazy_frees"],
-        "host": {k: stats[k] for k in ("admit_ms_max", "admit_ms_total", "dispatch_ms_p99",
-                                       "dispatch_delay_ms_p99")},
+        "host": {k: v for k, v in stats.items() if k.startswith(("admit_", "dispatch_"))},
+        "loop": (f"native runtime (gdbg_server_*), {args.serve_dispatch_threads} dispatcher "
+                 "threads" if args.serve_loop == "native" else "Python loop (serving.Server)"),
         "hbm_budget_GB": args.serve_budget_gb,
         "rate_sweep": sweep,
         "capacity_at_p99_under_5ms": capacity,
@@ -955,10 +962,12 @@ def main():
     ap.add_argument("--mask-reads", type=int, default=5_000_000)
     ap.add_argument("--serve-streams", type=int, default=64)
     ap.add_argument("--serve-scale", type=float, default=1.0)
+    ap.add_argument("--serve-loop", default="native", choices=["native", "python"])
+    ap.add_argument("--serve-dispatch-threads", type=int, default=2)
     ap.add_argument("--serve-window", type=float, default=3.0,
                     help="seconds of arrivals per point of the rate sweep")
     ap.add_argument("--serve-sweep-gaps", type=lambda v: [float(x) for x in v.split(",")],
-                    default=[0.008, 0.004, 0.002, 0.001, 0.0005],
+                    default=[0.008, 0.004, 0.002, 0.001, 0.0005, 0.00025],
                     help="mean chunk gaps per stream (s) of the rate sweep")
     ap.add_argument("--serve-gap", type=float, default=0.002)
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)

@@ -87,6 +87,17 @@ SIGNATURES = {
     "gdbg_set_bucket_bits": [c_vp, c_u32],
     "gdbg_device_status": [c_vp, u32p],
     "gdbg_set_wait_limits": [c_vp, c_u32, c_u32],
+    "gdbg_server_create": [c_int, c_int, c_u16, c_u16, c_u64, c_u32, c_u32, P(c_vp)],
+    "gdbg_server_stream": [c_vp, c_u64, c_u64, c_u64, c_u64],
+    "gdbg_server_submit": [c_vp, c_u64, c_vp, c_u64, c_vp, c_u64, c_u64, ctypes.c_double, c_vp,
+                           c_u64],
+    "gdbg_server_finish": [c_vp, c_u64],
+    "gdbg_server_stream_bytes": [c_vp, c_u64, P(c_u64)],
+    "gdbg_server_start": [c_vp],
+    "gdbg_server_wait": [c_vp, ctypes.c_double],
+    "gdbg_server_poll": [c_vp, c_vp, c_vp, c_vp, c_vp, c_u64, P(c_u64)],
+    "gdbg_server_stats": [c_vp, c_vp],
+    "gdbg_server_destroy": [c_vp],
     "gdbg_noalloc_table_layout": [c_int, u64p, c_u16, u64p],
     "gdbg_insert_batch_noalloc": [c_int, c_int, c_u16, u64p, c_u16, c_vp, c_vp, c_u64, c_vp,
                                   c_u64, c_vp, c_vp, c_vp],
@@ -97,6 +108,17 @@ SIGNATURES = {
 }
 
 _lib = None
+
+
+class ServerReport(ctypes.Structure):
+    """gdbg_server_report (include/goetia_gb300.h)."""
+    _fields_ = [(n, c_u64) for n in ("chunks_submitted", "chunks_done", "chunks_failed",
+                                      "kmers_done", "streams", "streams_admitted",
+                                      "admission_waits", "lazy_frees", "peak_hbm_bytes")] + \
+               [(n, ctypes.c_double) for n in ("first_dispatch_s", "last_done_s", "admit_s_max",
+                                                "admit_s_total", "dispatch_s_max",
+                                                "dispatch_s_total")] + \
+               [("device_status", c_u32)]
 
 
 class GoetiaError(RuntimeError):
@@ -137,6 +159,8 @@ def load():
     L.gdbg_last_error.argtypes = []
     L.gdbg_version.restype = c_cp
     L.gdbg_version.argtypes = []
+    L.gdbg_server_last_error.restype = c_cp
+    L.gdbg_server_last_error.argtypes = [c_vp]
     _lib = L
     return L
 

@@ -284,6 +284,113 @@ class Server:
         return results, stats
 
 
+class NativeServer:
+    """The same serving loop run by the library's native runtime
+    (gdbg_server_*): admission, dispatch and completion polling in C++
+    threads, so the per-chunk host cost is a copy into pinned staging and one
+    asynchronous insert call instead of a Python iteration.  Same run(specs)
+    contract as Server: chunks are released at their arrival times and each
+    result equals a sequential replay of its stream."""
+
+    def __init__(self, storage_type=D.BitStorage, shifter_type=D.CanLemireShifter, K=31,
+                 n_tables=4, hbm_budget=16 << 30, depth=4, dispatch_threads=2, device=0):
+        import torch
+        self.torch = torch
+        self.device = device
+        self.kinds = (storage_type.kind, shifter_type.kind)
+        self.K = K
+        self.n_tables = n_tables
+        self.budget = hbm_budget
+        self.depth = depth
+        self.dispatch_threads = dispatch_threads
+
+    def footprints(self, specs):
+        """The native runtime's HBM budget share of each stream (bytes)."""
+        import ctypes
+        from . import _lib
+        h = ctypes.c_void_p()
+        _lib.call("gdbg_server_create", self.kinds[0], self.kinds[1], self.K, self.n_tables,
+                  (1 << 63), self.depth, 1, ctypes.byref(h))
+        try:
+            out = []
+            for spec in specs:
+                _lib.call("gdbg_server_stream", h, spec.sid, spec.max_table,
+                          max(c.n_reads for c in spec.chunks),
+                          max(c.packed.size for c in spec.chunks))
+                b = ctypes.c_uint64()
+                _lib.call("gdbg_server_stream_bytes", h, spec.sid, ctypes.byref(b))
+                out.append(int(b.value))
+            return out
+        finally:
+            _lib.call("gdbg_server_destroy", h)
+
+    def run(self, specs, max_seconds=600.0):
+        import ctypes
+        from . import _lib
+        self.torch.cuda.set_device(self.device)
+        h = ctypes.c_void_p()
+        _lib.call("gdbg_server_create", self.kinds[0], self.kinds[1], self.K, self.n_tables,
+                  int(self.budget), self.depth, self.dispatch_threads, ctypes.byref(h))
+        try:
+            outs, index = {}, []
+            for spec in specs:
+                _lib.call("gdbg_server_stream", h, spec.sid, spec.max_table,
+                          max(c.n_reads for c in spec.chunks),
+                          max(c.packed.size for c in spec.chunks))
+            for spec in specs:
+                outs[spec.sid] = []
+                for i, (c, t) in enumerate(zip(spec.chunks, spec.arrivals)):
+                    nn = np.zeros(max(c.n_reads, 1), np.uint64)
+                    outs[spec.sid].append(nn)
+                    tag = len(index)
+                    index.append((spec.sid, i, c.n_reads, c.n_kmers(self.K), float(t)))
+                    _lib.call("gdbg_server_submit", h, spec.sid, c.packed.ctypes.data,
+                              c.packed.size, c.offsets.ctypes.data, c.n_reads, index[-1][3],
+                              float(t), nn.ctypes.data, tag)
+                _lib.call("gdbg_server_finish", h, spec.sid)
+            _lib.call("gdbg_server_start", h)
+            _lib.call("gdbg_server_wait", h, float(max_seconds))
+            n = len(index)
+            tags = np.zeros(max(n, 1), np.uint64)
+            lat = np.zeros(max(n, 1), np.float64)
+            done = np.zeros(max(n, 1), np.float64)
+            ok = np.zeros(max(n, 1), np.int32)
+            got = ctypes.c_uint64()
+            _lib.call("gdbg_server_poll", h, tags.ctypes.data, lat.ctypes.data, done.ctypes.data,
+                      ok.ctypes.data, n, ctypes.byref(got))
+            rep = _lib.ServerReport()
+            _lib.call("gdbg_server_stats", h, ctypes.byref(rep))
+            err = _lib.load().gdbg_server_last_error(h).decode(errors="replace")
+        finally:
+            _lib.call("gdbg_server_destroy", h)
+        m = int(got.value)
+        if m != n or not ok[:m].all() or rep.chunks_failed or rep.device_status:
+            raise _lib.GoetiaError(_lib.ERR_DEVICE,
+                                   f"serving: {m} of {n} chunks completed, {rep.chunks_failed} "
+                                   f"failed, device status {rep.device_status:#x}: {err}")
+        results = {spec.sid: [None] * len(spec.chunks) for spec in specs}
+        for k in range(m):
+            sid, i, nr, nk, t = index[int(tags[k])]
+            results[sid][i] = ChunkResult(sid, i, nr, nk, outs[sid][i][:nr], t, t + float(lat[k]))
+        lat_ms = lat[:m] * 1e3
+        span = rep.last_done_s - rep.first_dispatch_s
+        stats = {
+            "chunks": m, "kmers": int(rep.kmers_done),
+            "kmers_per_s": rep.kmers_done / span if span > 0 else 0.0,
+            "p50_ms": float(np.percentile(lat_ms, 50)) if m else 0.0,
+            "p99_ms": float(np.percentile(lat_ms, 99)) if m else 0.0,
+            "max_ms": float(lat_ms.max()) if m else 0.0,
+            "peak_hbm_bytes": int(rep.peak_hbm_bytes),
+            "admission_waits": int(rep.admission_waits), "lazy_frees": int(rep.lazy_frees),
+            "wall_s": span,
+            "admit_ms_max": 1e3 * rep.admit_s_max, "admit_ms_total": 1e3 * rep.admit_s_total,
+            "dispatch_ms_mean": 1e3 * rep.dispatch_s_total / max(m, 1),
+            "dispatch_ms_max": 1e3 * rep.dispatch_s_max,
+            "dispatch_threads": self.dispatch_threads,
+        }
+        return results, stats
+
+
 def replay(spec, storage_type=D.BitStorage, shifter_type=D.CanLemireShifter, K=31, n_tables=4):
     """Sequential replay of one stream: its chunks inserted one after another
     into a fresh graph (the reference's order).  Returns per-chunk n_new."""

@@ -328,6 +328,63 @@ int gdbg_stage_times(gdbg_graph* g, char* names, uint64_t names_len, double* tot
 /* Kernel launches issued by this handle since creation. */
 int gdbg_launch_count(const gdbg_graph* g, uint64_t* launches);
 
+/* ---- serving: many streams, one graph each, continuous batching ------- */
+
+/* The reference's streaming driver (goetia/processors.py:39-498,
+ * AsyncSequenceProcessor; each chunk is InserterProcessor::process_sequence
+ * per read, processors.hh:304-331) serves one sample at a time.  A server
+ * serves many at once on the current device: each declared stream gets its
+ * own graph (tables, windowed insert, own CUDA stream) when its first chunk
+ * is due and its footprint fits hbm_budget (streams are admitted in the order
+ * their next chunks are due; a drained stream returns its share at once and
+ * its device memory is freed when an admission needs the room).  Native
+ * dispatcher threads (dispatch_threads of them) copy each released chunk into
+ * pinned staging and insert it asynchronously, up to `depth` chunks of a
+ * stream in flight, so chunks of different streams overlap on the GPU while
+ * each stream's chunks apply in order; per-chunk new counts equal inserting
+ * the stream's reads one by one (dbg.hh:296-305).  Latency of a chunk =
+ * completion time - release time.
+ *
+ * Use: create; declare every stream (gdbg_server_stream: table size and its
+ * largest chunk); submit chunks (host buffers that stay valid until the chunk
+ * completes; n_new = host output of n_reads counts, may be NULL; release_s =
+ * seconds after gdbg_server_start, non-decreasing per stream; n_kmers =
+ * UINT64_MAX to count them here) and mark each stream finished; start; wait;
+ * poll the completions (tag, latency, completion time, ok); destroy.  Chunks
+ * may also be submitted after start.  A stream whose footprint exceeds the
+ * budget is rejected when declared (GDBG_ERR_OOM). */
+typedef struct gdbg_server gdbg_server;
+typedef struct {
+    uint64_t chunks_submitted, chunks_done, chunks_failed, kmers_done;
+    uint64_t streams, streams_admitted, admission_waits, lazy_frees, peak_hbm_bytes;
+    double first_dispatch_s, last_done_s;   /* seconds after start */
+    double admit_s_max, admit_s_total;      /* graph creation on admission */
+    double dispatch_s_max, dispatch_s_total;/* host time per chunk dispatch */
+    uint32_t device_status;                 /* OR of the streams' device status bits */
+} gdbg_server_report;
+int gdbg_server_create(int storage, int shifter, uint16_t K, uint16_t n_tables,
+                       uint64_t hbm_budget, uint32_t depth, uint32_t dispatch_threads,
+                       gdbg_server** out);
+int gdbg_server_stream(gdbg_server* s, uint64_t stream_id, uint64_t max_table,
+                       uint64_t max_chunk_reads, uint64_t max_chunk_words);
+/* The HBM budget share of a declared stream (its admission footprint). */
+int gdbg_server_stream_bytes(gdbg_server* s, uint64_t stream_id, uint64_t* bytes);
+int gdbg_server_submit(gdbg_server* s, uint64_t stream_id, const uint32_t* packed,
+                       uint64_t n_words, const uint64_t* offsets, uint64_t n_reads,
+                       uint64_t n_kmers, double release_s, uint64_t* n_new, uint64_t tag);
+int gdbg_server_finish(gdbg_server* s, uint64_t stream_id);
+int gdbg_server_start(gdbg_server* s);
+/* Until every declared stream has drained (GDBG_ERR_DEVICE after timeout_s). */
+int gdbg_server_wait(gdbg_server* s, double timeout_s);
+/* Completions not yet polled, in completion order (up to max). */
+int gdbg_server_poll(gdbg_server* s, uint64_t* tags, double* latency_s, double* done_s,
+                     int32_t* ok, uint64_t max, uint64_t* n_out);
+int gdbg_server_stats(gdbg_server* s, gdbg_server_report* out);
+/* Message of the server's last failure (admission or dispatch), or "". */
+const char* gdbg_server_last_error(gdbg_server* s);
+/* Stops the threads (queued chunks are dropped), frees every stream. */
+int gdbg_server_destroy(gdbg_server* s);
+
 /* ---- insert without device allocation -------------------------------- */
 
 /* Limits of gdbg_insert_batch_noalloc (sizes of its static scratch). */

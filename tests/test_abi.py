@@ -42,7 +42,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_binding_table_matches_header():
-    names = declared() - {"gdbg_last_error", "gdbg_version"}
+    names = declared() - {"gdbg_last_error", "gdbg_version", "gdbg_server_last_error"}
     assert set(_lib.SIGNATURES) <= declared()
     missing = names - set(_lib.SIGNATURES)
     assert not missing, missing
