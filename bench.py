@@ -963,11 +963,11 @@ def main():
     ap.add_argument("--serve-streams", type=int, default=64)
     ap.add_argument("--serve-scale", type=float, default=1.0)
     ap.add_argument("--serve-loop", default="native", choices=["native", "python"])
-    ap.add_argument("--serve-dispatch-threads", type=int, default=2)
+    ap.add_argument("--serve-dispatch-threads", type=int, default=4)
     ap.add_argument("--serve-window", type=float, default=3.0,
                     help="seconds of arrivals per point of the rate sweep")
     ap.add_argument("--serve-sweep-gaps", type=lambda v: [float(x) for x in v.split(",")],
-                    default=[0.008, 0.004, 0.002, 0.001, 0.0005, 0.00025],
+                    default=[0.004, 0.002, 0.001, 0.0008, 0.00067, 0.00057, 0.0005, 0.00025],
                     help="mean chunk gaps per stream (s) of the rate sweep")
     ap.add_argument("--serve-gap", type=float, default=0.002)
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)

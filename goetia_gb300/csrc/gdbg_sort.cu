@@ -1,4 +1,6 @@
 // Launchers for the segmented bucketed insert (kernels in gdbg_sort.cuh).
+#include <algorithm>
+
 #include "gdbg_launch.h"
 #include "gdbg_sort.cuh"
 
@@ -60,11 +62,31 @@ cudaError_t launch_sp_starts(cudaStream_t st, const SortParams& sp, uint32_t* st
     return cudaGetLastError();
 }
 
+// Map space of the apply: 8 KB, or 16 KB when that keeps the most CTAs per
+// SM the region and record buffer allow (at most four of 512 threads).
+static uint32_t sp_apply_map_bytes(uint32_t region_words) {
+    int dev = 0, per_sm = 228 * 1024, reserved = 1024;
+    if (cudaGetDevice(&dev) == cudaSuccess) {
+        cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    }
+    const size_t static_b = 1024;   // the kernel's own __shared__ words, rounded up
+    auto ctas = [&](uint32_t map_b) {
+        const size_t per = sp_apply_smem(region_words, map_b) + static_b + (size_t)reserved;
+        return (int)std::min<size_t>(4, (size_t)per_sm / per);
+    };
+    const int best = ctas(SP_MAP_MIN);
+    return ctas(SP_MAP_MAX) >= best ? SP_MAP_MAX : SP_MAP_MIN;
+}
+
 template <int ST>
-static cudaError_t sp_apply_one(const TableParams& tp, const SortParams& sp, const uint64_t* recs,
+static cudaError_t sp_apply_one(const TableParams& tp, const SortParams& sp_in, const uint64_t* recs,
                                 const uint32_t* start, uint32_t* new_bits,
                                 unsigned long long* counters, cudaStream_t st) {
-    const size_t smem = sp_apply_smem((1u << sp.fs) / cells_per_word<ST>());
+    SortParams sp = sp_in;
+    const uint32_t region_words = (1u << sp.fs) / cells_per_word<ST>();
+    sp.map_bytes = sp_apply_map_bytes(region_words);
+    const size_t smem = sp_apply_smem(region_words, sp.map_bytes);
     cudaError_t e = cudaFuncSetAttribute(k_sp_apply<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
@@ -85,7 +107,7 @@ cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams
 
 size_t sp_apply_smem_bytes(int storage, uint32_t fs) {
     const uint32_t cpw = storage == GDBG_BIT ? 32u : storage == GDBG_BYTE ? 4u : 8u;
-    return sp_apply_smem((1u << fs) / cpw);
+    return sp_apply_smem((1u << fs) / cpw, sp_apply_map_bytes((1u << fs) / cpw));
 }
 
 }  // namespace gdbg

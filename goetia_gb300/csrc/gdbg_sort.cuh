@@ -561,21 +561,32 @@ __global__ void k_sp_starts(SortParams sp, uint32_t* __restrict__ start) {
 
 // ---- 4. order-independent apply -------------------------------------------
 
-constexpr uint32_t SP_RBUF = 4608;   // records of a bucket staged in shared memory at once
+// Shared memory of the apply: a bucket's records staged at once, its table
+// region, and one map space used two ways.  The single-chunk path (all of a
+// bucket's records staged) keys each zero cell to the staged record with the
+// smallest ordinal, in 32-bit entries (cell << 12 | record index); the
+// chunked path (buckets of more than SP_RBUF records) keeps 64-bit entries
+// (ordinal << 32 | cell).  The kernel is issue-bound, so the launcher sizes
+// the map space (SortParams::map_bytes, 8 or 16 KB) for the most CTAs per SM
+// the region allows: three with 32 KB regions, four with small ones, where
+// the larger map keeps fresh-cell-heavy buckets on one pass.
+constexpr uint32_t SP_RBUF = 4096;          // records staged at once (12-bit index)
+constexpr uint32_t SP_MAP_MIN = 8192, SP_MAP_MAX = 16384;   // map space bytes
+constexpr uint32_t SP_EMPTY32 = 0xFFFFFFFFu;
+static_assert(SP_RBUF <= 4096, "single-chunk map entries hold a 12-bit record index");
 
-__device__ __forceinline__ uint32_t sp_slot(uint32_t co) {
-    return (co * 0x9E3779B1u) >> (32 - 12);   // SP_MAPCAP = 2^12
+__device__ __forceinline__ uint32_t sp_slot_bits(uint32_t co, uint32_t bits) {
+    return (co * 0x9E3779B1u) >> (32 - bits);
 }
 
 // Shared-memory layout of k_sp_apply (byte offsets): region words (padded
-// to 16 bytes), fresh-cell map, record buffer (+2 alignment slack), dirty
+// to 16 bytes), map space, record buffer (+2 alignment slack), dirty
 // sector bits.
 struct ApplyLayout {
     uint32_t map_off, rec_off, dirty_off, total;
 };
-__host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words) {
+__host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words, uint32_t map_b) {
     const uint32_t region_b = ((region_words + 3u) & ~3u) * 4u;
-    const uint32_t map_b = SP_MAPCAP * 8u;
     const uint32_t rec_b = (SP_RBUF + 2u) * 8u;
     const uint32_t dirty_b = (((region_words + 7u) / 8u + 31u) / 32u) * 4u;
     return ApplyLayout{region_b, region_b + map_b, region_b + map_b + rec_b,
@@ -585,10 +596,11 @@ __host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words)
 // After pass 1 the map holds every cell of the range that was zero before
 // the batch, with the minimum ordinal of its records: that k-mer is the
 // cell's first toucher, so it is new.  Each thread reads its own slots.
-__device__ __forceinline__ void sp_map_winners(const uint64_t* map, const SortParams& sp, int ti,
+__device__ __forceinline__ void sp_map_winners(const uint64_t* map, uint32_t slots,
+                                               const SortParams& sp, int ti,
                                                uint32_t* __restrict__ new_bits,
                                                unsigned long long& occ) {
-    for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) {
+    for (uint32_t k = threadIdx.x; k < slots; k += SP_APPLY_BLOCK) {
         const uint64_t e = map[k];
         if (e == SP_EMPTY) continue;
         const uint32_t g = (uint32_t)(e >> 32);
@@ -599,14 +611,16 @@ __device__ __forceinline__ void sp_map_winners(const uint64_t* map, const SortPa
     }
 }
 
-// Map insert of a zero cell with ordinal g: the slot index, or SP_MAPCAP when
-// the map is full; *created is set when this call made the entry.
-__device__ __forceinline__ uint32_t sp_map_insert(uint64_t* map, uint32_t co, uint32_t g,
-                                                  bool* created) {
+// Chunked-path map insert of a zero cell with ordinal g (2^bits slots): the
+// slot index, or the slot count when the map is full; *created is set when
+// this call made the entry.
+__device__ __forceinline__ uint32_t sp_map_insert(uint64_t* map, uint32_t bits, uint32_t co,
+                                                  uint32_t g, bool* created) {
+    const uint32_t slots = 1u << bits;
     const uint64_t mine = ((uint64_t)g << 32) | co;   // (ordinal << 32) | cell
-    uint32_t sl = sp_slot(co);
+    uint32_t sl = sp_slot_bits(co, bits);
     *created = false;
-    for (uint32_t it = 0; it < SP_MAPCAP; ++it) {
+    for (uint32_t it = 0; it < slots; ++it) {
         uint64_t cur = map[sl];
         if (cur == SP_EMPTY) {
             cur = atomicCAS((unsigned long long*)&map[sl], SP_EMPTY, mine);
@@ -619,9 +633,46 @@ __device__ __forceinline__ uint32_t sp_map_insert(uint64_t* map, uint32_t co, ui
             if (mine < cur) atomicMin((unsigned long long*)&map[sl], mine);
             return sl;
         }
-        sl = (sl + 1) & (SP_MAPCAP - 1);
+        sl = (sl + 1) & (slots - 1);
     }
-    return SP_MAPCAP;
+    return slots;
+}
+
+// Single-chunk map insert (2^bits slots): zero cell co touched by staged
+// record k.  The slot keeps the cell's record with the smallest ordinal
+// (records of one bucket never share an ordinal: a k-mer has one cell per
+// table).  Returns the slot, or the slot count when the map is full;
+// *created when this call made it.
+__device__ __forceinline__ uint32_t sp_map32_insert(uint32_t* map, uint32_t bits,
+                                                    const uint64_t* src, uint32_t co, uint32_t k,
+                                                    bool* created) {
+    const uint32_t slots = 1u << bits;
+    const uint32_t mine = (co << 12) | k;
+    const uint32_t g = (uint32_t)src[k];
+    uint32_t sl = sp_slot_bits(co, bits);
+    *created = false;
+    for (uint32_t it = 0; it < slots; ++it) {
+        uint32_t cur = map[sl];
+        if (cur == SP_EMPTY32) {
+            cur = atomicCAS(map + sl, SP_EMPTY32, mine);
+            if (cur == SP_EMPTY32) {
+                *created = true;
+                return sl;
+            }
+        }
+        if ((cur >> 12) == co) {
+            // the same cell: this record takes the slot while its ordinal is
+            // smaller (each successful swap lowers the ordinal held)
+            for (uint32_t t = 0; t < SP_RBUF && (uint32_t)src[cur & 4095u] > g; ++t) {
+                const uint32_t prev = atomicCAS(map + sl, cur, mine);
+                if (prev == cur) break;
+                cur = prev;
+            }
+            return sl;
+        }
+        sl = (sl + 1) & (slots - 1);
+    }
+    return slots;
 }
 
 // Saturating increment of one region cell; true when the word changed.
@@ -649,14 +700,14 @@ __device__ __forceinline__ bool sp_increment(uint32_t* region, uint32_t word, ui
 // from pass 1 (pass 2 looks up nothing); larger or denser buckets take the
 // general loop over buffer chunks and cell ranges.
 template <int STORAGE>
-__global__ void __launch_bounds__(SP_APPLY_BLOCK, 2)
+__global__ void __launch_bounds__(SP_APPLY_BLOCK, 4)
 k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
            const uint32_t* __restrict__ start, uint32_t* __restrict__ new_bits,
            unsigned long long* counters) {
     extern __shared__ __align__(128) unsigned char sbytes[];
     __shared__ uint32_t n_fresh, overflow, abort_s;
     __shared__ __align__(8) uint64_t bar;
-    __shared__ uint32_t used[SP_MAPCAP / 32];   // map slots created by the fast path
+    __shared__ uint32_t used[SP_MAP_MAX / 4 / 32];   // single-chunk map slots created
     const uint32_t bk = blockIdx.x;
     const uint32_t rs = start[bk], re = start[bk + 1];
     if (rs >= re) return;
@@ -665,9 +716,13 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     const uint32_t region_cells = 1u << sp.fs;
     const uint32_t region_words = region_cells / cells_per_word<STORAGE>();
     const uint32_t region_sectors = (region_words + 7) / 8;
-    const ApplyLayout L = sp_apply_layout(region_words);
+    const ApplyLayout L = sp_apply_layout(region_words, sp.map_bytes);
+    // map slots: 32-bit entries for the single-chunk path, 64-bit for the chunked one
+    const uint32_t bits32 = 31u - __clz(sp.map_bytes / 4u), slots32 = 1u << bits32;
+    const uint32_t bits64 = bits32 - 1u, slots64 = 1u << bits64;
     uint32_t* region = reinterpret_cast<uint32_t*>(sbytes);
-    uint64_t* map = reinterpret_cast<uint64_t*>(sbytes + L.map_off);
+    uint64_t* map = reinterpret_cast<uint64_t*>(sbytes + L.map_off);     // chunked path
+    uint32_t* map32 = reinterpret_cast<uint32_t*>(sbytes + L.map_off);   // single-chunk path
     uint64_t* rbuf = reinterpret_cast<uint64_t*>(sbytes + L.rec_off);
     uint32_t* dirty = reinterpret_cast<uint32_t*>(sbytes + L.dirty_off);
     const uint64_t c0 = (uint64_t)(bk - sp.bbase[ti]) << sp.fs;
@@ -705,8 +760,8 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
         for (uint32_t k = threadIdx.x; k < nw; k += SP_APPLY_BLOCK) region[k] = __ldcs(gsrc + k);
     if (track)
         for (uint32_t k = threadIdx.x; k < (region_sectors + 31) / 32; k += SP_APPLY_BLOCK) dirty[k] = 0;
-    for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
-    for (uint32_t k = threadIdx.x; k < SP_MAPCAP / 32; k += SP_APPLY_BLOCK) used[k] = 0;
+    for (uint32_t k = threadIdx.x; k < slots32; k += SP_APPLY_BLOCK) map32[k] = SP_EMPTY32;
+    for (uint32_t k = threadIdx.x; k < slots32 / 32; k += SP_APPLY_BLOCK) used[k] = 0;
     __syncthreads();   // the barrier is initialised before anyone waits on it
     if (!copy_wait(sp, &bar, phase & 1u)) atomicExch(&abort_s, 1u);
     ++phase;
@@ -722,31 +777,55 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     unsigned long long occ = 0;
     bool done = false;
     if (n_chunks == 1) {
-        // fast path: all records staged, the whole region as one cell range
+        // all records staged: cell ranges [lo, lo + width), the whole region
+        // first, narrower when the zero cells of a range overflow the map
         const uint64_t* src = rbuf + (rs & 1u);
-        uint32_t inserted = 0;
-        bool lost = false;
-        for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
-            const uint64_t rec = src[k];
-            const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
-            uint32_t word, shift;
-            region_cell<STORAGE>(co, word, shift);
-            if (cell_value<STORAGE>(region[word], shift) == 0) {
-                bool created;
-                const uint32_t sl = sp_map_insert(map, co, (uint32_t)rec, &created);
-                inserted += created;
-                lost |= sl >= SP_MAPCAP;
-                if (created) atomicOr(&used[sl >> 5], 1u << (sl & 31u));
+        uint32_t lo = 0, width = region_cells;
+        bool first = true;
+        for (int guard = 0; lo < region_cells && guard < 4096; ++guard) {
+            const uint32_t hi = lo + width < region_cells ? lo + width : region_cells;
+            if (!first) {
+                for (uint32_t k = threadIdx.x; k < slots32; k += SP_APPLY_BLOCK) map32[k] = SP_EMPTY32;
+                for (uint32_t k = threadIdx.x; k < slots32 / 32; k += SP_APPLY_BLOCK) used[k] = 0;
+                if (threadIdx.x == 0) {
+                    n_fresh = 0;
+                    overflow = 0;
+                }
+                __syncthreads();
             }
-        }
-        inserted = __reduce_add_sync(0xFFFFFFFFu, inserted);
-        if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
-        if (lost) overflow = 1;
-        __syncthreads();
-        if (!overflow && n_fresh <= SP_MAPCAP / 2) {
+            first = false;
+            const bool whole = width == region_cells;
+            // pass 1: the staged record with the minimum ordinal per zero cell
+            uint32_t inserted = 0;
+            bool lost = false;
             for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
                 const uint64_t rec = src[k];
                 const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
+                if (!whole && (co < lo || co >= hi)) continue;
+                uint32_t word, shift;
+                region_cell<STORAGE>(co, word, shift);
+                if (cell_value<STORAGE>(region[word], shift) == 0) {
+                    bool created;
+                    const uint32_t sl = sp_map32_insert(map32, bits32, src, co, k, &created);
+                    inserted += created;
+                    lost |= sl >= slots32;
+                    if (created) atomicOr(&used[sl >> 5], 1u << (sl & 31u));
+                }
+            }
+            inserted = __reduce_add_sync(0xFFFFFFFFu, inserted);
+            if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
+            if (lost) overflow = 1;
+            __syncthreads();
+            if ((overflow || n_fresh > slots32 / 2) && width > 1) {
+                width >>= 1;   // redo this range narrower; nothing was applied yet
+                __syncthreads();
+                continue;
+            }
+            // pass 2: apply every record of the range
+            for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
+                const uint64_t rec = src[k];
+                const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
+                if (!whole && (co < lo || co >= hi)) continue;
                 uint32_t word, shift;
                 region_cell<STORAGE>(co, word, shift);
                 const bool changed = sp_increment<STORAGE>(region, word, shift);
@@ -757,18 +836,20 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
             }
             // the first touchers: the created map slots, word by word of the
             // used bits
-            for (uint32_t wd = threadIdx.x; wd < SP_MAPCAP / 32; wd += SP_APPLY_BLOCK) {
+            for (uint32_t wd = threadIdx.x; wd < slots32 / 32; wd += SP_APPLY_BLOCK) {
                 for (uint32_t m = used[wd]; m; m &= m - 1) {
-                    const uint32_t g = (uint32_t)(map[wd * 32 + __ffs(m) - 1] >> 32);
+                    const uint32_t g = (uint32_t)src[map32[wd * 32 + __ffs(m) - 1] & 4095u];
                     if (g < sp.kmer_cap) {
                         atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
                         if (ti == 0) ++occ;
                     }
                 }
             }
-            done = true;
+            __syncthreads();
+            lo = hi;
         }
-        __syncthreads();
+        if (lo < region_cells && threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
+        done = true;
     }
     if (!done) {
         uint32_t loaded = 0;   // chunk in rbuf
@@ -787,13 +868,13 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
             return abort_s == 0;
         };
         // cell ranges [lo, lo + width): narrower when the zero cells of a
-        // range overflow the map (the fast path already tried the whole region)
-        uint32_t lo = 0, width = n_chunks == 1 ? region_cells >> 1 : region_cells;
+        // range overflow the map
+        uint32_t lo = 0, width = region_cells;
         int guard = 0;
         bool ok = true;
         for (; ok && lo < region_cells && guard < 4096; ++guard) {
             const uint32_t hi = lo + width < region_cells ? lo + width : region_cells;
-            for (uint32_t k = threadIdx.x; k < SP_MAPCAP; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
+            for (uint32_t k = threadIdx.x; k < slots64; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
             if (threadIdx.x == 0) {
                 n_fresh = 0;
                 overflow = 0;
@@ -816,9 +897,9 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                     region_cell<STORAGE>(co, word, shift);
                     if (cell_value<STORAGE>(region[word], shift) != 0) continue;
                     bool created;
-                    const uint32_t sl = sp_map_insert(map, co, (uint32_t)rec, &created);
+                    const uint32_t sl = sp_map_insert(map, bits64, co, (uint32_t)rec, &created);
                     inserted += created;
-                    lost |= sl >= SP_MAPCAP;
+                    lost |= sl >= slots64;
                 }
             }
             if (!ok) break;
@@ -826,7 +907,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
             if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
             if (lost) overflow = 1;
             __syncthreads();
-            if ((overflow || n_fresh > SP_MAPCAP / 2) && width > 1) {
+            if ((overflow || n_fresh > slots64 / 2) && width > 1) {
                 width >>= 1;   // redo this range narrower; nothing was applied yet
                 __syncthreads();
                 continue;
@@ -852,7 +933,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                 }
             }
             if (!ok) break;
-            sp_map_winners(map, sp, ti, new_bits, occ);
+            sp_map_winners(map, slots64, sp, ti, new_bits, occ);
             __syncthreads();
             lo = hi;
         }
@@ -885,8 +966,8 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     if ((threadIdx.x & 31) == 0 && occ) atomicAdd(counters + 1, occ);
 }
 
-__host__ __device__ constexpr size_t sp_apply_smem(uint32_t region_words) {
-    return sp_apply_layout(region_words).total;
+__host__ __device__ constexpr size_t sp_apply_smem(uint32_t region_words, uint32_t map_b) {
+    return sp_apply_layout(region_words, map_b).total;
 }
 
 }  // namespace gdbg

@@ -98,7 +98,6 @@ constexpr uint32_t SP_TILE = 4096;       // records per partition tile
 constexpr uint32_t SP_SEGK = 32768;      // k-mers per pass-1 segment (multiple of MAP_TILE)
 constexpr uint32_t SP_SEG2 = 32768;      // records per pass-2 segment
 constexpr uint32_t SP_MAXBINS2 = 512;    // pass-2 digit bins at most
-constexpr uint32_t SP_MAPCAP = 4096;     // apply: fresh-cell map slots
 
 struct SortParams {
     uint32_t fs;                  // log2(cells per bucket)
@@ -120,6 +119,7 @@ struct SortParams {
     uint32_t* plan;               // s0[bins1 + 1] then G[bins1 + 1]
     uint32_t* err;                // device status word
     uint32_t wait_cap;            // polls of a bulk-copy wait before giving up (0: WAIT_CAP)
+    uint32_t map_bytes;           // apply: map space per CTA (set by its launcher)
 };
 
 // Persistent batch insert (gdbg_persist.cuh).
