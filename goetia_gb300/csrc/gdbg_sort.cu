@@ -1,5 +1,6 @@
 // Launchers for the segmented bucketed insert (kernels in gdbg_sort.cuh).
 #include <algorithm>
+#include <cmath>
 
 #include "gdbg_launch.h"
 #include "gdbg_sort.cuh"
@@ -62,21 +63,44 @@ cudaError_t launch_sp_starts(cudaStream_t st, const SortParams& sp, uint32_t* st
     return cudaGetLastError();
 }
 
-// Map space of the apply: 8 KB, or 16 KB when that keeps the most CTAs per
-// SM the region and record buffer allow (at most four of 512 threads).
-static uint32_t sp_apply_map_bytes(uint32_t region_words) {
+// Shared-memory plan of the apply for regions of region_words words and
+// buckets of about `load` records: the record buffer holds the load plus
+// eight standard deviations of a Poisson count (4096 to 8192 records,
+// indexable in the 32 - fs bits a map entry leaves; a rarer, fuller bucket
+// takes the chunked path), and the map space is 16 KB when that keeps as
+// many CTAs per SM (at most four of 512 threads) as 8 KB does.
+struct ApplyPlan {
+    uint32_t map_bytes, rbuf_cap, idx_bits;
+};
+static ApplyPlan sp_apply_plan(uint32_t region_words, uint32_t fs, double load) {
     int dev = 0, per_sm = 228 * 1024, reserved = 1024;
     if (cudaGetDevice(&dev) == cudaSuccess) {
         cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
         cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
     }
+    ApplyPlan p{};
+    // cell << idx_bits | index stays below the all-ones empty entry (the
+    // segmented path's regions are at most 64 KB, so fs <= 19)
+    p.idx_bits = fs <= 18 ? 13u : 12u;
+    const uint32_t cap_max = std::min<uint32_t>(SP_RBUF_MAX, 1u << p.idx_bits);
+    const double want = load + 8.0 * std::sqrt(load) + 64.0;
+    uint32_t rb = want >= cap_max ? cap_max : ((uint32_t)want + 63u) / 64u * 64u;
+    p.rbuf_cap = std::min(std::max(rb, std::min(SP_RBUF_MIN, cap_max)), cap_max);
     const size_t static_b = 1024;   // the kernel's own __shared__ words, rounded up
     auto ctas = [&](uint32_t map_b) {
-        const size_t per = sp_apply_smem(region_words, map_b) + static_b + (size_t)reserved;
+        const size_t per = sp_apply_smem(region_words, map_b, p.rbuf_cap) + static_b + (size_t)reserved;
         return (int)std::min<size_t>(4, (size_t)per_sm / per);
     };
-    const int best = ctas(SP_MAP_MIN);
-    return ctas(SP_MAP_MAX) >= best ? SP_MAP_MAX : SP_MAP_MIN;
+    p.map_bytes = ctas(SP_MAP_MAX) >= ctas(SP_MAP_MIN) ? SP_MAP_MAX : SP_MAP_MIN;
+    return p;
+}
+
+// Expected records per bucket of the batch: its k-mer bound times the cells
+// of a bucket over the smallest table.
+static double sp_bucket_load(const TableParams& tp, const SortParams& sp) {
+    uint64_t pmin = ~0ull;
+    for (int i = 0; i < tp.n; ++i) pmin = std::min<uint64_t>(pmin, tp.p[i]);
+    return (double)sp.kmer_cap * (double)(1ull << sp.fs) / (double)pmin;
 }
 
 template <int ST>
@@ -85,13 +109,21 @@ static cudaError_t sp_apply_one(const TableParams& tp, const SortParams& sp_in, 
                                 unsigned long long* counters, cudaStream_t st) {
     SortParams sp = sp_in;
     const uint32_t region_words = (1u << sp.fs) / cells_per_word<ST>();
-    sp.map_bytes = sp_apply_map_bytes(region_words);
-    const size_t smem = sp_apply_smem(region_words, sp.map_bytes);
-    cudaError_t e = cudaFuncSetAttribute(k_sp_apply<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    k_sp_apply<ST><<<sp.n_buckets, SP_APPLY_BLOCK, smem, st>>>(tp, sp, recs, start, new_bits, counters);
-    return cudaGetLastError();
+    const ApplyPlan plan = sp_apply_plan(region_words, sp.fs, sp_bucket_load(tp, sp));
+    sp.map_bytes = plan.map_bytes;
+    sp.rbuf_cap = plan.rbuf_cap;
+    sp.idx_bits = plan.idx_bits;
+    const size_t smem = sp_apply_smem(region_words, sp.map_bytes, sp.rbuf_cap);
+    auto go = [&](auto kern) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<sp.n_buckets, SP_APPLY_BLOCK, smem, st>>>(tp, sp, recs, start, new_bits, counters);
+        return cudaGetLastError();
+    };
+    const bool big = sp.map_bytes == SP_MAP_MAX;
+    if (sp.idx_bits == 13)
+        return big ? go(k_sp_apply<ST, SP_MAP_MAX, 13>) : go(k_sp_apply<ST, SP_MAP_MIN, 13>);
+    return big ? go(k_sp_apply<ST, SP_MAP_MAX, 12>) : go(k_sp_apply<ST, SP_MAP_MIN, 12>);
 }
 
 cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams& sp,
@@ -107,7 +139,8 @@ cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams
 
 size_t sp_apply_smem_bytes(int storage, uint32_t fs) {
     const uint32_t cpw = storage == GDBG_BIT ? 32u : storage == GDBG_BYTE ? 4u : 8u;
-    return sp_apply_smem((1u << fs) / cpw, sp_apply_map_bytes((1u << fs) / cpw));
+    const ApplyPlan p = sp_apply_plan((1u << fs) / cpw, fs, SP_RBUF_MIN);
+    return sp_apply_smem((1u << fs) / cpw, p.map_bytes, p.rbuf_cap);
 }
 
 }  // namespace gdbg

@@ -27,6 +27,8 @@
 //      60-100) cell by cell; a cell's final value does not depend on the
 //      order of its increments.
 #pragma once
+#include <type_traits>
+
 #include "gdbg_persist.cuh"
 
 namespace gdbg {
@@ -561,19 +563,25 @@ __global__ void k_sp_starts(SortParams sp, uint32_t* __restrict__ start) {
 
 // ---- 4. order-independent apply -------------------------------------------
 
-// Shared memory of the apply: a bucket's records staged at once, its table
-// region, and one map space used two ways.  The single-chunk path (all of a
-// bucket's records staged) keys each zero cell to the staged record with the
-// smallest ordinal, in 32-bit entries (cell << 12 | record index); the
-// chunked path (buckets of more than SP_RBUF records) keeps 64-bit entries
-// (ordinal << 32 | cell).  The kernel is issue-bound, so the launcher sizes
-// the map space (SortParams::map_bytes, 8 or 16 KB) for the most CTAs per SM
-// the region allows: three with 32 KB regions, four with small ones, where
-// the larger map keeps fresh-cell-heavy buckets on one pass.
-constexpr uint32_t SP_RBUF = 4096;          // records staged at once (12-bit index)
-constexpr uint32_t SP_MAP_MIN = 8192, SP_MAP_MAX = 16384;   // map space bytes
+// Shared memory of the apply: a bucket's records staged at once (up to
+// SortParams::rbuf_cap of them), its table region, and one map space used
+// two ways.  The single-chunk path (all of a bucket's records staged) keys
+// each zero cell to the staged record with the smallest ordinal, in 32-bit
+// entries (cell << idx_bits | record index); the chunked path (buckets of
+// more records than the buffer holds) keeps 64-bit entries (ordinal << 32 |
+// cell) and restages records per cell range.  The kernel is issue-bound, so
+// the launcher sizes the record buffer for the batch's expected bucket load
+// and the map space (8 or 16 KB) for the most CTAs per SM that leaves: three
+// with 32 KB regions, four with small regions and light buckets.
+constexpr uint32_t SP_RBUF_MIN = 4096, SP_RBUF_MAX = 8192;   // records staged at once
+constexpr uint32_t SP_MAP_MIN = 8192, SP_MAP_MAX = 16384;    // map space bytes
 constexpr uint32_t SP_EMPTY32 = 0xFFFFFFFFu;
-static_assert(SP_RBUF <= 4096, "single-chunk map entries hold a 12-bit record index");
+// Linear-probe limit of a map insert.  A map filled to half its slots needs
+// about two probes; a fuller one -- a fresh, empty table puts nearly every
+// cell of a region into the map -- would make each insert walk the whole map,
+// so an insert that runs this long reports the map full and the cell range is
+// narrowed.
+constexpr uint32_t SP_PROBE_CAP = 64;
 
 __device__ __forceinline__ uint32_t sp_slot_bits(uint32_t co, uint32_t bits) {
     return (co * 0x9E3779B1u) >> (32 - bits);
@@ -585,9 +593,10 @@ __device__ __forceinline__ uint32_t sp_slot_bits(uint32_t co, uint32_t bits) {
 struct ApplyLayout {
     uint32_t map_off, rec_off, dirty_off, total;
 };
-__host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words, uint32_t map_b) {
+__host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words, uint32_t map_b,
+                                                         uint32_t rbuf_cap) {
     const uint32_t region_b = ((region_words + 3u) & ~3u) * 4u;
-    const uint32_t rec_b = (SP_RBUF + 2u) * 8u;
+    const uint32_t rec_b = (rbuf_cap + 2u) * 8u;
     const uint32_t dirty_b = (((region_words + 7u) / 8u + 31u) / 32u) * 4u;
     return ApplyLayout{region_b, region_b + map_b, region_b + map_b + rec_b,
                        region_b + map_b + rec_b + dirty_b};
@@ -620,7 +629,7 @@ __device__ __forceinline__ uint32_t sp_map_insert(uint64_t* map, uint32_t bits, 
     const uint64_t mine = ((uint64_t)g << 32) | co;   // (ordinal << 32) | cell
     uint32_t sl = sp_slot_bits(co, bits);
     *created = false;
-    for (uint32_t it = 0; it < slots; ++it) {
+    for (uint32_t it = 0; it < SP_PROBE_CAP; ++it) {
         uint64_t cur = map[sl];
         if (cur == SP_EMPTY) {
             cur = atomicCAS((unsigned long long*)&map[sl], SP_EMPTY, mine);
@@ -639,19 +648,19 @@ __device__ __forceinline__ uint32_t sp_map_insert(uint64_t* map, uint32_t bits, 
 }
 
 // Single-chunk map insert (2^bits slots): zero cell co touched by staged
-// record k.  The slot keeps the cell's record with the smallest ordinal
-// (records of one bucket never share an ordinal: a k-mer has one cell per
-// table).  Returns the slot, or the slot count when the map is full;
-// *created when this call made it.
-__device__ __forceinline__ uint32_t sp_map32_insert(uint32_t* map, uint32_t bits,
+// record k (below 2^ib).  The slot keeps the cell's record with the
+// smallest ordinal (records of one bucket never share an ordinal: a k-mer
+// has one cell per table).  Returns the slot, or the slot count when the map
+// is full; *created when this call made it.
+__device__ __forceinline__ uint32_t sp_map32_insert(uint32_t* map, uint32_t bits, uint32_t ib,
                                                     const uint64_t* src, uint32_t co, uint32_t k,
                                                     bool* created) {
-    const uint32_t slots = 1u << bits;
-    const uint32_t mine = (co << 12) | k;
+    const uint32_t slots = 1u << bits, im = (1u << ib) - 1u;
+    const uint32_t mine = (co << ib) | k;
     const uint32_t g = (uint32_t)src[k];
     uint32_t sl = sp_slot_bits(co, bits);
     *created = false;
-    for (uint32_t it = 0; it < slots; ++it) {
+    for (uint32_t it = 0; it < SP_PROBE_CAP; ++it) {
         uint32_t cur = map[sl];
         if (cur == SP_EMPTY32) {
             cur = atomicCAS(map + sl, SP_EMPTY32, mine);
@@ -660,10 +669,10 @@ __device__ __forceinline__ uint32_t sp_map32_insert(uint32_t* map, uint32_t bits
                 return sl;
             }
         }
-        if ((cur >> 12) == co) {
+        if ((cur >> ib) == co) {
             // the same cell: this record takes the slot while its ordinal is
             // smaller (each successful swap lowers the ordinal held)
-            for (uint32_t t = 0; t < SP_RBUF && (uint32_t)src[cur & 4095u] > g; ++t) {
+            for (uint32_t t = 0; t < slots && (uint32_t)src[cur & im] > g; ++t) {
                 const uint32_t prev = atomicCAS(map + sl, cur, mine);
                 if (prev == cur) break;
                 cur = prev;
@@ -699,7 +708,10 @@ __device__ __forceinline__ bool sp_increment(uint32_t* region, uint32_t word, ui
 // A bucket whose records fit one staging buffer keeps each record's map slot
 // from pass 1 (pass 2 looks up nothing); larger or denser buckets take the
 // general loop over buffer chunks and cell ranges.
-template <int STORAGE>
+// MAPB: map space bytes (SortParams::map_bytes), IB: record-index bits of a
+// single-chunk map entry (SortParams::idx_bits); compile-time, so the map's
+// hashing and entry packing take no run-time shifts.
+template <int STORAGE, uint32_t MAPB, uint32_t IB>
 __global__ void __launch_bounds__(SP_APPLY_BLOCK, 4)
 k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
            const uint32_t* __restrict__ start, uint32_t* __restrict__ new_bits,
@@ -716,10 +728,17 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     const uint32_t region_cells = 1u << sp.fs;
     const uint32_t region_words = region_cells / cells_per_word<STORAGE>();
     const uint32_t region_sectors = (region_words + 7) / 8;
-    const ApplyLayout L = sp_apply_layout(region_words, sp.map_bytes);
+    const uint32_t RB = sp.rbuf_cap;   // records staged at once
+    const ApplyLayout L = sp_apply_layout(region_words, sp.map_bytes, RB);
     // map slots: 32-bit entries for the single-chunk path, 64-bit for the chunked one
-    const uint32_t bits32 = 31u - __clz(sp.map_bytes / 4u), slots32 = 1u << bits32;
-    const uint32_t bits64 = bits32 - 1u, slots64 = 1u << bits64;
+    constexpr uint32_t slots32 = MAPB / 4u, bits32 = slots32 == 4096u ? 12u : 11u;
+    // entries (cell << IB | index) never reach the all-ones empty entry
+    if (sp.fs + IB > 31u) {
+        if (threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_PARTITION);
+        return;
+    }
+    constexpr uint32_t bits64 = bits32 - 1u, slots64 = 1u << bits64;
+    static_assert((1u << bits32) == slots32, "map space of 8 or 16 KB");
     uint32_t* region = reinterpret_cast<uint32_t*>(sbytes);
     uint64_t* map = reinterpret_cast<uint64_t*>(sbytes + L.map_off);     // chunked path
     uint32_t* map32 = reinterpret_cast<uint32_t*>(sbytes + L.map_off);   // single-chunk path
@@ -733,15 +752,15 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     // the region by one bulk copy when it is a whole number of 16-byte units
     const bool bulk_region = ((w0 & 3u) == 0) && ((nw & 3u) == 0);
     const uint32_t n_recs = re - rs;
-    const uint32_t n_chunks = (n_recs + SP_RBUF - 1) / SP_RBUF;
+    const uint32_t n_chunks = (n_recs + RB - 1) / RB;
     // dense buckets write the whole region back; sparse ones their dirty sectors
     const bool track = n_recs < region_sectors;
     uint32_t phase = 0;
     // records of chunk c into rbuf, copied from the even index at or below
     // its first record (and the region with chunk 0)
     auto chunk_copy = [&](uint32_t c, bool with_region) {
-        const uint32_t a = rs + c * SP_RBUF;
-        const uint32_t b = a + SP_RBUF < re ? a + SP_RBUF : re;
+        const uint32_t a = rs + c * RB;
+        const uint32_t b = a + RB < re ? a + RB : re;
         const uint32_t a0 = a & ~1u, a1 = (b + 1) & ~1u;
         const uint32_t bytes = (a1 - a0) * 8u + (with_region ? nw * 4u : 0u);
         mbar_expect(&bar, bytes);
@@ -777,25 +796,16 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     unsigned long long occ = 0;
     bool done = false;
     if (n_chunks == 1) {
-        // all records staged: cell ranges [lo, lo + width), the whole region
-        // first, narrower when the zero cells of a range overflow the map
+        // all records staged: the whole region as one cell range first, then,
+        // when its zero cells overflow the map, narrower ranges
         const uint64_t* src = rbuf + (rs & 1u);
-        uint32_t lo = 0, width = region_cells;
-        bool first = true;
-        for (int guard = 0; lo < region_cells && guard < 4096; ++guard) {
-            const uint32_t hi = lo + width < region_cells ? lo + width : region_cells;
-            if (!first) {
-                for (uint32_t k = threadIdx.x; k < slots32; k += SP_APPLY_BLOCK) map32[k] = SP_EMPTY32;
-                for (uint32_t k = threadIdx.x; k < slots32 / 32; k += SP_APPLY_BLOCK) used[k] = 0;
-                if (threadIdx.x == 0) {
-                    n_fresh = 0;
-                    overflow = 0;
-                }
-                __syncthreads();
-            }
-            first = false;
-            const bool whole = width == region_cells;
-            // pass 1: the staged record with the minimum ordinal per zero cell
+        constexpr uint32_t ib = IB, im = (1u << IB) - 1u;
+        // pass 1 over [lo, hi): the staged record with the minimum ordinal per
+        // zero cell; true when the range fits the map
+        // (generic lambdas: the whole-region form is compiled without the
+        // range test)
+        auto map_pass = [&](auto whole_c, uint32_t lo, uint32_t hi) -> bool {
+            constexpr bool whole = decltype(whole_c)::value;
             uint32_t inserted = 0;
             bool lost = false;
             for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
@@ -804,11 +814,16 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                 if (!whole && (co < lo || co >= hi)) continue;
                 uint32_t word, shift;
                 region_cell<STORAGE>(co, word, shift);
-                if (cell_value<STORAGE>(region[word], shift) == 0) {
+                // once the map has overflowed the range is redone narrower:
+                // the remaining inserts are skipped
+                if (cell_value<STORAGE>(region[word], shift) == 0 && !*(volatile uint32_t*)&overflow) {
                     bool created;
-                    const uint32_t sl = sp_map32_insert(map32, bits32, src, co, k, &created);
+                    const uint32_t sl = sp_map32_insert(map32, bits32, ib, src, co, k, &created);
                     inserted += created;
-                    lost |= sl >= slots32;
+                    if (sl >= slots32) {
+                        lost = true;
+                        overflow = 1;
+                    }
                     if (created) atomicOr(&used[sl >> 5], 1u << (sl & 31u));
                 }
             }
@@ -816,12 +831,12 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
             if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
             if (lost) overflow = 1;
             __syncthreads();
-            if ((overflow || n_fresh > slots32 / 2) && width > 1) {
-                width >>= 1;   // redo this range narrower; nothing was applied yet
-                __syncthreads();
-                continue;
-            }
-            // pass 2: apply every record of the range
+            return !overflow && n_fresh <= slots32 / 2;
+        };
+        // pass 2 over [lo, hi): every record applied; then the map's entries
+        // (the first touchers) flagged new
+        auto apply_pass = [&](auto whole_c, uint32_t lo, uint32_t hi) {
+            constexpr bool whole = decltype(whole_c)::value;
             for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
                 const uint64_t rec = src[k];
                 const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
@@ -834,21 +849,45 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                     atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
                 }
             }
-            // the first touchers: the created map slots, word by word of the
-            // used bits
             for (uint32_t wd = threadIdx.x; wd < slots32 / 32; wd += SP_APPLY_BLOCK) {
                 for (uint32_t m = used[wd]; m; m &= m - 1) {
-                    const uint32_t g = (uint32_t)src[map32[wd * 32 + __ffs(m) - 1] & 4095u];
+                    const uint32_t g = (uint32_t)src[map32[wd * 32 + __ffs(m) - 1] & im];
                     if (g < sp.kmer_cap) {
                         atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
                         if (ti == 0) ++occ;
                     }
                 }
             }
+        };
+        auto clear_map = [&]() {
+            __syncthreads();   // everyone is done with the map and the counts
+            for (uint32_t k = threadIdx.x; k < slots32; k += SP_APPLY_BLOCK) map32[k] = SP_EMPTY32;
+            for (uint32_t k = threadIdx.x; k < slots32 / 32; k += SP_APPLY_BLOCK) used[k] = 0;
+            if (threadIdx.x == 0) {
+                n_fresh = 0;
+                overflow = 0;
+            }
             __syncthreads();
-            lo = hi;
+        };
+        using whole_t = std::true_type;
+        using ranged_t = std::false_type;
+        if (map_pass(whole_t{}, 0, region_cells)) {
+            apply_pass(whole_t{}, 0, region_cells);
+        } else {
+            uint32_t lo = 0, width = region_cells >> 1;
+            for (int guard = 0; lo < region_cells && guard < 4096; ++guard) {
+                const uint32_t hi = lo + width < region_cells ? lo + width : region_cells;
+                clear_map();
+                if (!map_pass(ranged_t{}, lo, hi) && width > 1) {
+                    width >>= 1;   // redo this range narrower; nothing was applied yet
+                    continue;
+                }
+                apply_pass(ranged_t{}, lo, hi);
+                lo = hi;
+            }
+            if (lo < region_cells && threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
         }
-        if (lo < region_cells && threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
+        __syncthreads();
         done = true;
     }
     if (!done) {
@@ -886,8 +925,8 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
             for (uint32_t c = 0; c < n_chunks && ok; ++c) {
                 ok = need_chunk(c);
                 if (!ok) break;
-                const uint32_t a = rs + c * SP_RBUF;
-                const uint32_t cnt = re - a < SP_RBUF ? re - a : SP_RBUF;
+                const uint32_t a = rs + c * RB;
+                const uint32_t cnt = re - a < RB ? re - a : RB;
                 const uint64_t* src = rbuf + (a & 1u);
                 for (uint32_t k = threadIdx.x; k < cnt; k += SP_APPLY_BLOCK) {
                     const uint64_t rec = src[k];
@@ -896,10 +935,14 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
                     uint32_t word, shift;
                     region_cell<STORAGE>(co, word, shift);
                     if (cell_value<STORAGE>(region[word], shift) != 0) continue;
+                    if (*(volatile uint32_t*)&overflow) continue;   // redone narrower anyway
                     bool created;
                     const uint32_t sl = sp_map_insert(map, bits64, co, (uint32_t)rec, &created);
                     inserted += created;
-                    lost |= sl >= slots64;
+                    if (sl >= slots64) {
+                        lost = true;
+                        overflow = 1;
+                    }
                 }
             }
             if (!ok) break;
@@ -916,8 +959,8 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
             for (uint32_t c = 0; c < n_chunks && ok; ++c) {
                 ok = need_chunk(c);
                 if (!ok) break;
-                const uint32_t a = rs + c * SP_RBUF;
-                const uint32_t cnt = re - a < SP_RBUF ? re - a : SP_RBUF;
+                const uint32_t a = rs + c * RB;
+                const uint32_t cnt = re - a < RB ? re - a : RB;
                 const uint64_t* src = rbuf + (a & 1u);
                 for (uint32_t k = threadIdx.x; k < cnt; k += SP_APPLY_BLOCK) {
                     const uint64_t rec = src[k];
@@ -966,8 +1009,9 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     if ((threadIdx.x & 31) == 0 && occ) atomicAdd(counters + 1, occ);
 }
 
-__host__ __device__ constexpr size_t sp_apply_smem(uint32_t region_words, uint32_t map_b) {
-    return sp_apply_layout(region_words, map_b).total;
+__host__ __device__ constexpr size_t sp_apply_smem(uint32_t region_words, uint32_t map_b,
+                                                   uint32_t rbuf_cap) {
+    return sp_apply_layout(region_words, map_b, rbuf_cap).total;
 }
 
 }  // namespace gdbg

@@ -120,6 +120,8 @@ struct SortParams {
     uint32_t* err;                // device status word
     uint32_t wait_cap;            // polls of a bulk-copy wait before giving up (0: WAIT_CAP)
     uint32_t map_bytes;           // apply: map space per CTA (set by its launcher)
+    uint32_t rbuf_cap;            // apply: records staged at once (set by its launcher)
+    uint32_t idx_bits;            // apply: record-index bits of a 32-bit map entry
 };
 
 // Persistent batch insert (gdbg_persist.cuh).
