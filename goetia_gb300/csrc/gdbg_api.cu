@@ -6,6 +6,7 @@
 // staging buffers for the host-pointer entry points.  All device work of a
 // handle runs on its stream in submission order.
 #include <algorithm>
+#include <cmath>
 #include <cerrno>
 #include <cstdio>
 #include <cstring>
@@ -121,6 +122,7 @@ struct gdbg_graph {
     DevBuf<uint32_t> hist, hist_off, scan_parts, bstart, new_bits;
     DevBuf<uint8_t> iq_vals;    // insert_and_query: post-insert value per table and k-mer
     DevBuf<uint32_t> sp_hist2, sp_off2, sp_plan;   // segmented path: pass-2 counts, plan
+    DevBuf<uint32_t> sp_fill, sp_end;              // spill word + per-bucket fill; bucket ends
     DevBuf<uint64_t> cq_keys;                      // compactor query: per-read new-k-mer sets
     DevBuf<uint32_t> cq_min, cq_ones;
     uint32_t* d_epoch = nullptr;
@@ -716,7 +718,28 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
     sp.nseg2_cap = sp.bins2 > 1 ? (uint32_t)(nrec / SP_SEG2 + sp.bins1 + 1) : 0u;
     const uint64_t h1 = (uint64_t)sp.bins1 * sp.nseg1;
     const uint64_t h2 = (uint64_t)sp.bins2 * sp.nseg2_cap;
-    GDBG_TRY(g->rec_a.ensure(nrec + 2));
+    // reserved pass-2 layout: a bucket of table i gets its expected records
+    // (the batch's k-mers times the bucket's share of the table) plus eight
+    // standard deviations of a Poisson count; a batch whose k-mers crowd
+    // some bucket past that takes the counted layout instead
+    uint64_t slots = nrec;
+    if (sp.bins2 > 1) {
+        uint64_t at = 0;
+        for (uint64_t i = 0; i < n; ++i) {
+            const double lam = (double)nk * (double)(1ull << fs) / (double)g->ts->sizes[i];
+            const uint64_t cap = ((uint64_t)std::ceil(lam + 8.0 * std::sqrt(lam) + 64.0) + 1) & ~1ull;
+            sp.cbase[i] = (uint32_t)std::min<uint64_t>(at, 0xFFFFFFFFull);
+            sp.bcap[i] = (uint32_t)std::min<uint64_t>(cap, 0xFFFFFFFFull);
+            at += (uint64_t)(sp.bbase[i + 1] - sp.bbase[i]) * cap;
+        }
+        if (at + SP_TILE < 0xFFFFFFFFull && at <= 2 * nrec + (1ull << 20)) {
+            slots = at;
+        } else {
+            for (uint64_t i = 0; i < n; ++i) sp.bcap[i] = sp.cbase[i] = 0;
+        }
+    }
+    sp.n_slots = (uint32_t)slots;
+    GDBG_TRY(g->rec_a.ensure(std::max(nrec, slots) + 2));
     GDBG_TRY(g->rec_b.ensure(nrec + 2));
     GDBG_TRY(g->hist.ensure(h1));
     GDBG_TRY(g->hist_off.ensure(h1));
@@ -727,7 +750,11 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
     GDBG_TRY(g->sp_plan.ensure(2 * (sp.bins1 + 1)));
     GDBG_TRY(g->scan_parts.ensure(scan32_partials_needed(std::max(h1, h2)) + 1));
     GDBG_TRY(g->bstart.ensure(nb + 1));
+    GDBG_TRY(g->sp_end.ensure(nb + 1));
+    GDBG_TRY(g->sp_fill.ensure(nb + 1));
     GDBG_TRY(g->new_bits.ensure(nk / 32 + 2));
+    sp.spill = g->sp_fill.p;
+    sp.bfill = g->sp_fill.p + 1;
     sp.hist1 = g->hist.p;
     sp.off1 = g->hist_off.p;
     sp.hist2 = h2 ? g->sp_hist2.p : nullptr;
@@ -772,14 +799,22 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
     }
     {
         Stage sg(g, "k_sp_part", st);
-        if ((e = launch_sp_part(false, st, sp, g->rec_a.p, g->rec_b.p)) != cudaSuccess)
+        if ((e = launch_sp_part(SP_PASS1, st, sp, g->rec_a.p, g->rec_b.p)) != cudaSuccess)
             return set_error_launch(e, "segment partition");
     }
     g->launches += 4;   // emit, 2 scan kernels, partition
     const uint64_t* fin = g->rec_b.p;
     if (sp.bins2 > 1) {
-        GDBG_CUDA(cudaMemsetAsync(sp.hist2, 0, h2 * sizeof(uint32_t), st));
+        // the reserved layout first; the counted one (counts, scan, pass)
+        // only does work when a bucket outgrew its reserved slots
+        const bool reserved = sp.bcap[0] != 0;
+        GDBG_CUDA(cudaMemsetAsync(g->sp_fill.p, 0, (nb + 1) * sizeof(uint32_t), st));
         if ((e = launch_sp_plan(st, sp)) != cudaSuccess) return set_error_launch(e, "segment plan");
+        if (reserved) {
+            Stage sg(g, "k_sp_part", st);
+            if ((e = launch_sp_part(SP_PASS2_RESERVED, st, sp, g->rec_b.p, g->rec_a.p)) != cudaSuccess)
+                return set_error_launch(e, "segment partition");
+        }
         {
             Stage sg(g, "k_sp_hist2", st);
             if ((e = launch_sp_hist2(st, sp, g->rec_b.p)) != cudaSuccess)
@@ -787,22 +822,23 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
         }
         {
             Stage sg(g, "k_scan32", st);
-            if ((e = launch_scan32(sp.hist2, sp.off2, h2, g->scan_parts.p, st)) != cudaSuccess)
+            if ((e = launch_scan32(sp.hist2, sp.off2, h2, g->scan_parts.p, st,
+                                   reserved ? sp.spill : nullptr)) != cudaSuccess)
                 return set_error_launch(e, "segment scan");
         }
         {
             Stage sg(g, "k_sp_part", st);
-            if ((e = launch_sp_part(true, st, sp, g->rec_b.p, g->rec_a.p)) != cudaSuccess)
+            if ((e = launch_sp_part(SP_PASS2_COUNTED, st, sp, g->rec_b.p, g->rec_a.p)) != cudaSuccess)
                 return set_error_launch(e, "segment partition");
         }
         fin = g->rec_a.p;
-        g->launches += 5;   // plan, counts, 2 scan kernels, partition
+        g->launches += reserved ? 6 : 5;   // plan, [reserved pass], counts, 2 scan kernels, counted pass
     }
-    if ((e = launch_sp_starts(st, sp, g->bstart.p)) != cudaSuccess)
+    if ((e = launch_sp_starts(st, sp, g->bstart.p, g->sp_end.p)) != cudaSuccess)
         return set_error_launch(e, "bucket starts");
     {
         Stage sg(g, "k_sp_apply", st);
-        if ((e = launch_sp_apply(g->storage, g->ts->tp, sp, fin, g->bstart.p, g->new_bits.p,
+        if ((e = launch_sp_apply(g->storage, g->ts->tp, sp, fin, g->bstart.p, g->sp_end.p, g->new_bits.p,
                                  g->ts->d_counters, st)) != cudaSuccess)
             return set_error_launch(e, "segment apply");
     }
@@ -1246,6 +1282,7 @@ int gdbg_destroy(gdbg_graph* g) {
     g->rec_a.release(); g->rec_b.release(); g->hist.release(); g->hist_off.release();
     g->scan_parts.release(); g->bstart.release(); g->new_bits.release(); g->iq_vals.release();
     g->sp_hist2.release(); g->sp_off2.release(); g->sp_plan.release();
+    g->sp_fill.release(); g->sp_end.release();
     g->cq_keys.release(); g->cq_min.release(); g->cq_ones.release();
     g->st_packed.release(); g->st_offsets.release(); g->st_out64.release();
     g->st_out64b.release(); g->st_out64c.release(); g->st_counts.release(); g->st_u8.release();

@@ -120,8 +120,10 @@ __device__ __forceinline__ uint32_t block_scan32(uint32_t v, uint32_t* ws) {
 }
 
 __global__ void __launch_bounds__(SCAN32_BLOCK)
-k_scan32_partials(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ partials) {
+k_scan32_partials(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ partials,
+                  const uint32_t* gate) {
     __shared__ uint32_t ws[32];
+    if (gate && *(volatile const uint32_t*)gate == 0) return;
     const uint64_t base = ((uint64_t)blockIdx.x * SCAN32_BLOCK + threadIdx.x) * SCAN32_ITEMS;
     uint32_t s = 0;
 #pragma unroll
@@ -135,9 +137,10 @@ k_scan32_partials(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restr
 // most), so no separate pass scans the partials.
 __global__ void __launch_bounds__(SCAN32_BLOCK)
 k_scan32_final(const uint32_t* __restrict__ in, uint64_t n, const uint32_t* __restrict__ partials,
-               uint32_t* __restrict__ out) {
+               uint32_t* __restrict__ out, const uint32_t* gate) {
     __shared__ uint32_t ws[32];
     __shared__ uint32_t before_s;
+    if (gate && *(volatile const uint32_t*)gate == 0) return;
     uint32_t pre = 0;
     for (uint32_t i = threadIdx.x; i < blockIdx.x; i += SCAN32_BLOCK) pre += partials[i];
     pre = block_scan32(pre, ws);
@@ -164,11 +167,11 @@ uint64_t scan32_partials_needed(uint64_t n) {
 }
 
 cudaError_t launch_scan32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* partials,
-                          cudaStream_t st) {
+                          cudaStream_t st, const uint32_t* gate) {
     if (n == 0) return cudaSuccess;
     const uint64_t nb = (n + SCAN32_BLOCK * SCAN32_ITEMS - 1) / (SCAN32_BLOCK * SCAN32_ITEMS);
-    k_scan32_partials<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials);
-    k_scan32_final<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials, out);
+    k_scan32_partials<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials, gate);
+    k_scan32_final<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials, out, gate);
     return cudaGetLastError();
 }
 

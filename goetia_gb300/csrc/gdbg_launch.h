@@ -71,8 +71,10 @@ cudaError_t launch_iq_counts(const uint8_t* vals, uint64_t cap, uint32_t n_table
 cudaError_t launch_bucket_read_new(const uint64_t* kofs, uint64_t n_reads, const uint32_t* new_bits,
                                    uint64_t* n_new, unsigned long long* counters, cudaStream_t st);
 uint64_t scan32_partials_needed(uint64_t n);
+// Exclusive scan of n uint32.  With a gate, the kernels return at once
+// unless *gate is non-zero when they run.
 cudaError_t launch_scan32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* partials,
-                          cudaStream_t st);
+                          cudaStream_t st, const uint32_t* gate = nullptr);
 
 // Batch preparation (gdbg_batch.cu): per-read k-mer prefix and tile map.
 // Validates offsets (non-decreasing, within max_bases) on the device; a bad
@@ -91,14 +93,18 @@ cudaError_t launch_tile_map(const uint64_t* kofs, uint64_t n_reads, uint64_t n_t
 cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
                            const TableParams& tp, const SortParams& sp, uint64_t* rout,
                            uint32_t seg0, uint32_t n_seg);
-cudaError_t launch_sp_part(bool pass2, cudaStream_t st, const SortParams& sp, const uint64_t* rin,
+// Partition passes: pass 1, pass 2 into the reserved layout, pass 2 into the
+// counted layout (a no-op when the reserved one was made and held).
+enum { SP_PASS1 = 0, SP_PASS2_RESERVED = 1, SP_PASS2_COUNTED = 2 };
+cudaError_t launch_sp_part(int pass, cudaStream_t st, const SortParams& sp, const uint64_t* rin,
                            uint64_t* rout);
 cudaError_t launch_sp_plan(cudaStream_t st, const SortParams& sp);
 cudaError_t launch_sp_hist2(cudaStream_t st, const SortParams& sp, const uint64_t* rin);
-cudaError_t launch_sp_starts(cudaStream_t st, const SortParams& sp, uint32_t* start);
+// Record range [start[b], end[b]) of every bucket.
+cudaError_t launch_sp_starts(cudaStream_t st, const SortParams& sp, uint32_t* start, uint32_t* end);
 cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams& sp,
-                            const uint64_t* recs, const uint32_t* start, uint32_t* new_bits,
-                            unsigned long long* counters, cudaStream_t st);
+                            const uint64_t* recs, const uint32_t* start, const uint32_t* end,
+                            uint32_t* new_bits, unsigned long long* counters, cudaStream_t st);
 size_t sp_apply_smem_bytes(int storage, uint32_t fs);
 
 // Compactor query (gdbg_compactor.cu): per k-mer new / seen flags and the

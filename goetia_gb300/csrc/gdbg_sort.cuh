@@ -15,19 +15,18 @@
 //      into segments of SP_SEG2 records that never cross a group, counted by
 //      the low digit and partitioned again; the scan is laid out group by
 //      group, so its entries are final record positions and bucket starts.
-//   4. k_sp_apply: one CTA per bucket loads its table region and records
-//      into shared memory.  The records of a bucket are in no particular
-//      order, so the first toucher of a cell is found as the minimum k-mer
-//      ordinal over all the bucket's records: pass 1 puts every cell that is
-//      zero in the region into a shared-memory map keyed by cell, holding
-//      the minimum ordinal; pass 2 applies every record and flags the map's
-//      minimum as new.  A region whose zero cells overflow the map is done
-//      in narrower cell ranges.  That is the reference's sequential rule
-//      (bitstorage.hh:195-219, bytestorage.cc:60-113, nibblestorage.cc:
-//      60-100) cell by cell; a cell's final value does not depend on the
-//      order of its increments.
+//   4. k_sp_apply: one CTA per bucket bulk-copies its table region into
+//      shared memory and reads the bucket's records, which are in no
+//      particular order, once.  A cell that was not zero before the batch
+//      takes its saturating increments at once; a zero cell stays zero
+//      while a shared-memory map counts its touches and keeps the minimum
+//      k-mer ordinal among them -- its first toucher, which is new -- and
+//      gets min(max, touches) after the last record.  Zero cells that
+//      overflow the map are redone in narrower cell ranges.  That is the
+//      reference's sequential rule (bitstorage.hh:195-219, bytestorage.cc:
+//      60-113, nibblestorage.cc:60-100) cell by cell; a cell's final value
+//      does not depend on the order of its increments.
 #pragma once
-#include <type_traits>
 
 #include "gdbg_persist.cuh"
 
@@ -364,10 +363,17 @@ __global__ void __launch_bounds__(SP_PART_BLOCK)
 k_sp_hist2(SortParams sp, const uint64_t* __restrict__ rin) {
     __shared__ uint32_t cnt[SP_MAXBINS2];
     __shared__ Seg2 sg;
+    // only for the counted layout: not needed when the reserved one held
+    if (sp.bcap[0] != 0 && *(volatile const uint32_t*)sp.spill == 0) return;
     if (threadIdx.x == 0) sg = seg2_of(sp, blockIdx.x);
     for (uint32_t k = threadIdx.x; k < sp.bins2; k += SP_PART_BLOCK) cnt[k] = 0;
     __syncthreads();
-    if (!sg.valid) return;
+    if (!sg.valid) {
+        // past the last segment: the scan's tail entries, zeroed here
+        const uint64_t tail = (uint64_t)sp.bins2 * blockIdx.x;
+        for (uint32_t d = threadIdx.x; d < sp.bins2; d += SP_PART_BLOCK) sp.hist2[tail + d] = 0;
+        return;
+    }
     const uint32_t mask = sp.bins2 - 1;
     constexpr int U = 8;   // loads in flight per thread
     for (uint32_t k0 = sg.rs + threadIdx.x; k0 < sg.re; k0 += U * SP_PART_BLOCK) {
@@ -395,7 +401,10 @@ __host__ __device__ constexpr size_t sp_part_smem() {
     return (size_t)(SP_NBUF * SP_BUF + SP_TILE) * 8;
 }
 
-template <bool PASS2>
+// PASS2 && RESERVE: the reserved layout (places taken per tile by atomics);
+// PASS2 && !RESERVE: the counted layout, which does nothing when the
+// reserved one was made and held.
+template <bool PASS2, bool RESERVE>
 __global__ void __launch_bounds__(SP_PART_BLOCK, 2)
 k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict__ rout) {
     extern __shared__ __align__(128) uint64_t sm[];
@@ -405,9 +414,10 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
     __shared__ uint32_t cnt[MB], lstart[MB], cursor[MB], delta[MB];
     __shared__ uint32_t wsum[SP_PART_BLOCK / 32];
     __shared__ __align__(8) uint64_t bars[SP_NBUF];
-    __shared__ uint32_t rs_s, re_s, abort_s;
+    __shared__ uint32_t rs_s, re_s, abort_s, group_s;
     const uint32_t tid = threadIdx.x;
     const uint32_t bins = PASS2 ? sp.bins2 : sp.bins1;
+    if (PASS2 && !RESERVE && sp.bcap[0] != 0 && *(volatile const uint32_t*)sp.spill == 0) return;
     if (tid == 0) {
         uint32_t rs = 0, re = 0;
         if (PASS2) {
@@ -415,6 +425,7 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
             if (sg.valid) {
                 rs = sg.rs;
                 re = sg.re;
+                group_s = sg.group;
             }
         } else {
             const uint64_t nr = sp_records(sp);
@@ -433,20 +444,24 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
     const uint32_t rs = rs_s, re = re_s;
     if (rs >= re) return;
     // segment cursors
-    if (PASS2) {
+    if (PASS2 && !RESERVE) {
         const Seg2 sg = seg2_of(sp, blockIdx.x);
         const uint64_t base = (uint64_t)sp.bins2 * sp.plan[sg.group];
         for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK)
             cursor[d] = sp.off2[base + (uint64_t)d * sg.nseg + sg.k];
-    } else {
+    } else if (!PASS2) {
         for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK)
             cursor[d] = sp.off1[(uint64_t)d * sp.nseg1 + blockIdx.x];
     }
+    const uint32_t group = PASS2 ? group_s : 0u;
     const uint32_t n_tiles = (re - rs + SP_TILE - 1) / SP_TILE;
     // digit of a record: (cell >> (fs + shift)) & mask
     const uint32_t dshift = sp.fs + (PASS2 ? 0u : sp.hi_shift);
     const uint32_t mask = PASS2 ? sp.bins2 - 1 : 0xFFFFFFFFu;
     const uint32_t n_recs = (uint32_t)sp_records(sp);
+    // output slots: the records, or the reserved layout's slots (a run that
+    // found its bucket full goes to n_slots, past the end, and is dropped)
+    const uint32_t limit = RESERVE ? sp.n_slots : n_recs;
     const uint32_t lane = tid & 31u, w = tid >> 5;
     // tile i covers records [rs + i*SP_TILE, ...); its copy starts at the
     // even index at or below, so the copy is 16-byte aligned and sized
@@ -516,8 +531,23 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
             for (uint32_t q = 0; q < w; ++q) pre += wsum[q];
             const uint32_t ex = pre + inc - c;
             lstart[tid] = ex;
-            delta[tid] = cursor[tid] - ex;
-            cursor[tid] += c;
+            if (RESERVE) {
+                uint32_t dl = sp.n_slots;
+                if (c) {
+                    const uint32_t bk = (group << sp.hi_shift) | tid;
+                    int ti = 0;
+                    while (ti + 1 < (int)sp.n_tables && sp.bbase[ti + 1] <= bk) ++ti;
+                    const uint32_t at = atomicAdd(sp.bfill + bk, c);
+                    if (at + c <= sp.bcap[ti])
+                        dl = sp.cbase[ti] + (bk - sp.bbase[ti]) * sp.bcap[ti] + at - ex;
+                    else
+                        atomicExch(sp.spill, 1u);
+                }
+                delta[tid] = dl;
+            } else {
+                delta[tid] = cursor[tid] - ex;
+                cursor[tid] += c;
+            }
         }
         __syncthreads();
 #pragma unroll
@@ -533,8 +563,8 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
             if (k < nt) {
                 const uint64_t v = stage[k];
                 const uint32_t p = delta[((uint32_t)(v >> 32) >> dshift) & mask] + k;
-                if (p < n_recs) rout[p] = v;
-                else atomicOr(sp.err, GDBG_ERR_PARTITION);
+                if (p < limit) rout[p] = v;
+                else if (!RESERVE) atomicOr(sp.err, GDBG_ERR_PARTITION);
             }
         }
     }
@@ -542,207 +572,145 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
 
 // ---- 3d. bucket starts ---------------------------------------------------------
 
-__global__ void k_sp_starts(SortParams sp, uint32_t* __restrict__ start) {
-    const uint32_t bk = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n_recs = (uint32_t)sp_records(sp);
-    if (bk > sp.n_buckets) return;
-    if (bk == sp.n_buckets) {
-        start[bk] = n_recs;
-        return;
-    }
-    if (sp.bins2 == 1) {
-        start[bk] = sp.off1[(uint64_t)bk * sp.nseg1];
-        return;
-    }
+// First record of bucket bk in the counted layout (bk == n_buckets: the end).
+__device__ __forceinline__ uint32_t sp_counted_start(const SortParams& sp, uint32_t bk,
+                                                     uint32_t n_recs) {
+    if (bk >= sp.n_buckets) return n_recs;
+    if (sp.bins2 == 1) return sp.off1[(uint64_t)bk * sp.nseg1];
     const uint32_t* s0 = sp.plan;
     const uint32_t* G = sp.plan + sp.bins1 + 1;
     const uint32_t g = bk >> sp.hi_shift, d = bk & (sp.bins2 - 1);
     const uint32_t nseg = s0[g + 1] - s0[g];
-    start[bk] = nseg ? sp.off2[(uint64_t)sp.bins2 * s0[g] + (uint64_t)d * nseg] : G[g];
+    return nseg ? sp.off2[(uint64_t)sp.bins2 * s0[g] + (uint64_t)d * nseg] : G[g];
+}
+
+// Record range [start, end) of every bucket, in whichever layout pass 2 made.
+__global__ void k_sp_starts(SortParams sp, uint32_t* __restrict__ start, uint32_t* __restrict__ end) {
+    const uint32_t bk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bk >= sp.n_buckets) return;
+    if (sp.bcap[0] != 0 && *(volatile const uint32_t*)sp.spill == 0) {
+        int ti = 0;
+        while (ti + 1 < (int)sp.n_tables && sp.bbase[ti + 1] <= bk) ++ti;
+        const uint32_t a = sp.cbase[ti] + (bk - sp.bbase[ti]) * sp.bcap[ti];
+        start[bk] = a;
+        end[bk] = a + sp.bfill[bk];
+        return;
+    }
+    const uint32_t n_recs = (uint32_t)sp_records(sp);
+    start[bk] = sp_counted_start(sp, bk, n_recs);
+    end[bk] = sp_counted_start(sp, bk + 1, n_recs);
 }
 
 // ---- 4. order-independent apply -------------------------------------------
 
-// Shared memory of the apply: a bucket's records staged at once (up to
-// SortParams::rbuf_cap of them), its table region, and one map space used
-// two ways.  The single-chunk path (all of a bucket's records staged) keys
-// each zero cell to the staged record with the smallest ordinal, in 32-bit
-// entries (cell << idx_bits | record index); the chunked path (buckets of
-// more records than the buffer holds) keeps 64-bit entries (ordinal << 32 |
-// cell) and restages records per cell range.  The kernel is issue-bound, so
-// the launcher sizes the record buffer for the batch's expected bucket load
-// and the map space (8 or 16 KB) for the most CTAs per SM that leaves: three
-// with 32 KB regions, four with small regions and light buckets.
-constexpr uint32_t SP_RBUF_MIN = 4096, SP_RBUF_MAX = 8192;   // records staged at once
-constexpr uint32_t SP_MAP_MIN = 8192, SP_MAP_MAX = 16384;    // map space bytes
-constexpr uint32_t SP_EMPTY32 = 0xFFFFFFFFu;
-// Linear-probe limit of a map insert.  A map filled to half its slots needs
-// about two probes; a fuller one -- a fresh, empty table puts nearly every
-// cell of a region into the map -- would make each insert walk the whole map,
-// so an insert that runs this long reports the map full and the cell range is
-// narrowed.
+// Shared memory of the apply: the bucket's table region, a map of the zero
+// cells its records touch, and dirty-sector bits.  The records are read from
+// global memory once, by the threads, while the region's bulk copy is in
+// flight; the kernel is issue-bound, so the launcher gives the map the
+// shared memory that four CTAs per SM leave beside their regions.
+//
+// A cell that is not zero before the batch takes its records' saturating
+// increments directly.  A cell that is zero stays zero while the records are
+// read: the map counts its touches and keeps the smallest k-mer ordinal among
+// them (its first toucher, so that k-mer is new), and the value, min(max,
+// touches), is written after the last record.  Since no zero cell changes
+// before then, the zero test of a record does not depend on which records ran
+// first.
+//
+// Map entry: (smallest ordinal << 32) | (cell << SP_TOUCH_BITS) | touches
+// (saturating); cells of a region are below 2^20.
+constexpr uint32_t SP_TOUCH_BITS = 12;
+constexpr uint32_t SP_TOUCH_MAX = (1u << SP_TOUCH_BITS) - 1u;
+// Linear-probe limit of a map entry.  A map filled to half its slots needs
+// about two probes; an insert that runs this long reports the map full (a
+// fresh table can put nearly every cell of a region in it), and the zero
+// cells are then redone in narrower cell ranges.
 constexpr uint32_t SP_PROBE_CAP = 64;
-
-__device__ __forceinline__ uint32_t sp_slot_bits(uint32_t co, uint32_t bits) {
-    return (co * 0x9E3779B1u) >> (32 - bits);
-}
+constexpr int SP_APPLY_CTAS = 4;    // CTAs per SM the launcher sizes the map for
+constexpr uint32_t SP_APPLY_U = 4;  // records each thread has in flight
 
 // Shared-memory layout of k_sp_apply (byte offsets): region words (padded
-// to 16 bytes), map space, record buffer (+2 alignment slack), dirty
-// sector bits.
+// to 16 bytes), map slots, the list of created slots (16-bit, padded to 16
+// bytes), dirty sector bits.
 struct ApplyLayout {
-    uint32_t map_off, rec_off, dirty_off, total;
+    uint32_t map_off, list_off, dirty_off, total;
 };
-__host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words, uint32_t map_b,
-                                                         uint32_t rbuf_cap) {
+__host__ __device__ constexpr ApplyLayout sp_apply_layout(uint32_t region_words, uint32_t slots) {
     const uint32_t region_b = ((region_words + 3u) & ~3u) * 4u;
-    const uint32_t rec_b = (rbuf_cap + 2u) * 8u;
+    const uint32_t list_b = ((slots * 2u) + 15u) & ~15u;
     const uint32_t dirty_b = (((region_words + 7u) / 8u + 31u) / 32u) * 4u;
-    return ApplyLayout{region_b, region_b + map_b, region_b + map_b + rec_b,
-                       region_b + map_b + rec_b + dirty_b};
+    return ApplyLayout{region_b, region_b + slots * 8u, region_b + slots * 8u + list_b,
+                       region_b + slots * 8u + list_b + dirty_b};
+}
+__host__ __device__ constexpr size_t sp_apply_smem(uint32_t region_words, uint32_t slots) {
+    return sp_apply_layout(region_words, slots).total;
 }
 
-// After pass 1 the map holds every cell of the range that was zero before
-// the batch, with the minimum ordinal of its records: that k-mer is the
-// cell's first toucher, so it is new.  Each thread reads its own slots.
-__device__ __forceinline__ void sp_map_winners(const uint64_t* map, uint32_t slots,
-                                               const SortParams& sp, int ti,
-                                               uint32_t* __restrict__ new_bits,
-                                               unsigned long long& occ) {
-    for (uint32_t k = threadIdx.x; k < slots; k += SP_APPLY_BLOCK) {
-        const uint64_t e = map[k];
-        if (e == SP_EMPTY) continue;
-        const uint32_t g = (uint32_t)(e >> 32);
-        if (g < sp.kmer_cap) {
-            atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
-            if (ti == 0) ++occ;
-        }
-    }
+__device__ __forceinline__ uint32_t sp_home(uint32_t co, uint32_t slots) {
+    return __umulhi(co * 0x9E3779B1u, slots);
 }
 
-// Chunked-path map insert of a zero cell with ordinal g (2^bits slots): the
-// slot index, or the slot count when the map is full; *created is set when
-// this call made the entry.
-__device__ __forceinline__ uint32_t sp_map_insert(uint64_t* map, uint32_t bits, uint32_t co,
-                                                  uint32_t g, bool* created) {
-    const uint32_t slots = 1u << bits;
-    const uint64_t mine = ((uint64_t)g << 32) | co;   // (ordinal << 32) | cell
-    uint32_t sl = sp_slot_bits(co, bits);
-    *created = false;
+// One touch of zero cell co by the k-mer with ordinal g; a new entry's slot
+// goes on the created list.  False when the probe limit ran out (the map is
+// too full).
+__device__ __forceinline__ bool sp_touch(uint64_t* map, uint32_t slots, uint32_t co, uint32_t g,
+                                         uint16_t* list, uint32_t* n_list) {
+    const uint32_t key = co << SP_TOUCH_BITS;
+    uint32_t sl = sp_home(co, slots);
     for (uint32_t it = 0; it < SP_PROBE_CAP; ++it) {
         uint64_t cur = map[sl];
         if (cur == SP_EMPTY) {
-            cur = atomicCAS((unsigned long long*)&map[sl], SP_EMPTY, mine);
+            cur = atomicCAS((unsigned long long*)(map + sl), SP_EMPTY,
+                            ((uint64_t)g << 32) | key | 1u);
             if (cur == SP_EMPTY) {
-                *created = true;
-                return sl;
+                list[atomicAdd(n_list, 1u)] = (uint16_t)sl;
+                return true;
             }
         }
-        if ((uint32_t)cur == co) {
-            if (mine < cur) atomicMin((unsigned long long*)&map[sl], mine);
-            return sl;
-        }
-        sl = (sl + 1) & (slots - 1);
-    }
-    return slots;
-}
-
-// Single-chunk map insert (2^bits slots): zero cell co touched by staged
-// record k (below 2^ib).  The slot keeps the cell's record with the
-// smallest ordinal (records of one bucket never share an ordinal: a k-mer
-// has one cell per table).  Returns the slot, or the slot count when the map
-// is full; *created when this call made it.
-__device__ __forceinline__ uint32_t sp_map32_insert(uint32_t* map, uint32_t bits, uint32_t ib,
-                                                    const uint64_t* src, uint32_t co, uint32_t k,
-                                                    bool* created) {
-    const uint32_t slots = 1u << bits, im = (1u << ib) - 1u;
-    const uint32_t mine = (co << ib) | k;
-    const uint32_t g = (uint32_t)src[k];
-    uint32_t sl = sp_slot_bits(co, bits);
-    *created = false;
-    for (uint32_t it = 0; it < SP_PROBE_CAP; ++it) {
-        uint32_t cur = map[sl];
-        if (cur == SP_EMPTY32) {
-            cur = atomicCAS(map + sl, SP_EMPTY32, mine);
-            if (cur == SP_EMPTY32) {
-                *created = true;
-                return sl;
-            }
-        }
-        if ((cur >> ib) == co) {
-            // the same cell: this record takes the slot while its ordinal is
-            // smaller (each successful swap lowers the ordinal held)
-            for (uint32_t t = 0; t < slots && (uint32_t)src[cur & im] > g; ++t) {
-                const uint32_t prev = atomicCAS(map + sl, cur, mine);
+        if (((uint32_t)cur & ~SP_TOUCH_MAX) == key) {
+            // the cell's entry: one more touch, the smaller ordinal (every
+            // failed swap means another touch of this cell went in)
+            for (uint32_t t = 0; t < (1u << 20); ++t) {
+                const uint32_t o = (uint32_t)(cur >> 32) < g ? (uint32_t)(cur >> 32) : g;
+                const uint32_t n = (uint32_t)cur & SP_TOUCH_MAX;
+                const uint64_t want = ((uint64_t)o << 32) | key | (n + (n < SP_TOUCH_MAX ? 1u : 0u));
+                const uint64_t prev = atomicCAS((unsigned long long*)(map + sl), cur, want);
                 if (prev == cur) break;
                 cur = prev;
             }
-            return sl;
+            return true;
         }
-        sl = (sl + 1) & (slots - 1);
-    }
-    return slots;
-}
-
-// Saturating increment of one region cell; true when the word changed.
-template <int STORAGE>
-__device__ __forceinline__ bool sp_increment(uint32_t* region, uint32_t word, uint32_t shift) {
-    if (STORAGE == GDBG_BIT) {
-        const uint32_t bit = 1u << shift;
-        return (atomicOr(region + word, bit) & bit) == 0;
-    }
-    uint32_t cur = region[word];
-    for (int it = 0; it < (1 << 20); ++it) {
-        if (cell_value<STORAGE>(cur, shift) >= cell_max<STORAGE>()) return false;
-        const uint32_t prev = atomicCAS(region + word, cur, cur + (1u << shift));
-        if (prev == cur) return true;
-        cur = prev;
+        if (++sl == slots) sl = 0;
     }
     return false;
 }
 
-// One CTA per bucket; the region and the bucket's records are bulk-copied
-// into shared memory.  Pass 1 puts every cell that is zero in the region
-// into the map with the minimum k-mer ordinal of its records; pass 2 applies
-// every record (saturating increment) and flags the map's minimum as new.
-// A bucket whose records fit one staging buffer keeps each record's map slot
-// from pass 1 (pass 2 looks up nothing); larger or denser buckets take the
-// general loop over buffer chunks and cell ranges.
-// MAPB: map space bytes (SortParams::map_bytes), IB: record-index bits of a
-// single-chunk map entry (SortParams::idx_bits); compile-time, so the map's
-// hashing and entry packing take no run-time shifts.
-template <int STORAGE, uint32_t MAPB, uint32_t IB>
-__global__ void __launch_bounds__(SP_APPLY_BLOCK, 4)
+// One CTA per bucket.  Pass over the records: increments of cells that were
+// not zero, touches of zero cells into the map; then each zero cell gets its
+// value and its first toucher is flagged new.  When the zero cells overflow
+// the map, they are redone in narrower cell ranges (the increments stand).
+template <int STORAGE>
+__global__ void __launch_bounds__(SP_APPLY_BLOCK, SP_APPLY_CTAS)
 k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
-           const uint32_t* __restrict__ start, uint32_t* __restrict__ new_bits,
-           unsigned long long* counters) {
+           const uint32_t* __restrict__ start, const uint32_t* __restrict__ end,
+           uint32_t* __restrict__ new_bits, unsigned long long* counters) {
     extern __shared__ __align__(128) unsigned char sbytes[];
-    __shared__ uint32_t n_fresh, overflow, abort_s;
+    __shared__ uint32_t overflow, abort_s, n_list;
     __shared__ __align__(8) uint64_t bar;
-    __shared__ uint32_t used[SP_MAP_MAX / 4 / 32];   // single-chunk map slots created
+    const uint32_t tid = threadIdx.x;
     const uint32_t bk = blockIdx.x;
-    const uint32_t rs = start[bk], re = start[bk + 1];
+    const uint32_t rs = start[bk], re = end[bk];
     if (rs >= re) return;
     int ti = 0;
     while (ti + 1 < tp.n && sp.bbase[ti + 1] <= bk) ++ti;
     const uint32_t region_cells = 1u << sp.fs;
     const uint32_t region_words = region_cells / cells_per_word<STORAGE>();
     const uint32_t region_sectors = (region_words + 7) / 8;
-    const uint32_t RB = sp.rbuf_cap;   // records staged at once
-    const ApplyLayout L = sp_apply_layout(region_words, sp.map_bytes, RB);
-    // map slots: 32-bit entries for the single-chunk path, 64-bit for the chunked one
-    constexpr uint32_t slots32 = MAPB / 4u, bits32 = slots32 == 4096u ? 12u : 11u;
-    // entries (cell << IB | index) never reach the all-ones empty entry
-    if (sp.fs + IB > 31u) {
-        if (threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_PARTITION);
-        return;
-    }
-    constexpr uint32_t bits64 = bits32 - 1u, slots64 = 1u << bits64;
-    static_assert((1u << bits32) == slots32, "map space of 8 or 16 KB");
+    const uint32_t slots = sp.map_slots;
+    const ApplyLayout L = sp_apply_layout(region_words, slots);
     uint32_t* region = reinterpret_cast<uint32_t*>(sbytes);
-    uint64_t* map = reinterpret_cast<uint64_t*>(sbytes + L.map_off);     // chunked path
-    uint32_t* map32 = reinterpret_cast<uint32_t*>(sbytes + L.map_off);   // single-chunk path
-    uint64_t* rbuf = reinterpret_cast<uint64_t*>(sbytes + L.rec_off);
+    uint64_t* map = reinterpret_cast<uint64_t*>(sbytes + L.map_off);
+    uint16_t* list = reinterpret_cast<uint16_t*>(sbytes + L.list_off);
     uint32_t* dirty = reinterpret_cast<uint32_t*>(sbytes + L.dirty_off);
     const uint64_t c0 = (uint64_t)(bk - sp.bbase[ti]) << sp.fs;
     const uint64_t w0 = c0 / cells_per_word<STORAGE>();
@@ -752,248 +720,150 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
     // the region by one bulk copy when it is a whole number of 16-byte units
     const bool bulk_region = ((w0 & 3u) == 0) && ((nw & 3u) == 0);
     const uint32_t n_recs = re - rs;
-    const uint32_t n_chunks = (n_recs + RB - 1) / RB;
+    const uint64_t* brec = recs + rs;
     // dense buckets write the whole region back; sparse ones their dirty sectors
     const bool track = n_recs < region_sectors;
-    uint32_t phase = 0;
-    // records of chunk c into rbuf, copied from the even index at or below
-    // its first record (and the region with chunk 0)
-    auto chunk_copy = [&](uint32_t c, bool with_region) {
-        const uint32_t a = rs + c * RB;
-        const uint32_t b = a + RB < re ? a + RB : re;
-        const uint32_t a0 = a & ~1u, a1 = (b + 1) & ~1u;
-        const uint32_t bytes = (a1 - a0) * 8u + (with_region ? nw * 4u : 0u);
-        mbar_expect(&bar, bytes);
-        if (with_region) bulk_load(region, gsrc, nw * 4u, &bar);
-        bulk_load(rbuf, recs + a0, (a1 - a0) * 8u, &bar);
-    };
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         abort_s = 0;
-        n_fresh = 0;
         overflow = 0;
-        mbar_init(&bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        chunk_copy(0, bulk_region);
+        n_list = 0;
+        if (bulk_region) {
+            mbar_init(&bar, 1);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            mbar_expect(&bar, nw * 4u);
+            bulk_load(region, gsrc, nw * 4u, &bar);
+        }
     }
     if (!bulk_region)
-        for (uint32_t k = threadIdx.x; k < nw; k += SP_APPLY_BLOCK) region[k] = __ldcs(gsrc + k);
+        for (uint32_t k = tid; k < nw; k += SP_APPLY_BLOCK) region[k] = __ldcs(gsrc + k);
     if (track)
-        for (uint32_t k = threadIdx.x; k < (region_sectors + 31) / 32; k += SP_APPLY_BLOCK) dirty[k] = 0;
-    for (uint32_t k = threadIdx.x; k < slots32; k += SP_APPLY_BLOCK) map32[k] = SP_EMPTY32;
-    for (uint32_t k = threadIdx.x; k < slots32 / 32; k += SP_APPLY_BLOCK) used[k] = 0;
+        for (uint32_t k = tid; k < (region_sectors + 31) / 32; k += SP_APPLY_BLOCK) dirty[k] = 0;
+    for (uint32_t k = tid; k < slots; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
+    // the first records in flight while the region arrives
+    uint64_t r[SP_APPLY_U];
+#pragma unroll
+    for (uint32_t u = 0; u < SP_APPLY_U; ++u) {
+        const uint32_t k = tid + u * SP_APPLY_BLOCK;
+        r[u] = k < n_recs ? __ldcs(brec + k) : 0ull;
+    }
     __syncthreads();   // the barrier is initialised before anyone waits on it
-    if (!copy_wait(sp, &bar, phase & 1u)) atomicExch(&abort_s, 1u);
-    ++phase;
+    if (bulk_region && !copy_wait(sp, &bar, 0)) atomicExch(&abort_s, 1u);
     __syncthreads();
     if (abort_s) {
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             atomicOr(sp.err, GDBG_ERR_COPY_TIMEOUT);
-            mbar_wait(&bar, (phase - 1) & 1u);
+            mbar_wait(&bar, 0);
         }
         return;
     }
     const uint32_t co_mask = region_cells - 1;
-    unsigned long long occ = 0;
-    bool done = false;
-    if (n_chunks == 1) {
-        // all records staged: the whole region as one cell range first, then,
-        // when its zero cells overflow the map, narrower ranges
-        const uint64_t* src = rbuf + (rs & 1u);
-        constexpr uint32_t ib = IB, im = (1u << IB) - 1u;
-        // pass 1 over [lo, hi): the staged record with the minimum ordinal per
-        // zero cell; true when the range fits the map
-        // (generic lambdas: the whole-region form is compiled without the
-        // range test)
-        auto map_pass = [&](auto whole_c, uint32_t lo, uint32_t hi) -> bool {
-            constexpr bool whole = decltype(whole_c)::value;
-            uint32_t inserted = 0;
-            bool lost = false;
-            for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
-                const uint64_t rec = src[k];
-                const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
-                if (!whole && (co < lo || co >= hi)) continue;
-                uint32_t word, shift;
-                region_cell<STORAGE>(co, word, shift);
-                // once the map has overflowed the range is redone narrower:
-                // the remaining inserts are skipped
-                if (cell_value<STORAGE>(region[word], shift) == 0 && !*(volatile uint32_t*)&overflow) {
-                    bool created;
-                    const uint32_t sl = sp_map32_insert(map32, bits32, ib, src, co, k, &created);
-                    inserted += created;
-                    if (sl >= slots32) {
-                        lost = true;
-                        overflow = 1;
-                    }
-                    if (created) atomicOr(&used[sl >> 5], 1u << (sl & 31u));
-                }
+    auto mark = [&](uint32_t word) {
+        const uint32_t sec = word >> 3;
+        atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
+    };
+    // the pass over the records
+    for (uint32_t k0 = 0; k0 < n_recs; k0 += SP_APPLY_U * SP_APPLY_BLOCK) {
+        if (k0) {
+#pragma unroll
+            for (uint32_t u = 0; u < SP_APPLY_U; ++u) {
+                const uint32_t k = k0 + tid + u * SP_APPLY_BLOCK;
+                r[u] = k < n_recs ? __ldcs(brec + k) : 0ull;
             }
-            inserted = __reduce_add_sync(0xFFFFFFFFu, inserted);
-            if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
-            if (lost) overflow = 1;
-            __syncthreads();
-            return !overflow && n_fresh <= slots32 / 2;
-        };
-        // pass 2 over [lo, hi): every record applied; then the map's entries
-        // (the first touchers) flagged new
-        auto apply_pass = [&](auto whole_c, uint32_t lo, uint32_t hi) {
-            constexpr bool whole = decltype(whole_c)::value;
-            for (uint32_t k = threadIdx.x; k < n_recs; k += SP_APPLY_BLOCK) {
-                const uint64_t rec = src[k];
-                const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
-                if (!whole && (co < lo || co >= hi)) continue;
-                uint32_t word, shift;
-                region_cell<STORAGE>(co, word, shift);
-                const bool changed = sp_increment<STORAGE>(region, word, shift);
-                if (track && changed) {
-                    const uint32_t sec = word >> 3;
-                    atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
-                }
-            }
-            for (uint32_t wd = threadIdx.x; wd < slots32 / 32; wd += SP_APPLY_BLOCK) {
-                for (uint32_t m = used[wd]; m; m &= m - 1) {
-                    const uint32_t g = (uint32_t)src[map32[wd * 32 + __ffs(m) - 1] & im];
-                    if (g < sp.kmer_cap) {
-                        atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
-                        if (ti == 0) ++occ;
-                    }
-                }
-            }
-        };
-        auto clear_map = [&]() {
-            __syncthreads();   // everyone is done with the map and the counts
-            for (uint32_t k = threadIdx.x; k < slots32; k += SP_APPLY_BLOCK) map32[k] = SP_EMPTY32;
-            for (uint32_t k = threadIdx.x; k < slots32 / 32; k += SP_APPLY_BLOCK) used[k] = 0;
-            if (threadIdx.x == 0) {
-                n_fresh = 0;
-                overflow = 0;
-            }
-            __syncthreads();
-        };
-        using whole_t = std::true_type;
-        using ranged_t = std::false_type;
-        if (map_pass(whole_t{}, 0, region_cells)) {
-            apply_pass(whole_t{}, 0, region_cells);
-        } else {
-            uint32_t lo = 0, width = region_cells >> 1;
-            for (int guard = 0; lo < region_cells && guard < 4096; ++guard) {
-                const uint32_t hi = lo + width < region_cells ? lo + width : region_cells;
-                clear_map();
-                if (!map_pass(ranged_t{}, lo, hi) && width > 1) {
-                    width >>= 1;   // redo this range narrower; nothing was applied yet
-                    continue;
-                }
-                apply_pass(ranged_t{}, lo, hi);
-                lo = hi;
-            }
-            if (lo < region_cells && threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
         }
-        __syncthreads();
-        done = true;
+#pragma unroll
+        for (uint32_t u = 0; u < SP_APPLY_U; ++u) {
+            if (k0 + tid + u * SP_APPLY_BLOCK >= n_recs) break;
+            const uint32_t co = (uint32_t)(r[u] >> 32) & co_mask;
+            uint32_t word, shift;
+            region_cell<STORAGE>(co, word, shift);
+            uint32_t cur = region[word];
+            if (cell_value<STORAGE>(cur, shift) != 0) {
+                if (STORAGE != GDBG_BIT) {
+                    for (int it = 0; it < (1 << 20); ++it) {
+                        if (cell_value<STORAGE>(cur, shift) >= cell_max<STORAGE>()) break;
+                        const uint32_t prev = atomicCAS(region + word, cur, cur + (1u << shift));
+                        if (prev == cur) {
+                            if (track) mark(word);
+                            break;
+                        }
+                        cur = prev;
+                    }
+                }
+            } else if (!*(volatile uint32_t*)&overflow) {
+                if (!sp_touch(map, slots, co, (uint32_t)r[u], list, &n_list)) overflow = 1;
+            }
+        }
     }
-    if (!done) {
-        uint32_t loaded = 0;   // chunk in rbuf
-        // all threads: make chunk c the one in rbuf (no-op when it already is)
-        auto need_chunk = [&](uint32_t c) -> bool {
-            if (c == loaded) return true;
-            __syncthreads();   // everyone is done with the old chunk
-            if (threadIdx.x == 0) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                chunk_copy(c, false);
+    __syncthreads();
+    unsigned long long occ = 0;
+    // zero cells of the map: their values, and their first touchers flagged new
+    auto settle = [&]() {
+        const uint32_t nl = n_list;
+        for (uint32_t i = tid; i < nl; i += SP_APPLY_BLOCK) {
+            const uint64_t e = map[list[i]];
+            const uint32_t co = (uint32_t)e >> SP_TOUCH_BITS;
+            const uint32_t n = (uint32_t)e & SP_TOUCH_MAX;
+            const uint32_t g = (uint32_t)(e >> 32);
+            uint32_t word, shift;
+            region_cell<STORAGE>(co, word, shift);
+            atomicOr(region + word, (n < cell_max<STORAGE>() ? n : cell_max<STORAGE>()) << shift);
+            if (track) mark(word);
+            if (g < sp.kmer_cap) {
+                atomicOr(new_bits + (g >> 5), 1u << (g & 31u));
+                if (ti == 0) ++occ;
             }
-            if (!copy_wait(sp, &bar, phase & 1u)) atomicExch(&abort_s, 1u);
-            ++phase;
-            __syncthreads();
-            loaded = c;
-            return abort_s == 0;
-        };
-        // cell ranges [lo, lo + width): narrower when the zero cells of a
-        // range overflow the map
-        uint32_t lo = 0, width = region_cells;
+        }
+    };
+    if (!overflow) {
+        settle();
+    } else {
+        // zero cells by ranges [lo, lo + width): still zero, nothing of them
+        // applied yet; a range whose zero cells overflow the map is redone
+        // narrower
+        uint32_t lo = 0, width = region_cells >> 1;
         int guard = 0;
-        bool ok = true;
-        for (; ok && lo < region_cells && guard < 4096; ++guard) {
+        for (; lo < region_cells && guard < 4096; ++guard) {
             const uint32_t hi = lo + width < region_cells ? lo + width : region_cells;
-            for (uint32_t k = threadIdx.x; k < slots64; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
-            if (threadIdx.x == 0) {
-                n_fresh = 0;
+            __syncthreads();   // everyone is done with the map
+            for (uint32_t k = tid; k < slots; k += SP_APPLY_BLOCK) map[k] = SP_EMPTY;
+            if (tid == 0) {
                 overflow = 0;
+                n_list = 0;
             }
             __syncthreads();
-            // pass 1: minimum ordinal per zero cell
-            uint32_t inserted = 0;
-            bool lost = false;
-            for (uint32_t c = 0; c < n_chunks && ok; ++c) {
-                ok = need_chunk(c);
-                if (!ok) break;
-                const uint32_t a = rs + c * RB;
-                const uint32_t cnt = re - a < RB ? re - a : RB;
-                const uint64_t* src = rbuf + (a & 1u);
-                for (uint32_t k = threadIdx.x; k < cnt; k += SP_APPLY_BLOCK) {
-                    const uint64_t rec = src[k];
-                    const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
+            for (uint32_t k0 = 0; k0 < n_recs; k0 += SP_APPLY_U * SP_APPLY_BLOCK) {
+#pragma unroll
+                for (uint32_t u = 0; u < SP_APPLY_U; ++u) {
+                    const uint32_t k = k0 + tid + u * SP_APPLY_BLOCK;
+                    r[u] = k < n_recs ? __ldg(brec + k) : 0ull;
+                }
+#pragma unroll
+                for (uint32_t u = 0; u < SP_APPLY_U; ++u) {
+                    if (k0 + tid + u * SP_APPLY_BLOCK >= n_recs) break;
+                    const uint32_t co = (uint32_t)(r[u] >> 32) & co_mask;
                     if (co < lo || co >= hi) continue;
                     uint32_t word, shift;
                     region_cell<STORAGE>(co, word, shift);
                     if (cell_value<STORAGE>(region[word], shift) != 0) continue;
-                    if (*(volatile uint32_t*)&overflow) continue;   // redone narrower anyway
-                    bool created;
-                    const uint32_t sl = sp_map_insert(map, bits64, co, (uint32_t)rec, &created);
-                    inserted += created;
-                    if (sl >= slots64) {
-                        lost = true;
-                        overflow = 1;
-                    }
+                    if (*(volatile uint32_t*)&overflow) continue;
+                    if (!sp_touch(map, slots, co, (uint32_t)r[u], list, &n_list)) overflow = 1;
                 }
             }
-            if (!ok) break;
-            inserted = __reduce_add_sync(0xFFFFFFFFu, inserted);
-            if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(&n_fresh, inserted);
-            if (lost) overflow = 1;
             __syncthreads();
-            if ((overflow || n_fresh > slots64 / 2) && width > 1) {
-                width >>= 1;   // redo this range narrower; nothing was applied yet
-                __syncthreads();
+            if (overflow && width > 1) {
+                width >>= 1;
                 continue;
             }
-            // pass 2: apply every record of the range; the map's minima are new
-            for (uint32_t c = 0; c < n_chunks && ok; ++c) {
-                ok = need_chunk(c);
-                if (!ok) break;
-                const uint32_t a = rs + c * RB;
-                const uint32_t cnt = re - a < RB ? re - a : RB;
-                const uint64_t* src = rbuf + (a & 1u);
-                for (uint32_t k = threadIdx.x; k < cnt; k += SP_APPLY_BLOCK) {
-                    const uint64_t rec = src[k];
-                    const uint32_t co = (uint32_t)(rec >> 32) & co_mask;
-                    if (co < lo || co >= hi) continue;
-                    uint32_t word, shift;
-                    region_cell<STORAGE>(co, word, shift);
-                    const bool changed = sp_increment<STORAGE>(region, word, shift);
-                    if (track && changed) {
-                        const uint32_t sec = word >> 3;
-                        atomicOr(dirty + (sec >> 5), 1u << (sec & 31u));
-                    }
-                }
-            }
-            if (!ok) break;
-            sp_map_winners(map, slots64, sp, ti, new_bits, occ);
-            __syncthreads();
+            settle();
             lo = hi;
         }
-        if (!ok) {
-            // a copy wait ran out: flag it, give that copy one more bounded wait, leave
-            if (threadIdx.x == 0) {
-                atomicOr(sp.err, GDBG_ERR_COPY_TIMEOUT);
-                mbar_wait(&bar, (phase - 1) & 1u);
-            }
-            return;
-        }
-        if (lo < region_cells && threadIdx.x == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
+        if (lo < region_cells && tid == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
     }
+    __syncthreads();
     // write back the region: every sector of a dense bucket, the dirty ones
     // of a sparse one (8 words each)
     uint32_t* gdst = tp.words[ti] + w0;
-    for (uint32_t sec = threadIdx.x; sec < region_sectors; sec += SP_APPLY_BLOCK) {
+    for (uint32_t sec = tid; sec < region_sectors; sec += SP_APPLY_BLOCK) {
         if (track && !((dirty[sec >> 5] >> (sec & 31u)) & 1u)) continue;
         const uint32_t wb = sec * 8;
         if (bulk_region && wb + 8 <= nw) {
@@ -1006,12 +876,7 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
         }
     }
     occ = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)occ);
-    if ((threadIdx.x & 31) == 0 && occ) atomicAdd(counters + 1, occ);
-}
-
-__host__ __device__ constexpr size_t sp_apply_smem(uint32_t region_words, uint32_t map_b,
-                                                   uint32_t rbuf_cap) {
-    return sp_apply_layout(region_words, map_b, rbuf_cap).total;
+    if ((tid & 31) == 0 && occ) atomicAdd(counters + 1, occ);
 }
 
 }  // namespace gdbg

@@ -119,9 +119,17 @@ struct SortParams {
     uint32_t* plan;               // s0[bins1 + 1] then G[bins1 + 1]
     uint32_t* err;                // device status word
     uint32_t wait_cap;            // polls of a bulk-copy wait before giving up (0: WAIT_CAP)
-    uint32_t map_bytes;           // apply: map space per CTA (set by its launcher)
-    uint32_t rbuf_cap;            // apply: records staged at once (set by its launcher)
-    uint32_t idx_bits;            // apply: record-index bits of a 32-bit map entry
+    uint32_t map_slots;           // apply: zero-cell map slots per CTA (set by its launcher)
+    // Reserved layout of pass 2 (bcap[0] != 0): each bucket of table i owns
+    // bcap[i] record slots from cbase[i] + (bucket - bbase[i]) * bcap[i] on,
+    // and a pass-2 tile takes its runs' places by atomics on bfill; a bucket
+    // that outgrows its slots sets *spill, and the counted, exact layout is
+    // made instead.
+    uint32_t bcap[BK_MAXNT];
+    uint32_t cbase[BK_MAXNT];
+    uint32_t n_slots;             // record slots of the pass-2 output
+    uint32_t* bfill;              // records placed per bucket
+    uint32_t* spill;
 };
 
 // Persistent batch insert (gdbg_persist.cuh).

@@ -1,14 +1,16 @@
 """The segmented insert's apply on crowded buckets, against the oracle.
 
-The apply stages a bucket's records in shared memory and keys every cell
-that was zero before the batch to its first toucher (the record with the
-smallest k-mer ordinal) in a map.  Ordinary batches take one pass; these
-cases force the other paths by fixing large buckets on small tables:
+The apply reads a bucket's records once: cells that were not zero before
+the batch take their increments at once, zero cells are counted in a
+shared-memory map that keeps each one's first toucher (the record with the
+smallest k-mer ordinal) and get their values after the last record.
+Ordinary batches fit the map; these cases force the other paths by fixing
+large buckets on small tables:
 
-* all of a bucket's records staged, but more zero cells than the map
-  holds (a fresh, empty table): the cells are taken in narrower ranges;
-* more records than the staging buffer holds: records are staged in
-  chunks, per cell range.
+* fresh, empty tables with more zero cells per bucket than the map holds:
+  the zero cells are redone in narrower cell ranges, the increments stand;
+* a small genome read many times over: hundreds of touches per cell in one
+  batch, so counts saturate (255 / 15) on cells that were zero before it.
 
 Each must give the sequential insert's per-read new counts, table bytes and
 counters (bitstorage.hh:195-219, bytestorage.cc:60-113, nibblestorage.cc:
@@ -26,12 +28,14 @@ pytestmark = pytest.mark.gpu
 STORAGES = {"bit": G.BitStorage, "byte": G.ByteStorage, "nibble": G.NibbleStorage}
 
 
-@pytest.mark.parametrize("kind,bucket_bits,n_reads", [
-    ("nibble", 14, 14_000),   # ~6,500 records per bucket: one chunk, narrowed cell ranges
-    ("byte", 14, 28_000),     # ~13,000 records per bucket: two chunks
-    ("bit", 15, 24_000),      # ~22,500 records per bucket: three chunks
+@pytest.mark.parametrize("kind,bucket_bits,n_reads,genome_bp", [
+    ("nibble", 14, 14_000, 3_000_000),   # ~6,500 records, ~5,400 zero cells per bucket
+    ("byte", 15, 28_000, 3_000_000),     # ~26,000 records, ~18,000 zero cells: ranges
+    ("bit", 15, 24_000, 3_000_000),      # ~22,500 records, ~16,000 zero cells: ranges
+    ("byte", 15, 20_000, 2_000),         # ~600 touches per k-mer in each batch
+    ("nibble", 14, 20_000, 2_000),
 ])
-def test_crowded_buckets_match_oracle(cuda_ready, kind, bucket_bits, n_reads):
+def test_crowded_buckets_match_oracle(cuda_ready, kind, bucket_bits, n_reads, genome_bp):
     sizes = oracle.primes(4, 1 << 22)
     st = STORAGES[kind]
     g = G.dBG[st, G.CanLemireShifter].build(st(tablesizes=sizes), 31)
@@ -39,7 +43,7 @@ def test_crowded_buckets_match_oracle(cuda_ready, kind, bucket_bits, n_reads):
     g.set_bucket_bits(bucket_bits)
     g.set_profiling(True)
     ref = oracle.Storage(kind, sizes)
-    gen = synth.genome(3_000_000, 61)
+    gen = synth.genome(genome_bp, 61)
     for b in range(2):
         pr = synth.rows_to_packed(synth.sample_reads(gen, n_reads, 150, 0.01, 62 + b))
         got = g.insert_packed(pr)
