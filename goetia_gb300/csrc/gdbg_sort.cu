@@ -38,10 +38,20 @@ static cudaError_t sp_part_one(cudaStream_t st, const SortParams& sp, uint32_t g
     return cudaGetLastError();
 }
 
+static uint32_t sm_count() {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (uint32_t)sms;
+}
+
+// Pass 1 and the reserved pass 2 take one segment per CTA; the counted pass
+// 2, which usually returns at once, loops over the segments with two CTAs
+// per SM (as many as fit), so its launch costs little when it has no work.
 cudaError_t launch_sp_part(int pass, cudaStream_t st, const SortParams& sp, const uint64_t* rin,
                            uint64_t* rout) {
-    const uint32_t grid = pass == SP_PASS1 ? sp.nseg1 : sp.nseg2_cap;
+    uint32_t grid = pass == SP_PASS1 ? sp.nseg1 : sp.nseg2_cap;
     if (grid == 0) return cudaSuccess;
+    if (pass == SP_PASS2_COUNTED) grid = std::min(grid, 2 * sm_count());
     switch (pass) {
     case SP_PASS1: return sp_part_one<false, false>(st, sp, grid, rin, rout);
     case SP_PASS2_RESERVED: return sp_part_one<true, true>(st, sp, grid, rin, rout);
@@ -56,7 +66,7 @@ cudaError_t launch_sp_plan(cudaStream_t st, const SortParams& sp) {
 
 cudaError_t launch_sp_hist2(cudaStream_t st, const SortParams& sp, const uint64_t* rin) {
     if (sp.nseg2_cap == 0) return cudaSuccess;
-    k_sp_hist2<<<sp.nseg2_cap, SP_PART_BLOCK, 0, st>>>(sp, rin);
+    k_sp_hist2<<<std::min(sp.nseg2_cap, 4 * sm_count()), SP_PART_BLOCK, 0, st>>>(sp, rin);
     return cudaGetLastError();
 }
 

@@ -365,32 +365,35 @@ k_sp_hist2(SortParams sp, const uint64_t* __restrict__ rin) {
     __shared__ Seg2 sg;
     // only for the counted layout: not needed when the reserved one held
     if (sp.bcap[0] != 0 && *(volatile const uint32_t*)sp.spill == 0) return;
-    if (threadIdx.x == 0) sg = seg2_of(sp, blockIdx.x);
-    for (uint32_t k = threadIdx.x; k < sp.bins2; k += SP_PART_BLOCK) cnt[k] = 0;
-    __syncthreads();
-    if (!sg.valid) {
-        // past the last segment: the scan's tail entries, zeroed here
-        const uint64_t tail = (uint64_t)sp.bins2 * blockIdx.x;
-        for (uint32_t d = threadIdx.x; d < sp.bins2; d += SP_PART_BLOCK) sp.hist2[tail + d] = 0;
-        return;
-    }
     const uint32_t mask = sp.bins2 - 1;
-    constexpr int U = 8;   // loads in flight per thread
-    for (uint32_t k0 = sg.rs + threadIdx.x; k0 < sg.re; k0 += U * SP_PART_BLOCK) {
-        uint64_t v[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint32_t k = k0 + u * SP_PART_BLOCK;
-            v[u] = k < sg.re ? __ldcs(rin + k) : SP_EMPTY;
+    for (uint32_t s = blockIdx.x; s < sp.nseg2_cap; s += gridDim.x) {
+        __syncthreads();   // the previous segment's counts are written out
+        if (threadIdx.x == 0) sg = seg2_of(sp, s);
+        for (uint32_t k = threadIdx.x; k < sp.bins2; k += SP_PART_BLOCK) cnt[k] = 0;
+        __syncthreads();
+        if (!sg.valid) {
+            // past the last segment: the scan's tail entries, zeroed here
+            const uint64_t tail = (uint64_t)sp.bins2 * s;
+            for (uint32_t d = threadIdx.x; d < sp.bins2; d += SP_PART_BLOCK) sp.hist2[tail + d] = 0;
+            continue;
         }
+        constexpr int U = 8;   // loads in flight per thread
+        for (uint32_t k0 = sg.rs + threadIdx.x; k0 < sg.re; k0 += U * SP_PART_BLOCK) {
+            uint64_t v[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (v[u] != SP_EMPTY) atomicAdd(&cnt[sp_bucket(v[u], sp.fs) & mask], 1u);
+            for (int u = 0; u < U; ++u) {
+                const uint32_t k = k0 + u * SP_PART_BLOCK;
+                v[u] = k < sg.re ? __ldcs(rin + k) : SP_EMPTY;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (v[u] != SP_EMPTY) atomicAdd(&cnt[sp_bucket(v[u], sp.fs) & mask], 1u);
+        }
+        __syncthreads();
+        const uint64_t base = (uint64_t)sp.bins2 * sp.plan[sg.group];
+        for (uint32_t d = threadIdx.x; d < sp.bins2; d += SP_PART_BLOCK)
+            sp.hist2[base + (uint64_t)d * sg.nseg + sg.k] = cnt[d];
     }
-    __syncthreads();
-    const uint64_t base = (uint64_t)sp.bins2 * sp.plan[sg.group];
-    for (uint32_t d = threadIdx.x; d < sp.bins2; d += SP_PART_BLOCK)
-        sp.hist2[base + (uint64_t)d * sg.nseg + sg.k] = cnt[d];
 }
 
 // ---- 2 / 3c. partition passes -----------------------------------------------
@@ -419,42 +422,11 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
     const uint32_t bins = PASS2 ? sp.bins2 : sp.bins1;
     if (PASS2 && !RESERVE && sp.bcap[0] != 0 && *(volatile const uint32_t*)sp.spill == 0) return;
     if (tid == 0) {
-        uint32_t rs = 0, re = 0;
-        if (PASS2) {
-            const Seg2 sg = seg2_of(sp, blockIdx.x);
-            if (sg.valid) {
-                rs = sg.rs;
-                re = sg.re;
-                group_s = sg.group;
-            }
-        } else {
-            const uint64_t nr = sp_records(sp);
-            const uint64_t a = (uint64_t)blockIdx.x * SP_SEGK * sp.n_tables;
-            const uint64_t e = a + (uint64_t)SP_SEGK * sp.n_tables;
-            rs = (uint32_t)(a < nr ? a : nr);
-            re = (uint32_t)(e < nr ? e : nr);
-        }
-        rs_s = rs;
-        re_s = re;
         abort_s = 0;
         for (int i = 0; i < SP_NBUF; ++i) mbar_init(&bars[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
-    const uint32_t rs = rs_s, re = re_s;
-    if (rs >= re) return;
-    // segment cursors
-    if (PASS2 && !RESERVE) {
-        const Seg2 sg = seg2_of(sp, blockIdx.x);
-        const uint64_t base = (uint64_t)sp.bins2 * sp.plan[sg.group];
-        for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK)
-            cursor[d] = sp.off2[base + (uint64_t)d * sg.nseg + sg.k];
-    } else if (!PASS2) {
-        for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK)
-            cursor[d] = sp.off1[(uint64_t)d * sp.nseg1 + blockIdx.x];
-    }
-    const uint32_t group = PASS2 ? group_s : 0u;
-    const uint32_t n_tiles = (re - rs + SP_TILE - 1) / SP_TILE;
+    for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK) cnt[d] = 0;
     // digit of a record: (cell >> (fs + shift)) & mask
     const uint32_t dshift = sp.fs + (PASS2 ? 0u : sp.hi_shift);
     const uint32_t mask = PASS2 ? sp.bins2 - 1 : 0xFFFFFFFFu;
@@ -463,110 +435,155 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
     // found its bucket full goes to n_slots, past the end, and is dropped)
     const uint32_t limit = RESERVE ? sp.n_slots : n_recs;
     const uint32_t lane = tid & 31u, w = tid >> 5;
-    // tile i covers records [rs + i*SP_TILE, ...); its copy starts at the
-    // even index at or below, so the copy is 16-byte aligned and sized
-    auto issue = [&](uint32_t i) {
-        const uint32_t ts = rs + i * SP_TILE;
-        const uint32_t te = ts + SP_TILE < re ? ts + SP_TILE : re;
-        const uint32_t a0 = ts & ~1u, a1 = (te + 1) & ~1u;
-        uint64_t* bar = &bars[i % SP_NBUF];
-        mbar_expect(bar, (a1 - a0) * 8u);
-        bulk_load(inbuf + (i % SP_NBUF) * SP_BUF, rin + a0, (a1 - a0) * 8u, bar);
-    };
-    for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK) cnt[d] = 0;
-    if (tid == 0)
-        for (uint32_t i = 0; i < SP_NBUF && i < n_tiles; ++i) issue(i);
     constexpr int IPT = SP_TILE / SP_PART_BLOCK;
-    for (uint32_t i = 0; i < n_tiles; ++i) {
-        const uint32_t ts = rs + i * SP_TILE;
-        const uint32_t nt = re - ts < SP_TILE ? re - ts : SP_TILE;
-        const uint64_t* src = inbuf + (i % SP_NBUF) * SP_BUF + (ts & 1u);
-        if (!copy_wait(sp, &bars[i % SP_NBUF], (i / SP_NBUF) & 1u)) atomicExch(&abort_s, 1u);
-        // also orders the previous tile's reads of stage / delta before this
-        // tile's writes
-        __syncthreads();
-        if (abort_s) {
-            // give the copies in flight a last bounded wait, then leave
-            if (tid == 0) {
-                atomicOr(sp.err, GDBG_ERR_COPY_TIMEOUT);
-                for (uint32_t j = i; j < i + SP_NBUF && j < n_tiles; ++j)
-                    mbar_wait(&bars[j % SP_NBUF], (j / SP_NBUF) & 1u);
-            }
-            return;
-        }
-        // ranks inside the tile: all loads first, then all atomics
-        uint64_t r[IPT];
-        uint32_t dg[IPT], pos[IPT];
-#pragma unroll
-        for (int j = 0; j < IPT; ++j) {
-            const uint32_t k = j * SP_PART_BLOCK + tid;
-            r[j] = k < nt ? src[k] : 0;
-        }
-#pragma unroll
-        for (int j = 0; j < IPT; ++j) {
-            const uint32_t k = j * SP_PART_BLOCK + tid;
-            dg[j] = ((uint32_t)(r[j] >> 32) >> dshift) & mask;
-            pos[j] = k < nt ? atomicAdd(&cnt[dg[j]], 1u) : 0u;
-        }
-        __syncthreads();
-        // buffer consumed: refill it with tile i + SP_NBUF
-        if (tid == 0 && i + SP_NBUF < n_tiles) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(i + SP_NBUF);
-        }
-        // tile-local bin starts: one bin per thread, warp scans, then the
-        // warps' totals; delta[d] = global base - local start
-        const uint32_t c = tid < bins ? cnt[tid] : 0u;
-        if (tid < bins) cnt[tid] = 0;
-        uint32_t inc = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-            if (lane >= (uint32_t)o) inc += y;
-        }
-        if (lane == 31) wsum[w] = inc;
-        __syncthreads();
-        if (tid < bins) {
-            uint32_t pre = 0;
-            for (uint32_t q = 0; q < w; ++q) pre += wsum[q];
-            const uint32_t ex = pre + inc - c;
-            lstart[tid] = ex;
-            if (RESERVE) {
-                uint32_t dl = sp.n_slots;
-                if (c) {
-                    const uint32_t bk = (group << sp.hi_shift) | tid;
-                    int ti = 0;
-                    while (ti + 1 < (int)sp.n_tables && sp.bbase[ti + 1] <= bk) ++ti;
-                    const uint32_t at = atomicAdd(sp.bfill + bk, c);
-                    if (at + c <= sp.bcap[ti])
-                        dl = sp.cbase[ti] + (bk - sp.bbase[ti]) * sp.bcap[ti] + at - ex;
-                    else
-                        atomicExch(sp.spill, 1u);
+    const uint32_t n_segs = PASS2 ? sp.nseg2_cap : sp.nseg1;
+    // tiles this CTA has consumed before the current segment: tile g of the
+    // CTA uses buffer g % SP_NBUF at barrier phase (g / SP_NBUF) & 1
+    uint32_t g0 = 0;
+    for (uint32_t seg = blockIdx.x; seg < n_segs; seg += gridDim.x) {
+        __syncthreads();   // the previous segment's last tile is written out
+        if (tid == 0) {
+            uint32_t rs = 0, re = 0;
+            if (PASS2) {
+                const Seg2 sg = seg2_of(sp, seg);
+                if (sg.valid) {
+                    rs = sg.rs;
+                    re = sg.re;
+                    group_s = sg.group;
                 }
-                delta[tid] = dl;
             } else {
-                delta[tid] = cursor[tid] - ex;
-                cursor[tid] += c;
+                const uint64_t nr = sp_records(sp);
+                const uint64_t a = (uint64_t)seg * SP_SEGK * sp.n_tables;
+                const uint64_t e = a + (uint64_t)SP_SEGK * sp.n_tables;
+                rs = (uint32_t)(a < nr ? a : nr);
+                re = (uint32_t)(e < nr ? e : nr);
             }
+            rs_s = rs;
+            re_s = re;
         }
         __syncthreads();
-#pragma unroll
-        for (int j = 0; j < IPT; ++j) {
-            const uint32_t k = j * SP_PART_BLOCK + tid;
-            if (k < nt) stage[lstart[dg[j]] + pos[j]] = r[j];
+        const uint32_t rs = rs_s, re = re_s;
+        if (rs >= re) continue;
+        // segment cursors
+        if (PASS2 && !RESERVE) {
+            const Seg2 sg = seg2_of(sp, seg);
+            const uint64_t base = (uint64_t)sp.bins2 * sp.plan[sg.group];
+            for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK)
+                cursor[d] = sp.off2[base + (uint64_t)d * sg.nseg + sg.k];
+        } else if (!PASS2) {
+            for (uint32_t d = tid; d < bins; d += SP_PART_BLOCK)
+                cursor[d] = sp.off1[(uint64_t)d * sp.nseg1 + seg];
         }
-        __syncthreads();
-        // runs of equal digits go out contiguously
+        const uint32_t group = PASS2 ? group_s : 0u;
+        const uint32_t n_tiles = (re - rs + SP_TILE - 1) / SP_TILE;
+        // tile i covers records [rs + i*SP_TILE, ...); its copy starts at the
+        // even index at or below, so the copy is 16-byte aligned and sized
+        auto issue = [&](uint32_t i) {
+            const uint32_t ts = rs + i * SP_TILE;
+            const uint32_t te = ts + SP_TILE < re ? ts + SP_TILE : re;
+            const uint32_t a0 = ts & ~1u, a1 = (te + 1) & ~1u;
+            const uint32_t b = (g0 + i) % SP_NBUF;
+            mbar_expect(&bars[b], (a1 - a0) * 8u);
+            bulk_load(inbuf + b * SP_BUF, rin + a0, (a1 - a0) * 8u, &bars[b]);
+        };
+        if (tid == 0) {
+            // the buffers' last readers (the previous segment) are past the barrier above
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            for (uint32_t i = 0; i < SP_NBUF && i < n_tiles; ++i) issue(i);
+        }
+        for (uint32_t i = 0; i < n_tiles; ++i) {
+            const uint32_t gi = g0 + i;
+            const uint32_t ts = rs + i * SP_TILE;
+            const uint32_t nt = re - ts < SP_TILE ? re - ts : SP_TILE;
+            const uint64_t* src = inbuf + (gi % SP_NBUF) * SP_BUF + (ts & 1u);
+            if (!copy_wait(sp, &bars[gi % SP_NBUF], (gi / SP_NBUF) & 1u)) atomicExch(&abort_s, 1u);
+            // also orders the previous tile's reads of stage / delta before this
+            // tile's writes
+            __syncthreads();
+            if (abort_s) {
+                // give the copies in flight a last bounded wait, then leave
+                if (tid == 0) {
+                    atomicOr(sp.err, GDBG_ERR_COPY_TIMEOUT);
+                    for (uint32_t j = i; j < i + SP_NBUF && j < n_tiles; ++j)
+                        mbar_wait(&bars[(g0 + j) % SP_NBUF], ((g0 + j) / SP_NBUF) & 1u);
+                }
+                return;
+            }
+            // ranks inside the tile: all loads first, then all atomics
+            uint64_t r[IPT];
+            uint32_t dg[IPT], pos[IPT];
 #pragma unroll
-        for (int j = 0; j < IPT; ++j) {
-            const uint32_t k = j * SP_PART_BLOCK + tid;
-            if (k < nt) {
-                const uint64_t v = stage[k];
-                const uint32_t p = delta[((uint32_t)(v >> 32) >> dshift) & mask] + k;
-                if (p < limit) rout[p] = v;
-                else if (!RESERVE) atomicOr(sp.err, GDBG_ERR_PARTITION);
+            for (int j = 0; j < IPT; ++j) {
+                const uint32_t k = j * SP_PART_BLOCK + tid;
+                r[j] = k < nt ? src[k] : 0;
+            }
+#pragma unroll
+            for (int j = 0; j < IPT; ++j) {
+                const uint32_t k = j * SP_PART_BLOCK + tid;
+                dg[j] = ((uint32_t)(r[j] >> 32) >> dshift) & mask;
+                pos[j] = k < nt ? atomicAdd(&cnt[dg[j]], 1u) : 0u;
+            }
+            __syncthreads();
+            // buffer consumed: refill it with tile i + SP_NBUF
+            if (tid == 0 && i + SP_NBUF < n_tiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(i + SP_NBUF);
+            }
+            // tile-local bin starts: one bin per thread, warp scans, then the
+            // warps' totals; delta[d] = global base - local start
+            const uint32_t c = tid < bins ? cnt[tid] : 0u;
+            if (tid < bins) cnt[tid] = 0;
+            uint32_t inc = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+                if (lane >= (uint32_t)o) inc += y;
+            }
+            if (lane == 31) wsum[w] = inc;
+            __syncthreads();
+            if (tid < bins) {
+                uint32_t pre = 0;
+                for (uint32_t q = 0; q < w; ++q) pre += wsum[q];
+                const uint32_t ex = pre + inc - c;
+                lstart[tid] = ex;
+                if (RESERVE) {
+                    uint32_t dl = sp.n_slots;
+                    if (c) {
+                        const uint32_t bk = (group << sp.hi_shift) | tid;
+                        int ti = 0;
+                        while (ti + 1 < (int)sp.n_tables && sp.bbase[ti + 1] <= bk) ++ti;
+                        const uint32_t at = atomicAdd(sp.bfill + bk, c);
+                        if (at + c <= sp.bcap[ti])
+                            dl = sp.cbase[ti] + (bk - sp.bbase[ti]) * sp.bcap[ti] + at - ex;
+                        else
+                            atomicExch(sp.spill, 1u);
+                    }
+                    delta[tid] = dl;
+                } else {
+                    delta[tid] = cursor[tid] - ex;
+                    cursor[tid] += c;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < IPT; ++j) {
+                const uint32_t k = j * SP_PART_BLOCK + tid;
+                if (k < nt) stage[lstart[dg[j]] + pos[j]] = r[j];
+            }
+            __syncthreads();
+            // runs of equal digits go out contiguously
+#pragma unroll
+            for (int j = 0; j < IPT; ++j) {
+                const uint32_t k = j * SP_PART_BLOCK + tid;
+                if (k < nt) {
+                    const uint64_t v = stage[k];
+                    const uint32_t p = delta[((uint32_t)(v >> 32) >> dshift) & mask] + k;
+                    if (p < limit) rout[p] = v;
+                    else if (!RESERVE) atomicOr(sp.err, GDBG_ERR_PARTITION);
+                }
             }
         }
+        g0 += n_tiles;
     }
 }
 
