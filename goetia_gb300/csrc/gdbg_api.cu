@@ -123,6 +123,7 @@ struct gdbg_graph {
     DevBuf<uint8_t> iq_vals;    // insert_and_query: post-insert value per table and k-mer
     DevBuf<uint32_t> sp_hist2, sp_off2, sp_plan;   // segmented path: pass-2 counts, plan
     DevBuf<uint32_t> sp_fill, sp_end;              // spill word + per-bucket fill; bucket ends
+    DevBuf<uint32_t> sp_groups;                    // fused pass 1: group slots, bases, fills, spill
     DevBuf<uint64_t> cq_keys;                      // compactor query: per-read new-k-mer sets
     DevBuf<uint32_t> cq_min, cq_ones;
     uint32_t* d_epoch = nullptr;
@@ -739,15 +740,39 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
         }
     }
     sp.n_slots = (uint32_t)slots;
+    // reserved pass-1 layout, for the fused emit (four tables, two passes):
+    // the device sizes each group from lam[] (k_sp_groups); the same integer
+    // sum here gives the slots to allocate
+    uint64_t slots1 = nrec;
+    bool fused = n == 4 && sp.bins2 > 1 && sp.bins1 == 256;
+    if (fused) {
+        for (uint64_t i = 0; i < n; ++i)
+            sp.lam[i] = ((nk << fs) + g->ts->sizes[i] - 1) / g->ts->sizes[i];
+        uint64_t at = 0;
+        for (uint32_t grp = 0; grp < 256; ++grp) at += sp_group_cap(sp, grp);
+        if (at + 2 * SP_TILE < 0xFFFFFFFFull && at <= 2 * nrec + (1ull << 24)) {
+            slots1 = at;
+            sp.n_slots1 = (uint32_t)at;
+        } else {
+            fused = false;
+        }
+    }
     GDBG_TRY(g->rec_a.ensure(std::max(nrec, slots) + 2));
-    GDBG_TRY(g->rec_b.ensure(nrec + 2));
+    GDBG_TRY(g->rec_b.ensure(std::max(nrec, slots1) + 2));
     GDBG_TRY(g->hist.ensure(h1));
     GDBG_TRY(g->hist_off.ensure(h1));
     if (h2) {
         GDBG_TRY(g->sp_hist2.ensure(h2));
         GDBG_TRY(g->sp_off2.ensure(h2));
     }
-    GDBG_TRY(g->sp_plan.ensure(2 * (sp.bins1 + 1)));
+    GDBG_TRY(g->sp_plan.ensure(4 * (sp.bins1 + 1)));
+    if (fused) {
+        GDBG_TRY(g->sp_groups.ensure(3 * 256 + 1));
+        sp.gcap = g->sp_groups.p;
+        sp.gbase = g->sp_groups.p + 256;
+        sp.gfill = g->sp_groups.p + 512;
+        sp.spill1 = g->sp_groups.p + 768;
+    }
     GDBG_TRY(g->scan_parts.ensure(scan32_partials_needed(std::max(h1, h2)) + 1));
     GDBG_TRY(g->bstart.ensure(nb + 1));
     GDBG_TRY(g->sp_end.ensure(nb + 1));
@@ -765,11 +790,15 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
     GDBG_CUDA(cudaMemsetAsync(g->new_bits.p, 0, (nk / 32 + 2) * sizeof(uint32_t), st));
     const bool canon = g->shifter == GDBG_CAN_LEMIRE;
     cudaError_t e;
-    {
-        Stage sg(g, "k_sp_emit", st);
+    // the batch's emit: per copied chunk while a host batch is still
+    // arriving (each piece covers the segments whose reads are all in, after
+    // its chunk's copy), else one launch
+    auto emit = [&](bool fused_kernel, uint64_t* out) -> int {
+        auto one = [&](uint32_t s0, uint32_t ns) {
+            return fused_kernel ? launch_sp_emit_part(canon, st, b, g->hp, g->ts->tp, sp, out, s0, ns)
+                                : launch_sp_emit(canon, st, b, g->hp, g->ts->tp, sp, out, s0, ns);
+        };
         if (g->plan.n > 0) {
-            // a host batch still arriving in chunks: each piece covers the
-            // segments whose reads are all in, after its chunk's copy
             uint32_t s0 = 0;
             for (int c = 0; c < g->plan.n; ++c) {
                 uint32_t s1 = sp.nseg1;
@@ -778,29 +807,58 @@ int run_insert_sorted(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cudaSt
                 if (s1 < s0) s1 = s0;
                 GDBG_CUDA(cudaStreamWaitEvent(st, g->chunk_ev[c], 0));
                 if (s1 > s0) {
-                    if ((e = launch_sp_emit(canon, st, b, g->hp, g->ts->tp, sp, g->rec_a.p, s0,
-                                            s1 - s0)) != cudaSuccess)
-                        return set_error_launch(e, "segment emit");
+                    if ((e = one(s0, s1 - s0)) != cudaSuccess) return set_error_launch(e, "segment emit");
                     g->launches += 1;
                 }
                 s0 = s1;
             }
             g->plan.n = 0;
-            g->launches -= 1;   // counted with the scans below
-        } else if ((e = launch_sp_emit(canon, st, b, g->hp, g->ts->tp, sp, g->rec_a.p, 0,
-                                       sp.nseg1)) != cudaSuccess) {
+            g->launches -= 1;   // counted by the caller
+        } else if ((e = one(0, sp.nseg1)) != cudaSuccess) {
             return set_error_launch(e, "segment emit");
         }
-    }
-    {
-        Stage sg(g, "k_scan32", st);
-        if ((e = launch_scan32(sp.hist1, sp.off1, h1, g->scan_parts.p, st)) != cudaSuccess)
-            return set_error_launch(e, "segment scan");
-    }
-    {
-        Stage sg(g, "k_sp_part", st);
-        if ((e = launch_sp_part(SP_PASS1, st, sp, g->rec_a.p, g->rec_b.p)) != cudaSuccess)
-            return set_error_launch(e, "segment partition");
+        return GDBG_OK;
+    };
+    if (fused) {
+        // records partitioned as they are made, into the reserved pass-1
+        // layout; the separate emit, its counts and the counted pass 1 follow,
+        // and work only when a group outgrew its slots
+        if ((e = launch_sp_groups(st, sp)) != cudaSuccess) return set_error_launch(e, "segment groups");
+        {
+            Stage sg(g, "k_sp_emit_part", st);
+            GDBG_TRY(emit(true, g->rec_b.p));
+        }
+        sp.gate1 = sp.spill1;
+        {
+            Stage sg(g, "k_sp_emit", st);
+            GDBG_TRY(emit(false, g->rec_a.p));
+        }
+        {
+            Stage sg(g, "k_scan32", st);
+            if ((e = launch_scan32(sp.hist1, sp.off1, h1, g->scan_parts.p, st, sp.gate1)) != cudaSuccess)
+                return set_error_launch(e, "segment scan");
+        }
+        {
+            Stage sg(g, "k_sp_part", st);
+            if ((e = launch_sp_part(SP_PASS1, st, sp, g->rec_a.p, g->rec_b.p)) != cudaSuccess)
+                return set_error_launch(e, "segment partition");
+        }
+        g->launches += 2;   // groups, fused emit (the rest counted below)
+    } else {
+        {
+            Stage sg(g, "k_sp_emit", st);
+            GDBG_TRY(emit(false, g->rec_a.p));
+        }
+        {
+            Stage sg(g, "k_scan32", st);
+            if ((e = launch_scan32(sp.hist1, sp.off1, h1, g->scan_parts.p, st)) != cudaSuccess)
+                return set_error_launch(e, "segment scan");
+        }
+        {
+            Stage sg(g, "k_sp_part", st);
+            if ((e = launch_sp_part(SP_PASS1, st, sp, g->rec_a.p, g->rec_b.p)) != cudaSuccess)
+                return set_error_launch(e, "segment partition");
+        }
     }
     g->launches += 4;   // emit, 2 scan kernels, partition
     const uint64_t* fin = g->rec_b.p;

@@ -283,4 +283,19 @@ __device__ __forceinline__ uint32_t claim_lookup(const uint64_t* __restrict__ ma
     return 0xFFFFFFFFu;
 }
 
+// Slots of digit group g in the reserved pass-1 layout of the segmented
+// insert (the host sizes its allocation with it, k_sp_groups the layout):
+// the group's expected records (sp.lam[i]: per bucket of table i, rounded
+// up) plus 1/64 of them plus two tiles.
+__host__ __device__ inline uint64_t sp_group_cap(const SortParams& sp, uint32_t g) {
+    const uint32_t b0 = g << sp.hi_shift, b1 = (g + 1) << sp.hi_shift;
+    uint64_t lam = 0;
+    for (uint32_t i = 0; i < sp.n_tables; ++i) {
+        const uint32_t lo = b0 > sp.bbase[i] ? b0 : sp.bbase[i];
+        const uint32_t hi = b1 < sp.bbase[i + 1] ? b1 : sp.bbase[i + 1];
+        if (hi > lo) lam += (uint64_t)(hi - lo) * sp.lam[i];
+    }
+    return lam + lam / 64 + 2 * SP_TILE;
+}
+
 }  // namespace gdbg

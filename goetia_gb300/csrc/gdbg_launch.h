@@ -93,6 +93,12 @@ cudaError_t launch_tile_map(const uint64_t* kofs, uint64_t n_reads, uint64_t n_t
 cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
                            const TableParams& tp, const SortParams& sp, uint64_t* rout,
                            uint32_t seg0, uint32_t n_seg);
+// The emit and pass 1 fused (four tables), into the reserved pass-1 layout
+// that k_sp_groups sizes; segments [seg0, seg0 + n_seg) of the batch.
+cudaError_t launch_sp_groups(cudaStream_t st, const SortParams& sp);
+cudaError_t launch_sp_emit_part(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
+                                const TableParams& tp, const SortParams& sp, uint64_t* rout,
+                                uint32_t seg0, uint32_t n_seg);
 // Partition passes: pass 1, pass 2 into the reserved layout, pass 2 into the
 // counted layout (a no-op when the reserved one was made and held).
 enum { SP_PASS1 = 0, SP_PASS2_RESERVED = 1, SP_PASS2_COUNTED = 2 };

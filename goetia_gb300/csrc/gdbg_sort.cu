@@ -3,6 +3,7 @@
 
 #include "gdbg_launch.h"
 #include "gdbg_sort.cuh"
+#include "gdbg_emit_part.cuh"
 
 namespace gdbg {
 
@@ -27,6 +28,29 @@ cudaError_t launch_sp_emit(bool canonical, cudaStream_t st, const BatchView& b, 
     return cudaGetLastError();
 }
 
+cudaError_t launch_sp_groups(cudaStream_t st, const SortParams& sp) {
+    k_sp_groups<<<1, 256, 0, st>>>(sp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sp_emit_part(bool canonical, cudaStream_t st, const BatchView& b, const HashParams& hp,
+                                const TableParams& tp, const SortParams& sp, uint64_t* rout,
+                                uint32_t seg0, uint32_t n_seg) {
+    if (n_seg == 0 || seg0 >= sp.nseg1) return cudaSuccess;
+    if (n_seg > sp.nseg1 - seg0) n_seg = sp.nseg1 - seg0;
+    bool small = true;   // every table below 2^31 cells: 32-bit remainders
+    for (int i = 0; i < tp.n; ++i) small = small && tp.p[i] < (1ull << 31);
+    const size_t smem = sp_ep_smem();
+    auto go = [&](auto kern) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<n_seg, SP_EP_BLOCK, smem, st>>>(b, hp, tp, sp, rout, seg0);
+        return cudaGetLastError();
+    };
+    if (canonical) return small ? go(k_sp_emit_part<true, true>) : go(k_sp_emit_part<true, false>);
+    return small ? go(k_sp_emit_part<false, true>) : go(k_sp_emit_part<false, false>);
+}
+
 template <bool PASS2, bool RESERVE>
 static cudaError_t sp_part_one(cudaStream_t st, const SortParams& sp, uint32_t grid, const uint64_t* rin,
                                uint64_t* rout) {
@@ -45,13 +69,14 @@ static uint32_t sm_count() {
 }
 
 // Pass 1 and the reserved pass 2 take one segment per CTA; the counted pass
-// 2, which usually returns at once, loops over the segments with two CTAs
-// per SM (as many as fit), so its launch costs little when it has no work.
+// 2 and a gated pass 1, which usually return at once, loop over the segments
+// with two CTAs per SM (as many as fit), so their launches cost little when
+// they have no work.
 cudaError_t launch_sp_part(int pass, cudaStream_t st, const SortParams& sp, const uint64_t* rin,
                            uint64_t* rout) {
     uint32_t grid = pass == SP_PASS1 ? sp.nseg1 : sp.nseg2_cap;
     if (grid == 0) return cudaSuccess;
-    if (pass == SP_PASS2_COUNTED) grid = std::min(grid, 2 * sm_count());
+    if (pass == SP_PASS2_COUNTED || (pass == SP_PASS1 && sp.gate1)) grid = std::min(grid, 2 * sm_count());
     switch (pass) {
     case SP_PASS1: return sp_part_one<false, false>(st, sp, grid, rin, rout);
     case SP_PASS2_RESERVED: return sp_part_one<true, true>(st, sp, grid, rin, rout);

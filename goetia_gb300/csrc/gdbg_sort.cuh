@@ -152,6 +152,8 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
     __shared__ uint64_t roll_fw[16], roll_rc[16];
     const uint32_t tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const uint32_t s = seg0 + blockIdx.x;   // launches may cover a range of segments
+    // behind the fused emit: only when a group outgrew its reserved slots
+    if (sp.gate1 && *(volatile const uint32_t*)sp.gate1 == 0) return;
     for (uint32_t k = tid; k < sp.bins1; k += SP_EMIT_BLOCK) hist[k] = 0;
     if (tid < 16) {
         const uint32_t out = tid >> 2, in = tid & 3u;
@@ -296,38 +298,67 @@ k_sp_emit(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* _
 
 // ---- 3a. pass-2 segment plan -------------------------------------------------
 
-// One block of 256 threads: group starts G[] from the pass-1 scan, segments
-// per group, and their exclusive scan s0[].
+// One block of 256 threads.  plan = s0[bins1 + 1] (exclusive scan of the
+// segments per group), G[bins1 + 1] (each group's first record), GE[bins1 +
+// 1] (its end) and D[bins1 + 1] (the records of the groups before it: where
+// the group starts in the counted pass-2 layout).  The groups are the
+// pass-1 output: dense (counted, from the emit's counts) or each in its
+// reserved slot range (the fused emit) -- whichever pass 1 made.
 __global__ void __launch_bounds__(256) k_sp_plan(SortParams sp) {
-    __shared__ uint32_t ws[8];
+    __shared__ uint32_t ws[8], wd[8];
     uint32_t* s0 = sp.plan;
-    uint32_t* G = sp.plan + sp.bins1 + 1;
+    uint32_t* G = sp.plan + (sp.bins1 + 1);
+    uint32_t* GE = sp.plan + 2 * (sp.bins1 + 1);
+    uint32_t* D = sp.plan + 3 * (sp.bins1 + 1);
     const uint32_t g = threadIdx.x;
     const uint32_t n_recs = (uint32_t)sp_records(sp);
-    uint32_t start = 0, next = n_recs;
-    if (g < sp.bins1) start = sp.off1[(uint64_t)g * sp.nseg1];
-    if (g + 1 < sp.bins1) next = sp.off1[(uint64_t)(g + 1) * sp.nseg1];
-    const uint32_t nseg = g < sp.bins1 ? (next - start + SP_SEG2 - 1) / SP_SEG2 : 0u;
-    // block exclusive scan of nseg
+    const bool reserved1 = sp.gcap != nullptr && *(volatile const uint32_t*)sp.spill1 == 0;
+    uint32_t start = 0, next = 0;
+    if (g < sp.bins1) {
+        if (reserved1) {
+            start = sp.gbase[g];
+            next = start + sp.gfill[g];
+        } else {
+            start = sp.off1[(uint64_t)g * sp.nseg1];
+            next = g + 1 < sp.bins1 ? sp.off1[(uint64_t)(g + 1) * sp.nseg1] : n_recs;
+        }
+    }
+    const uint32_t size = next - start;
+    const uint32_t nseg = g < sp.bins1 ? (size + SP_SEG2 - 1) / SP_SEG2 : 0u;
+    // block exclusive scans of nseg and size
     const uint32_t lane = g & 31, w = g >> 5;
-    uint32_t inc = nseg;
+    uint32_t inc = nseg, incd = size;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-        if (lane >= o) inc += y;
+        const uint32_t yd = __shfl_up_sync(0xFFFFFFFFu, incd, o);
+        if (lane >= o) {
+            inc += y;
+            incd += yd;
+        }
     }
-    if (lane == 31) ws[w] = inc;
+    if (lane == 31) {
+        ws[w] = inc;
+        wd[w] = incd;
+    }
     __syncthreads();
-    uint32_t add = 0;
-    for (uint32_t k = 0; k < w; ++k) add += ws[k];
-    const uint32_t excl = add + inc - nseg;
+    uint32_t add = 0, addd = 0;
+    for (uint32_t k = 0; k < w; ++k) {
+        add += ws[k];
+        addd += wd[k];
+    }
+    const uint32_t excl = add + inc - nseg, excld = addd + incd - size;
     if (g < sp.bins1) {
         s0[g] = excl;
         G[g] = start;
+        GE[g] = next;
+        D[g] = excld;
     }
     if (g == sp.bins1 - 1) {
         s0[sp.bins1] = excl + nseg;
-        G[sp.bins1] = n_recs;
+        G[sp.bins1] = next;
+        GE[sp.bins1] = next;
+        D[sp.bins1] = excld + size;
     }
 }
 
@@ -338,7 +369,8 @@ struct Seg2 {
 };
 __device__ __forceinline__ Seg2 seg2_of(const SortParams& sp, uint32_t s) {
     const uint32_t* s0 = sp.plan;
-    const uint32_t* G = sp.plan + sp.bins1 + 1;
+    const uint32_t* G = sp.plan + (sp.bins1 + 1);
+    const uint32_t* GE = sp.plan + 2 * (sp.bins1 + 1);
     Seg2 r{};
     r.valid = s < s0[sp.bins1] && s < sp.nseg2_cap;
     if (!r.valid) return r;
@@ -353,7 +385,7 @@ __device__ __forceinline__ Seg2 seg2_of(const SortParams& sp, uint32_t s) {
     r.nseg = s0[lo + 1] - s0[lo];
     r.rs = G[lo] + r.k * SP_SEG2;
     const uint32_t e = r.rs + SP_SEG2;
-    r.re = e < G[lo + 1] ? e : G[lo + 1];
+    r.re = e < GE[lo] ? e : GE[lo];
     return r;
 }
 
@@ -421,6 +453,7 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
     const uint32_t tid = threadIdx.x;
     const uint32_t bins = PASS2 ? sp.bins2 : sp.bins1;
     if (PASS2 && !RESERVE && sp.bcap[0] != 0 && *(volatile const uint32_t*)sp.spill == 0) return;
+    if (!PASS2 && sp.gate1 && *(volatile const uint32_t*)sp.gate1 == 0) return;
     if (tid == 0) {
         abort_s = 0;
         for (int i = 0; i < SP_NBUF; ++i) mbar_init(&bars[i], 1);
@@ -595,10 +628,10 @@ __device__ __forceinline__ uint32_t sp_counted_start(const SortParams& sp, uint3
     if (bk >= sp.n_buckets) return n_recs;
     if (sp.bins2 == 1) return sp.off1[(uint64_t)bk * sp.nseg1];
     const uint32_t* s0 = sp.plan;
-    const uint32_t* G = sp.plan + sp.bins1 + 1;
+    const uint32_t* D = sp.plan + 3 * (sp.bins1 + 1);
     const uint32_t g = bk >> sp.hi_shift, d = bk & (sp.bins2 - 1);
     const uint32_t nseg = s0[g + 1] - s0[g];
-    return nseg ? sp.off2[(uint64_t)sp.bins2 * s0[g] + (uint64_t)d * nseg] : G[g];
+    return nseg ? sp.off2[(uint64_t)sp.bins2 * s0[g] + (uint64_t)d * nseg] : D[g];
 }
 
 // Record range [start, end) of every bucket, in whichever layout pass 2 made.

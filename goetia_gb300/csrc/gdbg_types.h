@@ -130,6 +130,18 @@ struct SortParams {
     uint32_t n_slots;             // record slots of the pass-2 output
     uint32_t* bfill;              // records placed per bucket
     uint32_t* spill;
+    // Reserved layout of pass 1 (gcap != nullptr: the emit and pass 1 fused,
+    // k_sp_emit_part): digit group g owns gcap[g] slots from gbase[g] on;
+    // lam[i] = records expected per bucket of table i (rounded up).  A group
+    // that outgrows its slots sets *spill1, and the separate emit, its scan
+    // and the counted pass 1 (gated on gate1 = spill1) make the exact layout.
+    uint64_t lam[BK_MAXNT];
+    uint32_t* gcap;
+    uint32_t* gbase;
+    uint32_t* gfill;
+    uint32_t* spill1;
+    const uint32_t* gate1;
+    uint32_t n_slots1;            // record slots of the pass-1 output
 };
 
 // Persistent batch insert (gdbg_persist.cuh).
