@@ -11,11 +11,11 @@
 // k-mers from k-mer t * SP_EP_RUN of the segment (re-seeding at read
 // starts, a lane entering a new read seeded by its whole warp).  Every
 // SP_EP_STEPS steps of all threads make a tile of records, (global cell <<
-// 32) | k-mer ordinal, four per k-mer, in shared memory, which is partitioned
-// by the first digit like a pass-1 tile: ranks by shared-memory atomics, a
-// block scan of the tile's counts, one atomic add per (tile, group) on the
-// group's fill count for the run's place, the runs staged and written out
-// contiguously.  The records never go through HBM unpartitioned.  A group
+// 32) | k-mer ordinal, four per k-mer, partitioned by the first digit like a
+// pass-1 tile: each record ranked by a shared-memory atomic as it is made
+// (it stays in registers), a block scan of the tile's counts, one atomic add
+// per (tile, group) on the group's fill count for the run's place, the runs
+// staged in shared memory and written out contiguously.  The records never go through HBM unpartitioned.  A group
 // that outgrows its slots sets *spill1; then the separate emit, its counts
 // and the counted pass 1, launched behind this kernel every time and idle
 // otherwise, make the exact layout instead.
@@ -30,7 +30,7 @@ constexpr uint32_t SP_EP_RUN = SP_SEGK / SP_EP_BLOCK;                // k-mers p
 constexpr uint32_t SP_EP_STEPS = SP_TILE / (4u * SP_EP_BLOCK);       // steps per tile
 static_assert(SP_EP_RUN % SP_EP_STEPS == 0, "whole tiles per run");
 
-__host__ __device__ constexpr size_t sp_ep_smem() { return (size_t)2 * SP_TILE * 8; }
+__host__ __device__ constexpr size_t sp_ep_smem() { return (size_t)SP_TILE * 8; }
 
 // One block of 256 threads: gcap / gbase of the 256 groups, fill counts and
 // the spill word cleared.
@@ -58,9 +58,7 @@ template <bool CANON, bool SMALLP>
 __global__ void __launch_bounds__(SP_EP_BLOCK, 2)
 k_sp_emit_part(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64_t* __restrict__ rout,
                uint32_t seg0) {
-    extern __shared__ __align__(16) uint64_t epsm[];
-    uint64_t* tile = epsm;              // the tile's records as made
-    uint64_t* stage = epsm + SP_TILE;   // the same, grouped by digit
+    extern __shared__ __align__(16) uint64_t stage[];   // a tile's records, grouped by digit
     __shared__ uint32_t cnt[256], lstart[256], delta[256], gcap_s[256], gbase_s[256];
     __shared__ uint32_t wsum[SP_EP_BLOCK / 32];
     // roll terms by (out, in): fw ^= symk(out) ^ sym(in), rc ^= symk(3-in) ^ sym(3-out)
@@ -111,9 +109,11 @@ k_sp_emit_part(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64
     constexpr int IPT = SP_TILE / SP_EP_BLOCK;
     for (uint32_t j0 = 0; j0 < n_steps; j0 += SP_EP_STEPS) {
         // the tile: steps j0 .. j0 + SP_EP_STEPS - 1 of every active thread,
-        // step by step in thread order (the threads active at a step are
-        // 0 .. A-1), four records per slot
+        // four records per step; each record is ranked among the tile's
+        // records of its digit as it is made (the rank and digit share a
+        // word: digit < 2^8, rank < 2^13), and kept in registers
         uint32_t slot0 = 0;
+        uint32_t cell[4 * SP_EP_STEPS], dp[4 * SP_EP_STEPS];
 #pragma unroll
         for (uint32_t q = 0; q < SP_EP_STEPS; ++q) {
             const uint32_t j = j0 + q;
@@ -165,29 +165,19 @@ k_sp_emit_part(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64
             const uint32_t A = j < P ? F + 1 : F;
             if (act) {
                 const uint64_t h = hash_value<CANON>(fw, rc);
-                uint32_t gc[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    gc[i] = (uint32_t)sp.tbase[i] + (SMALLP ? fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
-                                                            : (uint32_t)fastmod(h, tp.p[i], tp.m[i]));
-                const uint32_t gl = g0 + j;
-                uint4* d4 = reinterpret_cast<uint4*>(tile) + 2u * (slot0 + tid);
-                d4[0] = make_uint4(gl, gc[0], gl, gc[1]);
-                d4[1] = make_uint4(gl, gc[2], gl, gc[3]);
+                for (int i = 0; i < 4; ++i) {
+                    const uint32_t gc = (uint32_t)sp.tbase[i] +
+                                        (SMALLP ? fastmod_small(h, (uint32_t)tp.p[i], tp.m[i])
+                                                : (uint32_t)fastmod(h, tp.p[i], tp.m[i]));
+                    const uint32_t d = gc >> dsh;
+                    cell[4 * q + i] = gc;
+                    dp[4 * q + i] = (atomicAdd(&cnt[d], 1u) << 8) | d;
+                }
             }
             slot0 += A;
         }
         const uint32_t nt = slot0 * 4u;
-        __syncthreads();
-        // ranks inside the tile; digit and rank share a word (digit < 2^8,
-        // rank < 2^13)
-        uint32_t dp[IPT];
-#pragma unroll
-        for (int jj = 0; jj < IPT; ++jj) {
-            const uint32_t k = jj * SP_EP_BLOCK + tid;
-            const uint32_t d = k < nt ? (uint32_t)(tile[k] >> 32) >> dsh : 0u;
-            dp[jj] = k < nt ? (atomicAdd(&cnt[d], 1u) << 8) | d : 0u;
-        }
         __syncthreads();
         // tile-local group starts (one group per thread), each run's place in
         // its group's slots
@@ -216,9 +206,13 @@ k_sp_emit_part(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64
         }
         __syncthreads();
 #pragma unroll
-        for (int jj = 0; jj < IPT; ++jj) {
-            const uint32_t k = jj * SP_EP_BLOCK + tid;
-            if (k < nt) stage[lstart[dp[jj] & 255u] + (dp[jj] >> 8)] = tile[k];
+        for (uint32_t q = 0; q < SP_EP_STEPS; ++q) {
+            if (j0 + q >= my_len) break;
+            const uint64_t gl = g0 + j0 + q;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                stage[lstart[dp[4 * q + i] & 255u] + (dp[4 * q + i] >> 8)] =
+                    ((uint64_t)cell[4 * q + i] << 32) | gl;
         }
         __syncthreads();
         // runs of equal digits go out contiguously

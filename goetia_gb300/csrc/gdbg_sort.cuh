@@ -11,10 +11,15 @@
 //      with cp.async.bulk (two buffers in flight, mbarrier-tracked); ranks
 //      inside a tile come from shared-memory atomics (any order), and each
 //      bin's run is written contiguously at the segment's cursor.
-//   3. k_sp_plan / k_sp_hist2 / k_sp_part<true>: every digit group is cut
-//      into segments of SP_SEG2 records that never cross a group, counted by
-//      the low digit and partitioned again; the scan is laid out group by
-//      group, so its entries are final record positions and bucket starts.
+//      With four tables, k_sp_emit_part (gdbg_emit_part.cuh) does 1 and 2
+//      in one kernel into a reserved layout, and these two run (gated) only
+//      when one of its groups outgrew its slots.
+//   3. k_sp_plan / k_sp_part<true, true>: every digit group is cut into
+//      segments of SP_SEG2 records that never cross a group and partitioned
+//      again by the low digit, each bucket's runs into its reserved slots.
+//      k_sp_hist2 / its scan / k_sp_part<true, false> make the counted layout
+//      instead (scan entries laid out group by group, so they are final
+//      record positions), gated on a bucket outgrowing its slots.
 //   4. k_sp_apply: one CTA per bucket bulk-copies its table region into
 //      shared memory and reads the bucket's records, which are in no
 //      particular order, once.  A cell that was not zero before the batch
