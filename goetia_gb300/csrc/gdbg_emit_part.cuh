@@ -183,6 +183,8 @@ k_sp_emit_part(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64
         // its group's slots
         const uint32_t c = tid < 256 ? cnt[tid] : 0u;
         if (tid < 256) cnt[tid] = 0;
+        // the run's place in its group, taken now, its latency hidden behind the scan
+        const uint32_t at = c ? atomicAdd(sp.gfill + tid, c) : 0u;
         uint32_t inc = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -198,7 +200,6 @@ k_sp_emit_part(BatchView b, HashParams hp, TableParams tp, SortParams sp, uint64
             lstart[tid] = ex;
             uint32_t dl = limit;   // a run that found its group full is dropped
             if (c) {
-                const uint32_t at = atomicAdd(sp.gfill + tid, c);
                 if (at + c <= gcap_s[tid]) dl = gbase_s[tid] + at - ex;
                 else atomicExch(sp.spill1, 1u);
             }

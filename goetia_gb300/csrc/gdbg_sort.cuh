@@ -571,6 +571,15 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
             // warps' totals; delta[d] = global base - local start
             const uint32_t c = tid < bins ? cnt[tid] : 0u;
             if (tid < bins) cnt[tid] = 0;
+            // reserved layout: the run's place is taken now, its latency
+            // hidden behind the scan
+            int rti = 0;
+            uint32_t at = 0;
+            if (RESERVE && c) {
+                const uint32_t bk = (group << sp.hi_shift) | tid;
+                while (rti + 1 < (int)sp.n_tables && sp.bbase[rti + 1] <= bk) ++rti;
+                at = atomicAdd(sp.bfill + bk, c);
+            }
             uint32_t inc = c;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -588,11 +597,8 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
                     uint32_t dl = sp.n_slots;
                     if (c) {
                         const uint32_t bk = (group << sp.hi_shift) | tid;
-                        int ti = 0;
-                        while (ti + 1 < (int)sp.n_tables && sp.bbase[ti + 1] <= bk) ++ti;
-                        const uint32_t at = atomicAdd(sp.bfill + bk, c);
-                        if (at + c <= sp.bcap[ti])
-                            dl = sp.cbase[ti] + (bk - sp.bbase[ti]) * sp.bcap[ti] + at - ex;
+                        if (at + c <= sp.bcap[rti])
+                            dl = sp.cbase[rti] + (bk - sp.bbase[rti]) * sp.bcap[rti] + at - ex;
                         else
                             atomicExch(sp.spill, 1u);
                     }

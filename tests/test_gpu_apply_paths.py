@@ -10,7 +10,10 @@ large buckets on small tables:
 * fresh, empty tables with more zero cells per bucket than the map holds:
   the zero cells are redone in narrower cell ranges, the increments stand;
 * a small genome read many times over: hundreds of touches per cell in one
-  batch, so counts saturate (255 / 15) on cells that were zero before it.
+  batch, so counts saturate (255 / 15) on cells that were zero before it;
+* one read repeated: the records crowd a few digit groups and buckets far
+  past their reserved slots, so both partition passes fall back to their
+  counted layouts.
 
 Each must give the sequential insert's per-read new counts, table bytes and
 counters (bitstorage.hh:195-219, bytestorage.cc:60-113, nibblestorage.cc:
@@ -34,6 +37,8 @@ STORAGES = {"bit": G.BitStorage, "byte": G.ByteStorage, "nibble": G.NibbleStorag
     ("bit", 15, 24_000, 3_000_000),      # ~22,500 records, ~16,000 zero cells: ranges
     ("byte", 15, 20_000, 2_000),         # ~600 touches per k-mer in each batch
     ("nibble", 14, 20_000, 2_000),
+    ("byte", 15, 20_000, 150),           # one read, 20,000 times: every group and bucket
+                                         # but a few empty, the rest far over their slots
 ])
 def test_crowded_buckets_match_oracle(cuda_ready, kind, bucket_bits, n_reads, genome_bp):
     sizes = oracle.primes(4, 1 << 22)
