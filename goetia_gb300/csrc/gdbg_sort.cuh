@@ -534,9 +534,11 @@ k_sp_part(SortParams sp, const uint64_t* __restrict__ rin, uint64_t* __restrict_
             const uint32_t ts = rs + i * SP_TILE;
             const uint32_t nt = re - ts < SP_TILE ? re - ts : SP_TILE;
             const uint64_t* src = inbuf + (gi % SP_NBUF) * SP_BUF + (ts & 1u);
-            if (!copy_wait(sp, &bars[gi % SP_NBUF], (gi / SP_NBUF) & 1u)) atomicExch(&abort_s, 1u);
-            // also orders the previous tile's reads of stage / delta before this
-            // tile's writes
+            // one thread waits for the tile's copy, the others at the barrier
+            // (waiting warps would take issue slots from the working ones); the
+            // barrier also orders the previous tile's reads of stage / delta
+            // before this tile's writes
+            if (tid == 0 && !copy_wait(sp, &bars[gi % SP_NBUF], (gi / SP_NBUF) & 1u)) abort_s = 1u;
             __syncthreads();
             if (abort_s) {
                 // give the copies in flight a last bounded wait, then leave
@@ -807,8 +809,9 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
         const uint32_t k = tid + u * SP_APPLY_BLOCK;
         r[u] = k < n_recs ? __ldcs(brec + k) : 0ull;
     }
-    __syncthreads();   // the barrier is initialised before anyone waits on it
-    if (bulk_region && !copy_wait(sp, &bar, 0)) atomicExch(&abort_s, 1u);
+    // one thread waits for the region's copy, the others at the barrier
+    // (waiting warps would take issue slots from the other CTAs' work)
+    if (tid == 0 && bulk_region && !copy_wait(sp, &bar, 0)) abort_s = 1u;
     __syncthreads();
     if (abort_s) {
         if (tid == 0) {
