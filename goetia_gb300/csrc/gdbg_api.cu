@@ -6,6 +6,7 @@
 // staging buffers for the host-pointer entry points.  All device work of a
 // handle runs on its stream in submission order.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cerrno>
 #include <cstdio>
@@ -138,11 +139,16 @@ struct gdbg_graph {
     // one-sequence calls: the read, its prefix and its maps built on the host
     // in one pinned block and moved by one copy; small results come back
     // through the pinned ret block
+    // (mapped into the device's address space: insert_sequence's read kernel
+    // reads the block in place and writes its count and status back into it)
     uint8_t* h_single = nullptr;
+    uint8_t* h_single_dev = nullptr;     // the block's device address
     size_t h_single_cap = 0;
     DevBuf<uint8_t> d_single;
     cudaEvent_t single_done = nullptr;   // the last copy out of h_single
     uint64_t* single_nnew = nullptr;     // device n_new slot of the staged read
+    bool read_smem_set = false;          // the read kernel's shared-memory opt-in is done
+    uint32_t read_seq = 0;               // token of the last read insert watched in host memory
     struct Ret {
         uint32_t err, pad;
         uint64_t v[7];
@@ -351,20 +357,22 @@ int make_graph(int storage, int shifter, uint16_t K, const uint64_t* sizes, uint
     return GDBG_OK;
 }
 
+// A non-zero device status word: cleared on the device, reported.
+int device_status_fail(gdbg_graph* g, uint32_t err) {
+    cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
+    char buf[200];
+    std::snprintf(buf, sizeof buf,
+                  "device status 0x%x (1=CAS cap, 2=claims map full, 4=barrier timeout, "
+                  "8=bad read offsets, 16=bulk-copy timeout, 32=partition overflow)", err);
+    return fail(GDBG_ERR_DEVICE, buf);
+}
+
 int check_device_status(gdbg_graph* g) {
     GDBG_CUDA(cudaMemcpyAsync(&g->h_ret->err, g->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost,
                               g->stream));
     GDBG_CUDA(cudaStreamSynchronize(g->stream));
     const uint32_t err = g->h_ret->err;
-    if (err) {
-        cudaMemsetAsync(g->d_err, 0, sizeof(uint32_t), g->stream);
-        char buf[200];
-        std::snprintf(buf, sizeof buf,
-                      "device status 0x%x (1=CAS cap, 2=claims map full, 4=barrier timeout, "
-                      "8=bad read offsets, 16=bulk-copy timeout, 32=partition overflow)", err);
-        return fail(GDBG_ERR_DEVICE, buf);
-    }
-    return GDBG_OK;
+    return err ? device_status_fail(g, err) : GDBG_OK;
 }
 
 // Per-read k-mer prefix + tile map for a device-resident batch.
@@ -955,6 +963,34 @@ int run_insert_persistent(gdbg_graph* g, const BatchView& b, uint64_t* n_new, cu
     return GDBG_OK;
 }
 
+// One read's insert in one CTA, its first touchers found in shared memory
+// (k_insert_read); done, when given, gets (seq << 32) | the device status
+// word as the insert's last write.
+int run_insert_read(gdbg_graph* g, const BatchView& b, uint64_t* n_new, uint64_t* done,
+                    uint32_t seq, cudaStream_t st) {
+    const bool canon = g->shifter == GDBG_CAN_LEMIRE;
+    const bool set = !g->read_smem_set;
+    cudaError_t e;
+    switch (g->storage) {
+    case GDBG_BIT:
+        e = launch_insert_read<GDBG_BIT>(canon, set, st, b, g->hp, g->ts->tp, n_new, g->ts->d_counters, g->d_err,
+                                           done, seq);
+        break;
+    case GDBG_BYTE:
+        e = launch_insert_read<GDBG_BYTE>(canon, set, st, b, g->hp, g->ts->tp, n_new, g->ts->d_counters, g->d_err,
+                                           done, seq);
+        break;
+    default:
+        e = launch_insert_read<GDBG_NIBBLE>(canon, set, st, b, g->hp, g->ts->tp, n_new, g->ts->d_counters, g->d_err,
+                                           done, seq);
+        break;
+    }
+    if (e != cudaSuccess) return set_error_launch(e, "read insert");
+    g->read_smem_set = true;
+    g->launches += 1;
+    return GDBG_OK;
+}
+
 // Windowed probe + commit over n_total k-mers (from the batch or a hash array).
 int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64_t n_total,
                uint64_t* n_new, cudaStream_t st) {
@@ -970,6 +1006,8 @@ int run_insert(gdbg_graph* g, const BatchView& b, const uint64_t* hashes, uint64
         default: break;
         }
     }
+    if (!hashes && b.n_reads == 1 && g->ts->sizes.size() <= (size_t)READ_INSERT_MAXNT)
+        return run_insert_read(g, b, n_new, nullptr, 0, st);   // one read: one CTA
     GDBG_TRY(ensure_insert_scratch(g, st));
     if (g->epoch_on_device) {
         // the device owns the epoch counter: start the host-driven windows
@@ -1187,7 +1225,9 @@ int stage_host_insert(gdbg_graph* g, const uint32_t* packed, uint64_t n_words,
 // {0, n}, task prefix {0, ceil(n / TASK_KMERS)}, zero tile and task maps, a
 // zero n_new slot and the packed bases, written into the pinned block and
 // copied to the device in one transfer (no prefix or map kernels).
-int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view) {
+// mapped: the view points at the pinned block itself (no copy); the caller
+// synchronises the stream before the block is written again.
+int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view, bool mapped = false) {
     if (len < g->K) return fail(GDBG_ERR_SEQUENCE_LENGTH, "Sequence must have length >= K");
     if (!seq) return fail(GDBG_ERR_INVALID_ARG, "NULL sequence");
     const uint64_t nk = len - g->K + 1, words = len / 16 + 1;
@@ -1203,10 +1243,13 @@ int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view) 
         g->h_single = nullptr;
         g->h_single_cap = 0;
         const size_t want = std::max<size_t>(total + total / 4, 65536);
-        if (cudaHostAlloc((void**)&g->h_single, want, cudaHostAllocDefault) != cudaSuccess) {
+        if (cudaHostAlloc((void**)&g->h_single, want, cudaHostAllocMapped) != cudaSuccess) {
             g->h_single = nullptr;
             return fail(GDBG_ERR_OOM, "pinned staging allocation failed");
         }
+        void* dp = nullptr;
+        if (cudaHostGetDevicePointer(&dp, g->h_single, 0) != cudaSuccess) dp = nullptr;
+        g->h_single_dev = static_cast<uint8_t*>(dp);
         g->h_single_cap = want;
     }
     GDBG_TRY(g->d_single.ensure(total));
@@ -1237,8 +1280,12 @@ int stage_string(gdbg_graph* g, const char* seq, uint64_t len, BatchView* view) 
     hdr[7] = 0;
     std::memset(h + o_tile, 0, o_pack - o_tile);
     uint8_t* d = g->d_single.p;
-    GDBG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, g->stream));
-    GDBG_CUDA(cudaEventRecord(g->single_done, g->stream));
+    if (mapped && g->h_single_dev) {
+        d = g->h_single_dev;
+    } else {
+        GDBG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, g->stream));
+        GDBG_CUDA(cudaEventRecord(g->single_done, g->stream));
+    }
     view->packed = reinterpret_cast<const uint32_t*>(d + o_pack);
     view->offsets = reinterpret_cast<const uint64_t*>(d);
     view->kofs = reinterpret_cast<const uint64_t*>(d + 16);
@@ -1748,6 +1795,39 @@ int gdbg_insert_sequence(gdbg_graph* g, const char* seq, uint64_t len, uint64_t*
     if (!g) return fail(GDBG_ERR_INVALID_ARG, "NULL graph");
     GDBG_TRY(set_device(g));
     BatchView b;
+    if (g->ts->sizes.size() <= (size_t)READ_INSERT_MAXNT && len >= g->K &&
+        insert_kind(g, len - g->K + 1) == INS_WINDOWED) {
+        // the read kernel reads the staged block in place and writes the
+        // read's count and the device status back into it: no copies, one
+        // launch, one synchronisation
+        GDBG_TRY(stage_string(g, seq, len, &b, true));
+        if (g->h_single_dev) {
+            volatile uint64_t* hdr = reinterpret_cast<volatile uint64_t*>(g->h_single);
+            uint32_t seq = ++g->read_seq;
+            if (seq == 0) seq = g->read_seq = 1;   // 0 is the block's cleared word
+            GDBG_TRY(run_insert_read(g, b, g->single_nnew,
+                                     reinterpret_cast<uint64_t*>(g->h_single_dev + 56), seq, g->stream));
+            // the kernel's last write carries the token: watch for it (up to
+            // 2 ms), else wait for the stream, which also reports a failure
+            const auto t0 = std::chrono::steady_clock::now();
+            bool seen = false;
+            for (uint32_t it = 0;; ++it) {
+                if ((uint32_t)(hdr[7] >> 32) == seq) {
+                    seen = true;
+                    break;
+                }
+                if ((it & 1023u) == 1023u &&
+                    std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(2))
+                    break;
+            }
+            if (!seen) GDBG_CUDA(cudaStreamSynchronize(g->stream));
+            const uint32_t err = (uint32_t)hdr[7];
+            if (err) return device_status_fail(g, err);
+            if (n_kmers) *n_kmers = len - g->K + 1;
+            if (n_new) *n_new = hdr[6];
+            return GDBG_OK;
+        }
+    }
     GDBG_TRY(stage_string(g, seq, len, &b));
     GDBG_TRY(run_insert(g, b, nullptr, b.n_kmers, g->single_nnew, g->stream));
     GDBG_CUDA(cudaMemcpyAsync(&g->h_ret->v[0], g->single_nnew, sizeof(uint64_t),

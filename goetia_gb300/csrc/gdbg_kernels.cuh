@@ -293,6 +293,154 @@ k_insert_small(BatchView b, const uint64_t* __restrict__ hashes, HashParams hp, 
 }
 
 // ---------------------------------------------------------------------------
+// One read's insert in one CTA (insert_sequence, dbg.hh:249-265): chunks of
+// the read's k-mers in order, one k-mer per thread.  Per chunk every thread
+// hashes its k-mer and loads its cells (all tables at once); the cells that
+// were zero go into a shared-memory map keyed by (table, cell) that keeps
+// the smallest k-mer of the chunk touching each -- the one that sees it zero
+// in the sequential loop, so that k-mer is new -- and then every cell takes
+// its saturating increment.  The next chunk starts after the CTA barrier,
+// with this chunk's increments in place.  No claims map in global memory:
+// one round trip of loads and one of updates per chunk.  With `done`, the
+// last word written is (seq << 32) | device status, which a caller can watch
+// in host memory instead of synchronising the stream.
+constexpr int READ_BLOCK = 512;
+constexpr uint32_t READ_SLOTS = 4096;   // map slots: twice a chunk's records at most
+constexpr int READ_MAXNT = 8;           // tables (more take the windowed insert)
+
+__host__ __device__ constexpr size_t read_insert_smem() { return (size_t)READ_SLOTS * 12; }
+
+template <int STORAGE, bool CANON>
+__global__ void __launch_bounds__(READ_BLOCK, 1)
+k_insert_read(BatchView b, HashParams hp, TableParams tp, uint64_t* n_new,
+              unsigned long long* counters, uint32_t* err, uint64_t* done, uint32_t seq) {
+    extern __shared__ __align__(16) uint64_t rkey[];   // (table << 56) | cell, all ones = empty
+    uint32_t* rfirst = reinterpret_cast<uint32_t*>(rkey + READ_SLOTS);   // smallest k-mer per key
+    __shared__ unsigned long long red_new[READ_BLOCK / 32], red_occ[READ_BLOCK / 32];
+    // the chunk's bases, copied once from the packed read (which may be in
+    // host memory) when they fit (k-mers of up to 256 bases)
+    constexpr uint32_t RB_WORDS = (READ_BLOCK + 256) / 16 + 2;
+    __shared__ uint32_t rbases[RB_WORDS];
+    const uint32_t tid = threadIdx.x;
+    const int n = tp.n;
+    const uint32_t K = hp.K;
+    const uint64_t nk = __ldg(b.kofs + 1) - __ldg(b.kofs);
+    const uint64_t base = __ldg(b.offsets);
+    // k-mers per chunk: the chunk's records (k-mers x tables) fill at most half the map
+    const uint32_t chunk = READ_SLOTS / 2 / (uint32_t)n < READ_BLOCK ? READ_SLOTS / 2 / (uint32_t)n
+                                                                     : READ_BLOCK;
+    unsigned long long my_new = 0, my_occ = 0;
+    for (uint64_t c0 = 0; c0 < nk; c0 += chunk) {
+        const uint32_t ck = nk - c0 < chunk ? (uint32_t)(nk - c0) : chunk;   // k-mers of the chunk
+        // map slots: a power of two at least twice the chunk's records
+        uint32_t sbits = 6;
+        while ((1u << sbits) < 2u * ck * (uint32_t)n && sbits < 12) ++sbits;
+        const uint32_t nslots = 1u << sbits;
+        for (uint32_t k = tid; k < nslots; k += READ_BLOCK) {
+            rkey[k] = ~0ull;
+            rfirst[k] = 0xFFFFFFFFu;
+        }
+        const uint64_t w0 = (base + c0) >> 4;
+        const uint32_t nwords = (uint32_t)(((base + c0 + ck + K - 1 + 15) >> 4) - w0);
+        const bool staged = nwords <= RB_WORDS;
+        if (staged)
+            for (uint32_t k = tid; k < nwords; k += READ_BLOCK) rbases[k] = __ldg(b.packed + w0 + k);
+        __syncthreads();
+        const uint64_t j = c0 + tid;
+        const bool act = tid < chunk && j < nk;
+        uint64_t cell[READ_MAXNT];
+        uint32_t word[READ_MAXNT], shift[READ_MAXNT];
+        uint32_t fresh = 0, slot_of[READ_MAXNT];
+        if (act) {
+            // the k-mer's hash from its K bases (the rolling state's closed form)
+            uint64_t fw = 0, rc = 0;
+            const uint32_t p0 = (uint32_t)((base + j) - (w0 << 4));   // first base in rbases
+            for (uint32_t i = 0; i < K; ++i) {
+                const uint32_t q = p0 + i;
+                const uint32_t c = staged ? (rbases[q >> 4] >> ((q & 15u) << 1)) & 3u
+                                          : base_at(b.packed, base + j + i);
+                fw ^= rotl64(sym(c), (K - 1u - i) & 63u);
+                if (CANON) rc ^= rotl64(sym(3u - c), i & 63u);
+            }
+            const uint64_t h = hash_value<CANON>(fw, rc);
+#pragma unroll
+            for (int i = 0; i < READ_MAXNT; ++i) {
+                if (i >= n) break;
+                cell[i] = fastmod(h, tp.p[i], tp.m[i]);
+                const Cell cl = cell_of<STORAGE>(tp, i, cell[i]);
+                shift[i] = cl.shift;
+                word[i] = __ldcg(cl.word);
+            }
+#pragma unroll
+            for (int i = 0; i < READ_MAXNT; ++i) {
+                if (i >= n) break;
+                if (cell_value<STORAGE>(word[i], shift[i]) != 0) continue;
+                fresh |= 1u << i;
+                const uint64_t key = ((uint64_t)i << 56) | cell[i];
+                uint32_t sl = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - sbits));
+                for (uint32_t it = 0; it < nslots; ++it) {
+                    const uint64_t cur = atomicCAS((unsigned long long*)(rkey + sl), ~0ull, key);
+                    if (cur == ~0ull || cur == key) break;
+                    sl = (sl + 1) & (nslots - 1);
+                }
+                slot_of[i] = sl;
+                atomicMin(rfirst + sl, tid);
+            }
+        }
+        __syncthreads();
+        if (act) {
+            bool isnew = false;
+#pragma unroll
+            for (int i = 0; i < READ_MAXNT; ++i) {
+                if (!((fresh >> i) & 1u)) continue;
+                if (rfirst[slot_of[i]] == tid) {
+                    isnew = true;
+                    if (i == 0) ++my_occ;
+                }
+            }
+            my_new += isnew;
+#pragma unroll
+            for (int i = 0; i < READ_MAXNT; ++i) {
+                if (i >= n) break;
+                const Cell cl = cell_of<STORAGE>(tp, i, cell[i]);
+                if (STORAGE == GDBG_BIT) atomicOr(cl.word, 1u << cl.shift);
+                else sat_increment<STORAGE>(cl.word, cl.shift, word[i], err);
+            }
+        }
+        // this chunk's increments are in place before the next chunk's loads
+        __threadfence_block();
+        __syncthreads();
+    }
+    // the read's new k-mers and table 0's newly occupied cells
+    for (int o = 16; o > 0; o >>= 1) {
+        my_new += __shfl_xor_sync(0xFFFFFFFFu, my_new, o);
+        my_occ += __shfl_xor_sync(0xFFFFFFFFu, my_occ, o);
+    }
+    if ((tid & 31) == 0) {
+        red_new[tid >> 5] = my_new;
+        red_occ[tid >> 5] = my_occ;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long tn = 0, to = 0;
+        for (int k = 0; k < READ_BLOCK / 32; ++k) {
+            tn += red_new[k];
+            to += red_occ[k];
+        }
+        // the only writer of the read's count (it may live in host memory)
+        if (n_new) *n_new += tn;
+        if (tn) atomicAdd(counters + 0, tn);
+        if (to) atomicAdd(counters + 1, to);
+        if (done) {
+            // the caller's token with the device status word, after every
+            // update of this insert is visible system-wide
+            __threadfence_system();
+            *(volatile uint64_t*)done = ((uint64_t)seq << 32) | *(volatile uint32_t*)err;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // query: Bit -> AND over tables (bitstorage.cc:87-100); Byte/Nibble -> min
 // over tables capped at 255 / 15 (bytestorage.cc:116-139, nibblestorage.cc:112-130)
 template <int STORAGE, bool CANON, int H, int NT, bool FROM_HASHES>

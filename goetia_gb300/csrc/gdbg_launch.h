@@ -28,6 +28,17 @@ cudaError_t launch_insert_pass(int pass, const LaunchShape& s, uint64_t n_thread
                                const HashParams& hp, const TableParams& tp,
                                const WindowParams& w);
 
+// One read's insert in one CTA (k_insert_read, at most 8 tables): n_new[0]
+// gets the read's new k-mers added; counters[0] / [1] n_unique / n_occupied;
+// done (may be null) gets (seq << 32) | the device status word as the insert's
+// last write.  set_attr: the kernel's shared-memory opt-in (once per device).
+template <int STORAGE>
+cudaError_t launch_insert_read(bool canonical, bool set_attr, cudaStream_t st, const BatchView& b,
+                               const HashParams& hp, const TableParams& tp, uint64_t* n_new,
+                               unsigned long long* counters, uint32_t* err, uint64_t* done,
+                               uint32_t seq);
+constexpr int READ_INSERT_MAXNT = 8;
+
 struct PersistParams;
 
 // Persistent cooperative insert of a whole read batch (gdbg_persist.cuh).

@@ -161,6 +161,35 @@ cudaError_t launch_insert_persistent(const LaunchShape& s, uint64_t max_tasks, c
               : persist_one<ST, false, 0>(max_tasks, st, b, hp, tp, pp, grid_used);
 }
 
+static_assert(READ_MAXNT == READ_INSERT_MAXNT, "one table limit for the read insert");
+
+// One read in one CTA (k_insert_read): 48 KB of map beside the kernel's own
+// shared words, so the launch opts in to more than the default 48 KB (once
+// per handle: set_attr).
+template <int ST>
+cudaError_t launch_insert_read(bool canonical, bool set_attr, cudaStream_t st, const BatchView& b,
+                               const HashParams& hp, const TableParams& tp, uint64_t* n_new,
+                               unsigned long long* counters, uint32_t* err, uint64_t* done,
+                               uint32_t seq) {
+    if (tp.n > READ_MAXNT) return cudaErrorInvalidValue;
+    const int smem = (int)read_insert_smem();
+    auto go = [&](auto kern) {
+        if (set_attr) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+        }
+        kern<<<1, READ_BLOCK, smem, st>>>(b, hp, tp, n_new, counters, err, done, seq);
+        return cudaGetLastError();
+    };
+    // both forms' attributes on the first call, whichever shifter it uses
+    if (set_attr) {
+        cudaError_t e = cudaFuncSetAttribute(canonical ? k_insert_read<ST, false> : k_insert_read<ST, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+    }
+    return canonical ? go(k_insert_read<ST, true>) : go(k_insert_read<ST, false>);
+}
+
 #define GDBG_INSTANTIATE_LAUNCHERS(ST)                                                         \
     template cudaError_t launch_insert_pass<ST>(int, const LaunchShape&, uint64_t, cudaStream_t, \
                                                 const BatchView&, const uint64_t*,             \
@@ -174,6 +203,9 @@ cudaError_t launch_insert_persistent(const LaunchShape& s, uint64_t max_tasks, c
     template cudaError_t launch_insert_persistent<ST>(const LaunchShape&, uint64_t, cudaStream_t, \
                                                       const BatchView&, const HashParams&,    \
                                                       const TableParams&, const PersistParams&, \
-                                                      int*);
+                                                      int*);                                   \
+    template cudaError_t launch_insert_read<ST>(bool, bool, cudaStream_t, const BatchView&,   \
+                                                const HashParams&, const TableParams&, uint64_t*, \
+                                                unsigned long long*, uint32_t*, uint64_t*, uint32_t);
 
 }  // namespace gdbg

@@ -57,6 +57,34 @@ def test_golden_plain_per_read(cuda_ready, name):
         k += n
 
 
+@pytest.mark.parametrize("kind", ["bit", "byte", "nibble"])
+@pytest.mark.parametrize("K,lengths", [(31, [40, 600, 2500]), (101, [150, 1300]), (300, [320, 900])])
+def test_plain_long_reads_vs_oracle(cuda_ready, kind, K, lengths):
+    """insert_sequence on reads of several 512-k-mer chunks (the one-CTA read
+    insert works through a read's k-mers chunk by chunk, in order) and of
+    k-mers too long for its staged bases (K=300), on small tables so cells
+    collide within a read: per-read new counts, tables and counters against
+    the oracle's sequential insert."""
+    from goetia_gb300 import reads as R
+    sizes = oracle.primes(4, 50_000)
+    g = graph_for(kind, True, K, sizes)
+    ref = oracle.Storage(kind, sizes)
+    gen = synth.genome(20_000, 71)
+    rng = np.random.default_rng(72)
+    rows = []
+    for L in lengths * 3:
+        s0 = int(rng.integers(0, len(gen) - L))
+        rows.append(gen[s0:s0 + L].copy())
+    pr = R.from_codes(rows)
+    _, want = ref.insert_reads(True, K, pr.packed, pr.offsets)
+    for r, codes in enumerate(rows):
+        nk, nn = g.insert_sequence_new(R.codes_to_str(codes))
+        assert nk == len(codes) - K + 1
+        assert nn == int(want[r]), (r, nn, int(want[r]))
+    check_tables(g, ref.tables())
+    assert (g.n_unique(), g.n_occupied()) == ref.stats()
+
+
 # insert path, window, k-mers per thread, log2 cells per bucket (0 = default)
 PATHS = [("persistent", 262144, 4, 0), ("persistent", 64, 8, 0), ("persistent", 5, 4, 0),
          ("windowed", 262144, 4, 0), ("windowed", 64, 8, 0), ("windowed", 5, 4, 0),
