@@ -356,13 +356,19 @@ def run_profile_masks(args):
     three mask passes."""
     from goetia_gb300 import build as gbuild
     gbuild.build()
+    import torch
     _, _, g, pr, s, d_p, d_o, d_m = masks_setup(args.mask_reads)
     nk = pr.n_kmers(31)
     for rep in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
         g.neighbor_masks_device(d_p.data_ptr(), d_p.numel(), d_o.data_ptr(), pr.n_reads,
                                 d_m.data_ptr(), n_kmers=nk, stream=s.cuda_stream)
+        e1.record(s)
         s.synchronize()
-        print(json.dumps({"profile_masks_pass": rep, "kmers": nk}), flush=True)
+        ms = e0.elapsed_time(e1)
+        print(json.dumps({"profile_masks_pass": rep, "kmers": nk, "ms": round(ms, 3),
+                          "kmers_per_s": nk / (ms / 1000.0)}), flush=True)
     g.synchronize()
     return 0
 
