@@ -1,4 +1,6 @@
 // Launchers for the bucketed insert path (kernels in gdbg_bucket.cuh).
+#include <algorithm>
+
 #include "gdbg_bucket.cuh"
 #include "gdbg_launch.h"
 
@@ -119,46 +121,54 @@ __device__ __forceinline__ uint32_t block_scan32(uint32_t v, uint32_t* ws) {
     return v;
 }
 
+// Both kernels take chunks c = blockIdx.x, blockIdx.x + gridDim.x, ... of
+// SCAN32_BLOCK * SCAN32_ITEMS entries (a gated scan launches a small grid,
+// so it costs little when the gate keeps it idle).
 __global__ void __launch_bounds__(SCAN32_BLOCK)
 k_scan32_partials(const uint32_t* __restrict__ in, uint64_t n, uint32_t* __restrict__ partials,
-                  const uint32_t* gate) {
+                  const uint32_t* gate, uint64_t n_chunks) {
     __shared__ uint32_t ws[32];
     if (gate && *(volatile const uint32_t*)gate == 0) return;
-    const uint64_t base = ((uint64_t)blockIdx.x * SCAN32_BLOCK + threadIdx.x) * SCAN32_ITEMS;
-    uint32_t s = 0;
+    for (uint64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        const uint64_t base = (c * SCAN32_BLOCK + threadIdx.x) * SCAN32_ITEMS;
+        uint32_t s = 0;
 #pragma unroll
-    for (int j = 0; j < SCAN32_ITEMS; ++j)
-        if (base + j < n) s += in[base + j];
-    s = block_scan32(s, ws);
-    if (threadIdx.x == SCAN32_BLOCK - 1) partials[blockIdx.x] = s;
+        for (int j = 0; j < SCAN32_ITEMS; ++j)
+            if (base + j < n) s += in[base + j];
+        s = block_scan32(s, ws);
+        if (threadIdx.x == SCAN32_BLOCK - 1) partials[c] = s;
+    }
 }
 
 // Each block first sums the totals of the blocks before it (a few thousand at
 // most), so no separate pass scans the partials.
 __global__ void __launch_bounds__(SCAN32_BLOCK)
 k_scan32_final(const uint32_t* __restrict__ in, uint64_t n, const uint32_t* __restrict__ partials,
-               uint32_t* __restrict__ out, const uint32_t* gate) {
+               uint32_t* __restrict__ out, const uint32_t* gate, uint64_t n_chunks) {
     __shared__ uint32_t ws[32];
     __shared__ uint32_t before_s;
     if (gate && *(volatile const uint32_t*)gate == 0) return;
-    uint32_t pre = 0;
-    for (uint32_t i = threadIdx.x; i < blockIdx.x; i += SCAN32_BLOCK) pre += partials[i];
-    pre = block_scan32(pre, ws);
-    if (threadIdx.x == SCAN32_BLOCK - 1) before_s = pre;
-    __syncthreads();
-    const uint32_t before = before_s;
-    const uint64_t base = ((uint64_t)blockIdx.x * SCAN32_BLOCK + threadIdx.x) * SCAN32_ITEMS;
-    uint32_t v[SCAN32_ITEMS], s = 0;
+    for (uint64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        uint32_t pre = 0;
+        for (uint64_t i = threadIdx.x; i < c; i += SCAN32_BLOCK) pre += partials[i];
+        pre = block_scan32(pre, ws);
+        if (threadIdx.x == SCAN32_BLOCK - 1) before_s = pre;
+        __syncthreads();
+        const uint32_t before = before_s;
+        const uint64_t base = (c * SCAN32_BLOCK + threadIdx.x) * SCAN32_ITEMS;
+        uint32_t v[SCAN32_ITEMS], s = 0;
 #pragma unroll
-    for (int j = 0; j < SCAN32_ITEMS; ++j) {
-        v[j] = base + j < n ? in[base + j] : 0;
-        s += v[j];
-    }
-    uint32_t run = block_scan32(s, ws) - s + before;
+        for (int j = 0; j < SCAN32_ITEMS; ++j) {
+            v[j] = base + j < n ? in[base + j] : 0;
+            s += v[j];
+        }
+        uint32_t run = block_scan32(s, ws) - s + before;
 #pragma unroll
-    for (int j = 0; j < SCAN32_ITEMS; ++j) {
-        if (base + j < n) out[base + j] = run;
-        run += v[j];
+        for (int j = 0; j < SCAN32_ITEMS; ++j) {
+            if (base + j < n) out[base + j] = run;
+            run += v[j];
+        }
+        __syncthreads();   // before_s is rewritten for the next chunk
     }
 }
 
@@ -170,8 +180,14 @@ cudaError_t launch_scan32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_
                           cudaStream_t st, const uint32_t* gate) {
     if (n == 0) return cudaSuccess;
     const uint64_t nb = (n + SCAN32_BLOCK * SCAN32_ITEMS - 1) / (SCAN32_BLOCK * SCAN32_ITEMS);
-    k_scan32_partials<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials, gate);
-    k_scan32_final<<<(unsigned)nb, SCAN32_BLOCK, 0, st>>>(in, n, partials, out, gate);
+    uint64_t grid = nb;
+    if (gate) {
+        int dev = 0, sms = 152;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = std::min<uint64_t>(nb, 2 * (uint64_t)sms);
+    }
+    k_scan32_partials<<<(unsigned)grid, SCAN32_BLOCK, 0, st>>>(in, n, partials, gate, nb);
+    k_scan32_final<<<(unsigned)grid, SCAN32_BLOCK, 0, st>>>(in, n, partials, out, gate, nb);
     return cudaGetLastError();
 }
 
