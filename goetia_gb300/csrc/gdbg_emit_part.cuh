@@ -15,10 +15,11 @@
 // pass-1 tile: each record ranked by a shared-memory atomic as it is made
 // (it stays in registers), a block scan of the tile's counts, one atomic add
 // per (tile, group) on the group's fill count for the run's place, the runs
-// staged in shared memory and written out contiguously.  The records never go through HBM unpartitioned.  A group
-// that outgrows its slots sets *spill1; then the separate emit, its counts
-// and the counted pass 1, launched behind this kernel every time and idle
-// otherwise, make the exact layout instead.
+// staged in shared memory and written out contiguously.  The records never
+// go through HBM unpartitioned.  A group that outgrows its slots sets
+// *spill1; then the separate emit, its counts and the counted pass 1,
+// launched behind this kernel every time and idle otherwise, make the exact
+// layout instead.
 #pragma once
 
 #include "gdbg_sort.cuh"
