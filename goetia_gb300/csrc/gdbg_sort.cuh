@@ -924,9 +924,26 @@ k_sp_apply(TableParams tp, SortParams sp, const uint64_t* __restrict__ recs,
         if (lo < region_cells && tid == 0) atomicOr(sp.err, GDBG_ERR_CLAIMS_FULL);
     }
     __syncthreads();
-    // write back the region: every sector of a dense bucket, the dirty ones
-    // of a sparse one (8 words each)
     uint32_t* gdst = tp.words[ti] + w0;
+    if (!track && bulk_region) {
+        // a dense bucket: the whole region back by one bulk copy, which the
+        // copy engine reads out of shared memory while the SM goes on
+        if (tid == 0) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile(
+                "cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+                "r"(smem_addr(region)), "r"(nw * 4u)
+                : "memory");
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            // the CTA's shared memory stays until the copy has read it
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        }
+        occ = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)occ);
+        if ((tid & 31) == 0 && occ) atomicAdd(counters + 1, occ);
+        return;
+    }
+    // write back the region: the dirty sectors of a sparse bucket (8 words
+    // each), every sector otherwise
     for (uint32_t sec = tid; sec < region_sectors; sec += SP_APPLY_BLOCK) {
         if (track && !((dirty[sec >> 5] >> (sec & 31u)) & 1u)) continue;
         const uint32_t wb = sec * 8;
