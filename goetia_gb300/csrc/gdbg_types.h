@@ -96,7 +96,7 @@ struct BucketParams {
 // in an order-independent way.
 constexpr uint32_t SP_TILE = 4096;       // records per partition tile
 constexpr uint32_t SP_SEGK = 32768;      // k-mers per pass-1 segment (multiple of MAP_TILE)
-constexpr uint32_t SP_SEG2 = 32768;      // records per pass-2 segment
+constexpr uint32_t SP_SEG2 = 65536;      // records per pass-2 segment
 constexpr uint32_t SP_MAXBINS2 = 512;    // pass-2 digit bins at most
 
 struct SortParams {
