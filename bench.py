@@ -575,6 +575,62 @@ def run_batched(args, check_reads=2000, later_batch=4, cell_width=1 << 20):
     return stats, check
 
 
+def run_fastx(args, n_reads, seed):
+    """FASTQ text of one benchmark batch (the same seeded reads; each read
+    the generator marks for an 'N' gets one), parsed and packed on the GPU
+    by gdbg_parse_fastx_device (FastxParser<DNA_SIMPLE>::next over kseq,
+    then the packer's policy).  Timed with CUDA events over whole calls
+    (text already in HBM); checked against the batch the benchmark packs
+    from the same reads: packed words, offsets and dropped reads."""
+    import torch
+    from goetia_gb300 import synth, reads as R
+    g = synth.genome(GENOME_LEN, 3)
+    rows = synth.sample_reads(g, n_reads, READ_LEN, SUB_RATE, seed)
+    keep = ~synth.n_read_mask(n_reads, N_READ_FRAC, seed + 1)
+    seq = np.frombuffer(b"ACGT", np.uint8)[rows]
+    idx = np.nonzero(~keep)[0]
+    seq[idx, (idx * 37) % READ_LEN] = ord("N")
+    head = np.empty((n_reads, 10), np.uint8)
+    head[:, 0], head[:, 1], head[:, 9] = ord("@"), ord("r"), ord("\n")
+    i = np.arange(n_reads)
+    for d in range(7):
+        head[:, 2 + d] = (i // 10 ** (6 - d)) % 10 + ord("0")
+    nl = np.full((n_reads, 1), ord("\n"), np.uint8)
+    plus = np.tile(np.frombuffer(b"+\n", np.uint8), (n_reads, 1))
+    qual = np.full((n_reads, READ_LEN), ord("I"), np.uint8)
+    text = np.ascontiguousarray(np.concatenate([head, seq, nl, plus, qual, nl], axis=1)).reshape(-1)
+    expect = synth.rows_to_packed(rows[keep])
+    dev = torch.device("cuda", 0)
+    d_text = torch.from_numpy(text).to(dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize(dev)
+    for _ in range(2):
+        packed, offsets, st = R.parse_fastx_device(d_text, stream=stream.cuda_stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    torch.cuda.synchronize(dev)
+    ev0.record(stream)
+    for _ in range(reps):
+        packed, offsets, st = R.parse_fastx_device(d_text, stream=stream.cuda_stream)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1) / reps
+    off = offsets.cpu().numpy().view(np.uint64)
+    nw = (int(off[-1]) + 15) // 16
+    exact = (st["n_kept"] == expect.n_reads and st["n_dropped"] == int((~keep).sum()) and
+             np.array_equal(off, expect.offsets) and
+             np.array_equal(packed.cpu().numpy().view(np.uint32)[:nw], expect.packed[:nw]))
+    del d_text, packed, offsets
+    torch.cuda.empty_cache()
+    return {"text_GB_per_s": text.size / ms / 1e6, "reads_per_s": n_reads / ms * 1e3,
+            "ms_per_call": ms, "text_bytes": int(text.size), "reads": n_reads,
+            "reads_kept": st["n_kept"], "reads_dropped": st["n_dropped"],
+            "exact_vs_host_packed_batch": bool(exact),
+            "workload": f"FASTQ text of one benchmark batch ({n_reads} reads x {READ_LEN} bp, "
+                        "four-line records, N-reads dropped), in HBM; one "
+                        "gdbg_parse_fastx_device call (count, lines, classify, gather, pack)"}
+
+
 def run_profile_case(args):
     """The small case the ncu captures run: dBG<ByteStorage, CanLemireShifter>,
     K=31, 4 x ~2^28 cells (1 GiB of tables, 8x L2) through the segmented path,
@@ -893,6 +949,9 @@ def run_gpu(args):
     mask_stats = None
     if not args.no_masks:
         mask_stats, checks["decision_masks"] = run_masks(args)
+    fastx_stats = None
+    if not args.no_fastx:
+        fastx_stats = run_fastx(args, args.reads_per_step, 4 + 7919 * rank)
     serving_stats = None
     if not args.no_serving:
         del g, g3
@@ -948,6 +1007,7 @@ def run_gpu(args):
             "serving": serving_stats,
             "decision_masks": mask_stats,
             "batched_uneven": batched_stats,
+            "fastx_parse": fastx_stats,
             "roofline": roofline,
             "oracle_check": exact or None,
             "cpu_baseline": cpu,
@@ -974,6 +1034,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-masks", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-fastx", action="store_true")
     ap.add_argument("--no-oracle-check", action="store_true",
                     help="skip the oracle check of the timed run's end state")
     ap.add_argument("--batched-reads", type=int, default=2_000_000)

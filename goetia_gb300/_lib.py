@@ -63,6 +63,7 @@ SIGNATURES = {
     "gdbg_query_hashes": [c_vp, u64p, c_u64, i16p],
     "gdbg_neighbor_masks": [c_vp, c_cp, c_u64, u8p],
     "gdbg_pack_reads_device": [c_vp, c_vp, c_u64, c_u32, c_vp, c_u64, c_vp, u64p, u64p, c_vp],
+    "gdbg_parse_fastx_device": [c_vp, c_u64, c_u32, c_vp, c_u64, c_vp, c_u64, u64p, c_vp],
     "gdbg_pack_reads": [c_cp, u64p, c_u64, c_u32, u32p, c_u64, u64p, u64p, u64p],
     "gdbg_pack_codes": [u8p, c_u64, u32p],
     "gdbg_insert_batch": [c_vp, u32p, c_u64, u64p, c_u64, u64p, u64p],

@@ -124,6 +124,13 @@ cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams
                             uint32_t* new_bits, unsigned long long* counters, cudaStream_t st);
 size_t sp_apply_smem_bytes(int storage, uint32_t fs);
 
+// Device packing of text reads (gdbg_pack_device.cu): read r =
+// seqs[seq_offsets[r], seq_offsets[r + 1]); out[0] kept, [1] dropped, [2]
+// dropped reads both invalid and shorter than min_length.  Synchronous.
+int pack_device_run(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
+                    uint32_t min_length, uint32_t* packed, uint64_t packed_words,
+                    uint64_t* offsets, uint64_t out[3], cudaStream_t st);
+
 // Compactor query (gdbg_compactor.cu): per k-mer new / seen flags and the
 // neighbour masks over the storage plus each read's new k-mers.  keys /
 // minpos hold compactor_slots() entries set to all ones, allones n_reads.

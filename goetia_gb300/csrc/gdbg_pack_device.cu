@@ -30,7 +30,7 @@ __device__ __forceinline__ uint32_t pk_code(unsigned char c) {
 __global__ void __launch_bounds__(PK_BLOCK)
 k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ so, uint64_t n,
            uint32_t min_len, uint32_t* __restrict__ klen, uint32_t* __restrict__ kflag,
-           uint32_t* err) {
+           uint32_t* err, uint32_t* both) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_warps = (uint64_t)gridDim.x * PK_BLOCK / 32;
     for (uint64_t r = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32; r < n; r += n_warps) {
@@ -44,6 +44,8 @@ k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
         if (lane == 0) {
             klen[r] = kept ? (uint32_t)L : 0u;
             kflag[r] = kept ? 1u : 0u;
+            // FastxParser counts a read that is invalid and short twice
+            if (both && !ok && L < min_len) atomicAdd(both, 1u);
         }
     }
 }
@@ -77,12 +79,71 @@ k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
 }
 
 __global__ void k_pk_final(const uint32_t* klen, const uint32_t* kbase, const uint32_t* kflag,
-                           const uint32_t* kidx, uint64_t n, uint64_t* offsets, uint64_t* counts) {
+                           const uint32_t* kidx, uint64_t n, uint64_t* offsets, uint64_t* counts,
+                           const uint32_t* both) {
     offsets[0] = 0;
     const uint64_t kept = n ? (uint64_t)kidx[n - 1] + kflag[n - 1] : 0;
     counts[0] = kept;
     counts[1] = n - kept;
     counts[2] = n ? (uint64_t)kbase[n - 1] + klen[n - 1] : 0;
+    counts[3] = *both;
+}
+
+// The packing of n_seqs text reads in device memory (read r = seqs[so[r],
+// so[r + 1])); out[0] kept, [1] dropped, [2] dropped reads that were both
+// invalid and shorter than min_length.  Returns when done.
+int pack_device_run(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
+                    uint32_t min_length, uint32_t* packed, uint64_t packed_words,
+                    uint64_t* offsets, uint64_t out[3], cudaStream_t st) {
+    if (n_seqs >= (1ull << 31)) return report_error(GDBG_ERR_INVALID_ARG, "too many reads for one call");
+    const uint64_t parts = scan32_partials_needed(n_seqs + 1) + 1;
+    // scratch: klen, kflag, kbase, kidx (n + 1 each), scan partials, err, both, counts
+    const size_t bytes = (4 * (n_seqs + 1) + parts + 2) * sizeof(uint32_t) + 5 * sizeof(uint64_t);
+    void* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, bytes, st);
+    if (e != cudaSuccess) return report_error(GDBG_ERR_OOM, std::string("pack scratch: ") + cudaGetErrorString(e));
+    uint32_t* klen = (uint32_t*)scratch;
+    uint32_t* kflag = klen + (n_seqs + 1);
+    uint32_t* kbase = kflag + (n_seqs + 1);
+    uint32_t* kidx = kbase + (n_seqs + 1);
+    uint32_t* partials = kidx + (n_seqs + 1);
+    uint32_t* err = partials + parts;
+    uint32_t* both = err + 1;
+    uint64_t* counts = (uint64_t*)(((uintptr_t)(both + 1) + 7) & ~(uintptr_t)7);
+    auto done = [&](int rc, const std::string& msg) {
+        cudaFreeAsync(scratch, st);
+        cudaStreamSynchronize(st);
+        return rc == GDBG_OK ? rc : report_error(rc, msg);
+    };
+    if ((e = cudaMemsetAsync(err, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess ||
+        (packed_words && (e = cudaMemsetAsync(packed, 0, packed_words * sizeof(uint32_t), st)) != cudaSuccess))
+        return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    uint64_t grid = (n_seqs * 32 + PK_BLOCK - 1) / PK_BLOCK;
+    if (grid > 152 * 32) grid = 152 * 32;
+    if (grid == 0) grid = 1;
+    k_pk_check<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, seq_offsets, n_seqs,
+                                                    min_length, klen, kflag, err, both);
+    if (n_seqs) {
+        if ((e = launch_scan32(klen, kbase, n_seqs, partials, st)) != cudaSuccess ||
+            (e = launch_scan32(kflag, kidx, n_seqs, partials, st)) != cudaSuccess)
+            return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    k_pk_write<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, seq_offsets, n_seqs,
+                                                    klen, kflag, kbase, kidx, packed, packed_words,
+                                                    offsets, err);
+    k_pk_final<<<1, 1, 0, st>>>(klen, kbase, kflag, kidx, n_seqs, offsets, counts, both);
+    if ((e = cudaGetLastError()) != cudaSuccess) return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    uint64_t hc[4] = {0, 0, 0, 0};
+    uint32_t herr = 0;
+    cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(scratch, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return report_error(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    if (herr) return report_error(GDBG_ERR_INVALID_ARG, "read offsets decrease, a read is 2^31 bases or longer, or packed is too small");
+    out[0] = hc[0];
+    out[1] = hc[1];
+    out[2] = hc[3];
+    return GDBG_OK;
 }
 
 }  // namespace gdbg
@@ -96,52 +157,11 @@ extern "C" int gdbg_pack_reads_device(const char* seqs, const uint64_t* seq_offs
     if (!seq_offsets || !offsets || !n_kept || !n_skipped || (!seqs && n_seqs) ||
         (!packed && packed_words))
         return report_error(GDBG_ERR_INVALID_ARG, "NULL argument");
-    if (n_seqs >= (1ull << 31)) return report_error(GDBG_ERR_INVALID_ARG, "too many reads for one call");
-    cudaStream_t st = (cudaStream_t)stream;
-    const uint64_t parts = scan32_partials_needed(n_seqs + 1) + 1;
-    // scratch: klen, kflag, kbase, kidx (n + 1 each), scan partials, err, counts
-    const size_t bytes = (4 * (n_seqs + 1) + parts + 1) * sizeof(uint32_t) + 4 * sizeof(uint64_t);
-    void* scratch = nullptr;
-    cudaError_t e = cudaMallocAsync(&scratch, bytes, st);
-    if (e != cudaSuccess) return report_error(GDBG_ERR_OOM, std::string("pack scratch: ") + cudaGetErrorString(e));
-    uint32_t* klen = (uint32_t*)scratch;
-    uint32_t* kflag = klen + (n_seqs + 1);
-    uint32_t* kbase = kflag + (n_seqs + 1);
-    uint32_t* kidx = kbase + (n_seqs + 1);
-    uint32_t* partials = kidx + (n_seqs + 1);
-    uint32_t* err = partials + parts;
-    uint64_t* counts = (uint64_t*)(((uintptr_t)(err + 1) + 7) & ~(uintptr_t)7);
-    auto done = [&](int rc, const std::string& msg) {
-        cudaFreeAsync(scratch, st);
-        cudaStreamSynchronize(st);
-        return rc == GDBG_OK ? rc : report_error(rc, msg);
-    };
-    if ((e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st)) != cudaSuccess ||
-        (packed_words && (e = cudaMemsetAsync(packed, 0, packed_words * sizeof(uint32_t), st)) != cudaSuccess))
-        return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
-    uint64_t grid = (n_seqs * 32 + PK_BLOCK - 1) / PK_BLOCK;
-    if (grid > 152 * 32) grid = 152 * 32;
-    if (grid == 0) grid = 1;
-    k_pk_check<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, seq_offsets, n_seqs,
-                                                    min_length, klen, kflag, err);
-    if (n_seqs) {
-        if ((e = launch_scan32(klen, kbase, n_seqs, partials, st)) != cudaSuccess ||
-            (e = launch_scan32(kflag, kidx, n_seqs, partials, st)) != cudaSuccess)
-            return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
-    }
-    k_pk_write<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, seq_offsets, n_seqs,
-                                                    klen, kflag, kbase, kidx, packed, packed_words,
-                                                    offsets, err);
-    k_pk_final<<<1, 1, 0, st>>>(klen, kbase, kflag, kidx, n_seqs, offsets, counts);
-    if ((e = cudaGetLastError()) != cudaSuccess) return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
-    uint64_t hc[3] = {0, 0, 0};
-    uint32_t herr = 0;
-    cudaMemcpyAsync(hc, counts, sizeof hc, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, st);
-    cudaFreeAsync(scratch, st);
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return report_error(GDBG_ERR_CUDA, cudaGetErrorString(e));
-    if (herr) return report_error(GDBG_ERR_INVALID_ARG, "read offsets decrease, a read is 2^31 bases or longer, or packed is too small");
-    *n_kept = hc[0];
-    *n_skipped = hc[1];
+    uint64_t out[3];
+    const int rc = pack_device_run(seqs, seq_offsets, n_seqs, min_length, packed, packed_words,
+                                   offsets, out, (cudaStream_t)stream);
+    if (rc != GDBG_OK) return rc;
+    *n_kept = out[0];
+    *n_skipped = out[1];
     return GDBG_OK;
 }

@@ -119,6 +119,31 @@ def concat(parts):
     return PackedReads(out.astype(np.uint32), np.concatenate(offs))
 
 
+def parse_fastx_device(text, min_length=0, stream=None):
+    """FASTA / FASTQ text (torch uint8 CUDA tensor) -> what FastxParser's
+    next() yields, packed on the GPU (gdbg_parse_fastx_device).  Returns
+    (packed int32 tensor, offsets int64 tensor of n_kept+1, stats dict with
+    n_kept / n_dropped / n_parsed / n_skipped).  Text outside the regular
+    FASTA / four-line FASTQ layouts raises GoetiaError with code
+    ERR_UNSUPPORTED: parse it on the host."""
+    import torch
+    dev = text.device
+    n = int(text.numel())
+    words = n // 16 + 1
+    packed = torch.empty(words, dtype=torch.int32, device=dev)
+    # records <= lines: one entry per line (and one more) always suffices
+    cap = int((text == 10).sum().item()) + 2 if n else 1
+    offsets = torch.empty(cap, dtype=torch.int64, device=dev)
+    st = np.zeros(4, np.uint64)
+    if stream is None:
+        stream = torch.cuda.current_stream(dev).cuda_stream
+    _lib.call("gdbg_parse_fastx_device", text.data_ptr() if n else None, n, min_length,
+              packed.data_ptr(), words, offsets.data_ptr(), cap, _p(st, _lib.u64p), stream or None)
+    k = int(st[0])
+    return packed, offsets[:k + 1], {"n_kept": k, "n_dropped": int(st[1]),
+                                     "n_parsed": int(st[2]), "n_skipped": int(st[3])}
+
+
 def pack_reads_device(seqs, seq_offsets, min_length=0, stream=None):
     """pack_reads on the GPU.  seqs: torch uint8 CUDA tensor of the reads'
     bytes; seq_offsets: torch int64 CUDA tensor of n+1 byte offsets.

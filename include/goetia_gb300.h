@@ -174,6 +174,25 @@ int gdbg_pack_reads_device(const char* seqs, const uint64_t* seq_offsets, uint64
                            uint32_t min_length, uint32_t* packed, uint64_t packed_words,
                            uint64_t* offsets, uint64_t* n_kept, uint64_t* n_skipped,
                            void* stream);
+/* FastxParser<DNA_SIMPLE>::next called until the end (readers.hh:150-219,
+ * over kseq, kseq.h:88-220) on FASTA / FASTQ text in device memory
+ * (uncompressed, below 2^32 - 1 bytes), then gdbg_pack_reads_device's
+ * policy and packing of the sequences.  Records are found in parallel for
+ * the regular layouts -- four-line FASTQ records (one sequence line, one
+ * quality line of its length); FASTA with sequences over any number of
+ * lines and no line starting with '+' -- and the result is then what kseq
+ * gives; other text (several quality lines, junk before the first header,
+ * blank lines after a FASTQ record ...) is GDBG_ERR_UNSUPPORTED, naming the
+ * first line that breaks the layout, for the caller to parse on the host.
+ * stats: [0] reads kept, [1] reads dropped, [2] records parsed
+ * (FastxParser::n_parsed), [3] FastxParser::n_skipped (a read both invalid
+ * and shorter than min_length counts twice).  offsets needs stats[2] + 1
+ * entries (GDBG_ERR_INVALID_ARG with stats[2] set otherwise), packed the
+ * sequence bytes / 16 + 1 words (n_bytes / 16 + 1 always suffices).  Runs
+ * on `stream` and returns when done. */
+int gdbg_parse_fastx_device(const char* text, uint64_t n_bytes, uint32_t min_length,
+                            uint32_t* packed, uint64_t packed_words, uint64_t* offsets,
+                            uint64_t offsets_cap, uint64_t* stats, void* stream);
 /* 2-bit codes (one byte each, values 0..3) to the packed stream. */
 int gdbg_pack_codes(const uint8_t* codes, uint64_t n, uint32_t* packed);
 

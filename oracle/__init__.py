@@ -77,6 +77,10 @@ def lib():
         L.orc_pack_ascii.restype = ctypes.c_int64
         L.orc_pack_ascii.argtypes = [ctypes.c_char_p, u64p, ctypes.c_uint64, ctypes.c_uint32,
                                      u32p, u64p, u64p]
+        L.orc_parse_fastx.restype = ctypes.c_int64
+        L.orc_parse_fastx.argtypes = [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_uint32,
+                                      ctypes.c_char_p, ctypes.c_uint64, u64p, ctypes.c_uint64,
+                                      u64p]
         L.orc_symbol_table.argtypes = [u64p]
         L.orc_count_cells.restype = ctypes.c_int
         L.orc_count_cells.argtypes = [ctypes.c_int, ctypes.c_uint16, u32p, u64p, ctypes.c_uint64,
@@ -237,6 +241,31 @@ def pack_ascii(seqs, min_length=0):
     kept = lib().orc_pack_ascii(data, _p(so, u64p), len(seqs), min_length, _p(packed, u32p),
                                 _p(offsets, u64p), ctypes.byref(skipped))
     return packed, offsets[:kept + 1].copy(), int(skipped.value)
+
+
+def parse_fastx(text, min_length=0):
+    """FastxParser<DNA_SIMPLE>::next over FASTA/FASTQ text until the end
+    (kseq grammar).  Returns (kept sequences as a list of bytes, stats dict
+    with n_parsed / n_skipped / n_dropped, status): status 0, or -2 when
+    kseq reported differing sequence and quality lengths at record
+    stats["invalid_record"] (the reads before it are kept)."""
+    text = bytes(text)
+    cap = len(text) + 1
+    out = ctypes.create_string_buffer(cap)
+    rec_cap = len(text) // 2 + 2
+    off = np.zeros(rec_cap + 1, np.uint64)
+    st = np.zeros(4, np.uint64)
+    r = lib().orc_parse_fastx(text, len(text), min_length, out, cap, _p(off, u64p), rec_cap,
+                              _p(st, u64p))
+    if r == -5:
+        raise RuntimeError("parse_fastx: output capacity")
+    raw = out.raw
+    # at an InvalidRead, the reads kept before it: every parsed read was kept or dropped
+    kept = int(r) if r >= 0 else int(st[0] - st[2])
+    seqs = [raw[int(off[i]):int(off[i + 1])] for i in range(kept)]
+    stats = {"n_parsed": int(st[0]), "n_skipped": int(st[1]), "n_dropped": int(st[2]),
+             "invalid_record": int(st[3]) if r == -2 else None}
+    return seqs, stats, (0 if r >= 0 else int(r))
 
 
 # ---- OXLI v4 table files ----------------------------------------------------

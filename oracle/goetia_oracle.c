@@ -661,3 +661,121 @@ int64_t orc_pack_ascii(const char* seqs, const uint64_t* so, uint64_t n, uint32_
     *n_skipped = skipped;
     return (int64_t)kept;
 }
+
+/* ---- FASTA/FASTQ records (kseq.h:88-220, readers.hh:150-219) ------------ */
+
+/* The stream: text[pos..n).  ks_getc (kseq.h: one byte, -1 at the end). */
+typedef struct {
+    const char* s;
+    uint64_t n, pos;
+} orc_ks;
+
+static int ks_getc_(orc_ks* k) { return k->pos < k->n ? (unsigned char)k->s[k->pos++] : -1; }
+
+/* kstring_t (kseq.h:78-82): a growing byte string. */
+typedef struct {
+    char* s;
+    uint64_t l, cap;
+} orc_kstr;
+
+static void kstr_put(orc_kstr* t, const char* src, uint64_t m) {
+    if (t->l + m + 1 > t->cap) {
+        t->cap = 2 * (t->l + m) + 64;
+        t->s = (char*)realloc(t->s, t->cap);
+    }
+    memcpy(t->s + t->l, src, m);
+    t->l += m;
+}
+
+static int ks_isspace(int c) {
+    return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r';
+}
+
+/* ks_getuntil2 (kseq.h:88-139) with KS_SEP_SPACE (line = 0) or KS_SEP_LINE
+ * (line = 1): bytes up to the delimiter go to t (appended when append), the
+ * delimiter is consumed and reported in *dret (0 at the end of the text).
+ * -1 when the text had ended before the call; else the string's length,
+ * after dropping one trailing '\r' of a line string longer than one byte. */
+static int64_t ks_until(orc_ks* k, int line, orc_kstr* t, int append, int* dret) {
+    if (dret) *dret = 0;
+    if (!append) t->l = 0;
+    if (k->pos >= k->n) return -1;
+    uint64_t i = k->pos;
+    while (i < k->n && !(line ? k->s[i] == '\n' : ks_isspace((unsigned char)k->s[i]))) ++i;
+    kstr_put(t, k->s + k->pos, i - k->pos);
+    if (i < k->n && dret) *dret = (unsigned char)k->s[i];
+    k->pos = i < k->n ? i + 1 : k->n;
+    if (line && t->l > 1 && t->s[t->l - 1] == '\r') --t->l;
+    return (int64_t)t->l;
+}
+
+/* kseq_read (kseq.h:173-220): >= 0 the sequence length, -1 end, -2 the
+ * sequence and quality lengths differ (or no quality line). */
+static int64_t kseq_read_(orc_ks* k, int* last_char, orc_kstr* name, orc_kstr* comment,
+                          orc_kstr* seq, orc_kstr* qual) {
+    int c;
+    if (*last_char == 0) {
+        while ((c = ks_getc_(k)) >= 0 && c != '>' && c != '@') {}
+        if (c < 0) return c;
+        *last_char = c;
+    }
+    comment->l = seq->l = qual->l = 0;
+    const int64_t r = ks_until(k, 0, name, 0, &c);
+    if (r < 0) return r;
+    if (c != '\n') ks_until(k, 1, comment, 0, NULL);
+    while ((c = ks_getc_(k)) >= 0 && c != '>' && c != '+' && c != '@') {
+        if (c == '\n') continue;   /* empty lines */
+        const char ch = (char)c;
+        kstr_put(seq, &ch, 1);
+        ks_until(k, 1, seq, 1, NULL);
+    }
+    if (c == '>' || c == '@') *last_char = c;
+    if (c != '+') return (int64_t)seq->l;   /* FASTA */
+    while ((c = ks_getc_(k)) >= 0 && c != '\n') {}   /* rest of the '+' line */
+    if (c == -1) return -2;
+    while (ks_until(k, 1, qual, 1, NULL) >= 0 && qual->l < seq->l) {}
+    *last_char = 0;
+    if (seq->l != qual->l) return -2;
+    return (int64_t)seq->l;
+}
+
+int64_t orc_parse_fastx(const char* text, uint64_t n, uint32_t min_length, char* seq_out,
+                        uint64_t seq_cap, uint64_t* seq_off, uint64_t rec_cap,
+                        uint64_t stats[4]) {
+    orc_ks k = {text, n, 0};
+    int last_char = 0;
+    orc_kstr name = {0}, comment = {0}, seq = {0}, qual = {0};
+    uint64_t kept = 0, used = 0;
+    int64_t ret = 0;
+    stats[0] = stats[1] = stats[2] = stats[3] = 0;
+    seq_off[0] = 0;
+    for (;;) {
+        const int64_t stat = kseq_read_(&k, &last_char, &name, &comment, &seq, &qual);
+        if (stat == -1) break;
+        if (stat == -2) {
+            stats[1]++;
+            stats[3] = stats[0];
+            ret = -2;
+            break;
+        }
+        /* FastxParser::next: Alphabet::validate, then the length filter */
+        int valid = 1;
+        for (uint64_t i = 0; i < seq.l; ++i) {
+            const char c = seq.s[i];
+            const char u = (c == 'a') ? 'A' : (c == 'c') ? 'C' : (c == 'g') ? 'G' : (c == 't') ? 'T' : c;
+            if (u != 'A' && u != 'C' && u != 'G' && u != 'T') { valid = 0; break; }
+            seq.s[i] = u;
+        }
+        int keep = valid;
+        if (!valid) stats[1]++;
+        if (seq.l < min_length) { keep = 0; stats[1]++; }
+        stats[0]++;
+        if (!keep) { stats[2]++; continue; }
+        if (kept >= rec_cap || used + seq.l > seq_cap) { ret = -5; break; }
+        memcpy(seq_out + used, seq.s, seq.l);
+        used += seq.l;
+        seq_off[++kept] = used;
+    }
+    free(name.s); free(comment.s); free(seq.s); free(qual.s);
+    return ret < 0 ? ret : (int64_t)kept;
+}

@@ -91,6 +91,19 @@ int64_t  orc_pack_ascii(const char* seqs, const uint64_t* seq_offsets, uint64_t 
                         uint32_t min_length, uint32_t* packed, uint64_t* offsets,
                         uint64_t* n_skipped);
 
+/* FastxParser<DNA_SIMPLE>::next over FASTA/FASTQ text held in memory (kseq
+ * grammar, kseq.h:88-220; parser policy, readers.hh:150-219), called until
+ * the stream ends.  The kept reads' sequences (upper-cased) go to seq_out
+ * (seq_cap bytes) with their seq_off[0..kept] offsets (rec_cap + 1 entries).
+ * stats: [0] n_parsed, [1] n_skipped (FastxParser's counters: a read that is
+ * both invalid and shorter than min_length counts twice), [2] reads
+ * dropped, [3] the record at which kseq reported differing sequence and
+ * quality lengths.  Returns the kept count, -2 at that InvalidRead (reads
+ * before it are kept), -5 when seq_cap or rec_cap is too small. */
+int64_t  orc_parse_fastx(const char* text, uint64_t n, uint32_t min_length, char* seq_out,
+                         uint64_t seq_cap, uint64_t* seq_off, uint64_t rec_cap,
+                         uint64_t stats[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -141,3 +141,26 @@ def test_multithreaded_insert_equals_sequential(kind):
         assert any((t == 255).any() for t in seq.tables())          # saturated cells
     elif kind == "nibble":
         assert any(((t >> 4) == 15).any() for t in seq.tables())
+
+
+def _fastx_golden():
+    import os
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "fastx.npz"))
+
+
+def test_fastx_parser_vs_reference():
+    """The oracle's kseq / FastxParser restatement against what the
+    reference's own FastxParser<DNA_SIMPLE> returned for every FASTX case
+    (tests/golden/make_fastx_golden.py): kept sequences, n_parsed,
+    n_skipped (double counts included) and the InvalidRead throw."""
+    z = _fastx_golden()
+    for name in z["names"]:
+        text = z[name + "__text"].tobytes()
+        for ml in z["min_lengths"]:
+            k = f"{name}__m{ml}"
+            seq, off, st = z[k + "__seq"].tobytes(), z[k + "__off"], z[k + "__stats"]
+            gold = [seq[int(off[i]):int(off[i + 1])] for i in range(len(off) - 1)]
+            got, stats, status = oracle.parse_fastx(text, int(ml))
+            assert got == gold, k
+            assert (stats["n_parsed"], stats["n_skipped"]) == (int(st[0]), int(st[1])), k
+            assert (status == -2) == bool(st[2]), k
