@@ -1052,12 +1052,19 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)
     ap.add_argument("--profile-case", action="store_true",
                     help="run only the small insert case the ncu captures profile")
+    ap.add_argument("--profile-fastx", action="store_true",
+                    help="run only the FASTQ parse leg (one benchmark batch as text)")
     ap.add_argument("--profile-masks", action="store_true",
                     help="run only the decision-mask case the ncu captures profile "
                          "(--mask-reads query reads)")
     args = ap.parse_args()
     if args.profile_case:
         return run_profile_case(args)
+    if args.profile_fastx:
+        from goetia_gb300 import build as gbuild
+        gbuild.build()
+        print(json.dumps(run_fastx(args, args.reads_per_step, 4)), flush=True)
+        return 0
     if args.profile_masks:
         return run_profile_masks(args)
     if args.warmup < 3:

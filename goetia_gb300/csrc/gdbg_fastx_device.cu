@@ -263,7 +263,7 @@ extern "C" int gdbg_parse_fastx_device(const char* text, uint64_t n_bytes, uint3
     const uint64_t n_tiles = (n_bytes + FX_TILE - 1) / FX_TILE;
     std::vector<void*> bufs;
     auto alloc = [&](size_t bytes, void** p) {
-        const cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, st);
+        const cudaError_t e = scratch_alloc(p, bytes, st);
         if (e == cudaSuccess) bufs.push_back(*p);
         return e;
     };

@@ -124,6 +124,11 @@ cudaError_t launch_sp_apply(int storage, const TableParams& tp, const SortParams
                             uint32_t* new_bits, unsigned long long* counters, cudaStream_t st);
 size_t sp_apply_smem_bytes(int storage, uint32_t fs);
 
+// Stream-ordered scratch (free with cudaFreeAsync) from the library's own
+// pool of the current device, which keeps up to 2 GiB between calls
+// (gdbg_pack_device.cu).
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t st);
+
 // Device packing of text reads (gdbg_pack_device.cu): read r =
 // seqs[seq_offsets[r], seq_offsets[r + 1]); out[0] kept, [1] dropped, [2]
 // dropped reads both invalid and shorter than min_length.  Synchronous.

@@ -13,6 +13,8 @@
 //   k_pk_final  counts and offsets[0]
 #include <cuda_runtime.h>
 
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "gdbg_launch.h"
@@ -89,6 +91,41 @@ __global__ void k_pk_final(const uint32_t* klen, const uint32_t* kbase, const ui
     counts[3] = *both;
 }
 
+// Scratch of the packer and the FASTX parser comes from a pool of the
+// library's own per device, which keeps up to SCRATCH_KEEP bytes between
+// calls: the device's default pool gives its memory back at every
+// synchronisation, and mapping a batch's scratch again costs more than the
+// batch's kernels.  The pools live as long as the process.
+constexpr uint64_t SCRATCH_KEEP = 2ull << 30;
+
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t st) {
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = pools.find(dev);
+        if (it == pools.end()) {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.handleTypes = cudaMemHandleTypeNone;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            if ((e = cudaMemPoolCreate(&pool, &props)) != cudaSuccess) return e;
+            uint64_t keep = SCRATCH_KEEP;
+            if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess)
+                return e;
+            pools[dev] = pool;
+        } else {
+            pool = it->second;
+        }
+    }
+    return cudaMallocFromPoolAsync(p, bytes ? bytes : 16, pool, st);
+}
+
 // The packing of n_seqs text reads in device memory (read r = seqs[so[r],
 // so[r + 1])); out[0] kept, [1] dropped, [2] dropped reads that were both
 // invalid and shorter than min_length.  Returns when done.
@@ -100,7 +137,7 @@ int pack_device_run(const char* seqs, const uint64_t* seq_offsets, uint64_t n_se
     // scratch: klen, kflag, kbase, kidx (n + 1 each), scan partials, err, both, counts
     const size_t bytes = (4 * (n_seqs + 1) + parts + 2) * sizeof(uint32_t) + 5 * sizeof(uint64_t);
     void* scratch = nullptr;
-    cudaError_t e = cudaMallocAsync(&scratch, bytes, st);
+    cudaError_t e = scratch_alloc(&scratch, bytes, st);
     if (e != cudaSuccess) return report_error(GDBG_ERR_OOM, std::string("pack scratch: ") + cudaGetErrorString(e));
     uint32_t* klen = (uint32_t*)scratch;
     uint32_t* kflag = klen + (n_seqs + 1);
