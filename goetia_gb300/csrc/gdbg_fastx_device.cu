@@ -28,8 +28,10 @@
 //   k_fx_lines     each newline's position, in order
 //   k_fx_classify  per line: header flag, sequence bytes (clen), layout check
 //   scans          sequence byte offsets (cpos), record index of each header
-//   k_fx_gather    one warp per sequence line: its bytes to the compacted
-//                  sequence buffer; each header writes its record's start
+//   k_fx_spans     FASTQ: each record's sequence as a span of the text
+//   k_fx_gather    FASTA: one warp per sequence line, its bytes to the
+//                  compacted sequence buffer; each header writes its
+//                  record's start
 //   pack_device_run  the packer's drop policy and 2-bit packing
 #include <cuda_runtime.h>
 
@@ -232,6 +234,19 @@ k_fx_gather(const unsigned char* __restrict__ text, uint64_t n, const uint32_t* 
     }
 }
 
+// FASTQ: record r's sequence is one span of the text (line 4r + 1 less a
+// trailing '\r'), handed to the packer in place.
+__global__ void __launch_bounds__(FX_BLOCK)
+k_fx_spans(const unsigned char* __restrict__ text, uint64_t n, const uint32_t* __restrict__ nlpos,
+           uint32_t n_nl, uint64_t n_rec, uint64_t* __restrict__ starts, uint64_t* __restrict__ ends) {
+    const uint64_t r = (uint64_t)blockIdx.x * FX_BLOCK + threadIdx.x;
+    if (r >= n_rec) return;
+    uint64_t s, e;
+    fx_line(nlpos, n_nl, n, (uint32_t)(4 * r + 1), s, e);
+    starts[r] = s;
+    ends[r] = s + fx_eff_len(text, s, e);
+}
+
 __global__ void k_fx_tail(const uint32_t* clen, const uint32_t* cpos, const uint32_t* hflag,
                           const uint32_t* hidx, uint32_t n_lines, uint64_t* out) {
     out[0] = (uint64_t)cpos[n_lines - 1] + clen[n_lines - 1];   // sequence bytes
@@ -342,21 +357,38 @@ extern "C" int gdbg_parse_fastx_device(const char* text, uint64_t n_bytes, uint3
                                               " entries (the text's records + 1)");
     if (packed_words < seq_bytes / 16 + 1)
         return done(GDBG_ERR_INVALID_ARG, "packed needs " + std::to_string(seq_bytes / 16 + 1) + " words");
-    // pass 3: the records' sequences side by side, their offsets
-    unsigned char* seqs;
-    uint64_t* so;
-    if ((e = alloc(seq_bytes, (void**)&seqs)) != cudaSuccess ||
-        (e = alloc((n_rec + 1) * sizeof(uint64_t), (void**)&so)) != cudaSuccess)
-        return done(GDBG_ERR_OOM, std::string("parse scratch: ") + cudaGetErrorString(e));
-    uint64_t ggrid = ((uint64_t)n_lines * 32 + FX_BLOCK - 1) / FX_BLOCK;
-    if (ggrid > 152 * 32) ggrid = 152 * 32;
-    k_fx_gather<<<(unsigned)ggrid, FX_BLOCK, 0, st>>>(t, n_bytes, nlpos, n_nl, n_lines, clen, cpos,
-                                                      hflag, hidx, seqs, so);
-    if ((e = cudaMemcpyAsync(so + n_rec, &hinfo[0], sizeof(uint64_t), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
-        (e = cudaGetLastError()) != cudaSuccess)
-        return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
+    // pass 3: the records' sequences -- FASTQ: spans of the text; FASTA:
+    // their lines' bytes side by side -- then the packer
+    const char* src;
+    const uint64_t *starts, *ends;
+    if (hbad[1]) {
+        uint64_t* sp;
+        if ((e = alloc(2 * n_rec * sizeof(uint64_t), (void**)&sp)) != cudaSuccess)
+            return done(GDBG_ERR_OOM, std::string("parse scratch: ") + cudaGetErrorString(e));
+        k_fx_spans<<<(unsigned)((n_rec + FX_BLOCK - 1) / FX_BLOCK), FX_BLOCK, 0, st>>>(
+            t, n_bytes, nlpos, n_nl, n_rec, sp, sp + n_rec);
+        src = text;
+        starts = sp;
+        ends = sp + n_rec;
+    } else {
+        unsigned char* seqs;
+        uint64_t* so;
+        if ((e = alloc(seq_bytes, (void**)&seqs)) != cudaSuccess ||
+            (e = alloc((n_rec + 1) * sizeof(uint64_t), (void**)&so)) != cudaSuccess)
+            return done(GDBG_ERR_OOM, std::string("parse scratch: ") + cudaGetErrorString(e));
+        uint64_t ggrid = ((uint64_t)n_lines * 32 + FX_BLOCK - 1) / FX_BLOCK;
+        if (ggrid > 152 * 32) ggrid = 152 * 32;
+        k_fx_gather<<<(unsigned)ggrid, FX_BLOCK, 0, st>>>(t, n_bytes, nlpos, n_nl, n_lines, clen,
+                                                          cpos, hflag, hidx, seqs, so);
+        if ((e = cudaMemcpyAsync(so + n_rec, &hinfo[0], sizeof(uint64_t), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+            return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
+        src = (const char*)seqs;
+        starts = so;
+        ends = so + 1;
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
     uint64_t out[3];
-    const int rc = pack_device_run((const char*)seqs, so, n_rec, min_length, packed, packed_words,
+    const int rc = pack_device_run(src, starts, ends, n_rec, min_length, packed, packed_words,
                                    offsets, out, st);
     if (rc != GDBG_OK) {
         for (void* p : bufs) cudaFreeAsync(p, st);

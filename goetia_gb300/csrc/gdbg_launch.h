@@ -130,9 +130,9 @@ size_t sp_apply_smem_bytes(int storage, uint32_t fs);
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t st);
 
 // Device packing of text reads (gdbg_pack_device.cu): read r =
-// seqs[seq_offsets[r], seq_offsets[r + 1]); out[0] kept, [1] dropped, [2]
-// dropped reads both invalid and shorter than min_length.  Synchronous.
-int pack_device_run(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
+// seqs[starts[r], ends[r]); out[0] kept, [1] dropped, [2] dropped reads
+// both invalid and shorter than min_length.  Synchronous.
+int pack_device_run(const char* seqs, const uint64_t* starts, const uint64_t* ends, uint64_t n_seqs,
                     uint32_t min_length, uint32_t* packed, uint64_t packed_words,
                     uint64_t* offsets, uint64_t out[3], cudaStream_t st);
 

@@ -7,9 +7,10 @@
 //
 //   k_pk_check  one warp per read: validity and kept length
 //   scans       kept bases and kept reads (exclusive, 32-bit)
-//   k_pk_write  one warp per kept read: each lane builds whole output words
-//               of the read and ORs them in (words at read boundaries are
-//               shared with the neighbour read); the read's end offset
+//   k_pk_write  one warp per kept read, 32 bases per step: codes merged
+//               into words by shuffles, written by each word's first lane
+//               (atomic OR for words shared with a neighbour read or split
+//               between steps); the read's end offset
 //   k_pk_final  counts and offsets[0]
 #include <cuda_runtime.h>
 
@@ -30,13 +31,14 @@ __device__ __forceinline__ uint32_t pk_code(unsigned char c) {
 }
 
 __global__ void __launch_bounds__(PK_BLOCK)
-k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ so, uint64_t n,
+k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ starts,
+           const uint64_t* __restrict__ ends, uint64_t n,
            uint32_t min_len, uint32_t* __restrict__ klen, uint32_t* __restrict__ kflag,
            uint32_t* err, uint32_t* both) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_warps = (uint64_t)gridDim.x * PK_BLOCK / 32;
     for (uint64_t r = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32; r < n; r += n_warps) {
-        const uint64_t a = so[r], b = so[r + 1];
+        const uint64_t a = starts[r], b = ends[r];
         bool ok = b >= a && b - a < (1ull << 31);
         if (!ok && lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
         const uint64_t L = ok ? b - a : 0;
@@ -52,8 +54,14 @@ k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
     }
 }
 
+// One warp per kept read, 32 bases per step: lane l converts base i0 + l
+// (coalesced byte loads) into its 2-bit code at output position p; the
+// lanes of one output word (at most 16 consecutive lanes) OR their codes
+// together by shuffles, and the word's first lane writes it -- a plain store
+// when all 16 of the word's bases are in this step, an atomic OR for a word
+// split between two steps or shared with a neighbour read at either end.
 __global__ void __launch_bounds__(PK_BLOCK)
-k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ so, uint64_t n,
+k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ starts, uint64_t n,
            const uint32_t* __restrict__ klen, const uint32_t* __restrict__ kflag,
            const uint32_t* __restrict__ kbase, const uint32_t* __restrict__ kidx,
            uint32_t* __restrict__ packed, uint64_t packed_words, uint64_t* __restrict__ offsets,
@@ -63,18 +71,28 @@ k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
     for (uint64_t r = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32; r < n; r += n_warps) {
         if (!kflag[r]) continue;   // kept reads include empty ones (min_length 0)
         const uint64_t L = klen[r];
-        const uint64_t a = so[r], ob0 = kbase[r], ob1 = ob0 + L;
-        for (uint64_t w = ob0 / 16 + lane; w * 16 < ob1; w += 32) {
-            if (w >= packed_words) {
-                atomicOr(err, GDBG_ERR_BAD_OFFSETS);
-                break;
+        const uint64_t a = starts[r], ob0 = kbase[r], ob1 = ob0 + L;
+        if (L && (ob1 - 1) / 16 >= packed_words) {
+            if (lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
+            continue;
+        }
+        for (uint64_t i0 = 0; i0 < L; i0 += 32) {
+            const uint64_t i = i0 + lane;
+            const uint64_t p = ob0 + i;
+            const uint32_t q = (uint32_t)(p & 15u);
+            uint32_t v = i < L ? pk_code(seqs[a + i]) << (2u * q) : 0u;
+#pragma unroll
+            for (uint32_t o = 1; o < 16; o <<= 1) {
+                const uint32_t y = __shfl_down_sync(0xFFFFFFFFu, v, o);
+                if (lane + o < 32 && q + o < 16) v |= y;
             }
-            uint32_t v = 0;
-            for (uint32_t q = 0; q < 16; ++q) {
-                const uint64_t j = w * 16 + q;
-                if (j >= ob0 && j < ob1) v |= pk_code(seqs[a + (j - ob0)]) << (2u * q);
+            if (i < L && (q == 0 || lane == 0)) {
+                // a word whose 16 bases are all this step's gets a plain store;
+                // one split between steps or shared with a neighbour read, ORs
+                const uint64_t w = p >> 4;
+                if (q == 0 && lane + 15 < 32 && i + 16 <= L) packed[w] = v;
+                else atomicOr(packed + w, v);
             }
-            if (v) atomicOr(packed + w, v);
         }
         if (lane == 0) offsets[(uint64_t)kidx[r] + 1] = ob1;
     }
@@ -126,10 +144,10 @@ cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t st) {
     return cudaMallocFromPoolAsync(p, bytes ? bytes : 16, pool, st);
 }
 
-// The packing of n_seqs text reads in device memory (read r = seqs[so[r],
-// so[r + 1])); out[0] kept, [1] dropped, [2] dropped reads that were both
-// invalid and shorter than min_length.  Returns when done.
-int pack_device_run(const char* seqs, const uint64_t* seq_offsets, uint64_t n_seqs,
+// The packing of n_seqs text reads in device memory (read r =
+// seqs[starts[r], ends[r])); out[0] kept, [1] dropped, [2] dropped reads
+// that were both invalid and shorter than min_length.  Returns when done.
+int pack_device_run(const char* seqs, const uint64_t* starts, const uint64_t* ends, uint64_t n_seqs,
                     uint32_t min_length, uint32_t* packed, uint64_t packed_words,
                     uint64_t* offsets, uint64_t out[3], cudaStream_t st) {
     if (n_seqs >= (1ull << 31)) return report_error(GDBG_ERR_INVALID_ARG, "too many reads for one call");
@@ -158,14 +176,14 @@ int pack_device_run(const char* seqs, const uint64_t* seq_offsets, uint64_t n_se
     uint64_t grid = (n_seqs * 32 + PK_BLOCK - 1) / PK_BLOCK;
     if (grid > 152 * 32) grid = 152 * 32;
     if (grid == 0) grid = 1;
-    k_pk_check<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, seq_offsets, n_seqs,
+    k_pk_check<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, starts, ends, n_seqs,
                                                     min_length, klen, kflag, err, both);
     if (n_seqs) {
         if ((e = launch_scan32(klen, kbase, n_seqs, partials, st)) != cudaSuccess ||
             (e = launch_scan32(kflag, kidx, n_seqs, partials, st)) != cudaSuccess)
             return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
     }
-    k_pk_write<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, seq_offsets, n_seqs,
+    k_pk_write<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, starts, n_seqs,
                                                     klen, kflag, kbase, kidx, packed, packed_words,
                                                     offsets, err);
     k_pk_final<<<1, 1, 0, st>>>(klen, kbase, kflag, kidx, n_seqs, offsets, counts, both);
@@ -195,8 +213,8 @@ extern "C" int gdbg_pack_reads_device(const char* seqs, const uint64_t* seq_offs
         (!packed && packed_words))
         return report_error(GDBG_ERR_INVALID_ARG, "NULL argument");
     uint64_t out[3];
-    const int rc = pack_device_run(seqs, seq_offsets, n_seqs, min_length, packed, packed_words,
-                                   offsets, out, (cudaStream_t)stream);
+    const int rc = pack_device_run(seqs, seq_offsets, seq_offsets + 1, n_seqs, min_length, packed,
+                                   packed_words, offsets, out, (cudaStream_t)stream);
     if (rc != GDBG_OK) return rc;
     *n_kept = out[0];
     *n_skipped = out[1];

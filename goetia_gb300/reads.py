@@ -131,14 +131,22 @@ def parse_fastx_device(text, min_length=0, stream=None):
     n = int(text.numel())
     words = n // 16 + 1
     packed = torch.empty(words, dtype=torch.int32, device=dev)
-    # records <= lines: one entry per line (and one more) always suffices
-    cap = int((text == 10).sum().item()) + 2 if n else 1
-    offsets = torch.empty(cap, dtype=torch.int64, device=dev)
+    # a guess of one record per 32 bytes; a text of shorter records is parsed
+    # again with the record count the first call reports
+    cap = n // 32 + 2
     st = np.zeros(4, np.uint64)
     if stream is None:
         stream = torch.cuda.current_stream(dev).cuda_stream
-    _lib.call("gdbg_parse_fastx_device", text.data_ptr() if n else None, n, min_length,
-              packed.data_ptr(), words, offsets.data_ptr(), cap, _p(st, _lib.u64p), stream or None)
+    for _ in range(2):
+        offsets = torch.empty(cap, dtype=torch.int64, device=dev)
+        rc = _lib.load().gdbg_parse_fastx_device(text.data_ptr() if n else None, n, min_length,
+                                                 packed.data_ptr(), words, offsets.data_ptr(), cap,
+                                                 _p(st, _lib.u64p), stream or None)
+        if rc == _lib.ERR_INVALID_ARG and int(st[2]) + 1 > cap:
+            cap = int(st[2]) + 1
+            continue
+        _lib.check(rc)
+        break
     k = int(st[0])
     return packed, offsets[:k + 1], {"n_kept": k, "n_dropped": int(st[1]),
                                      "n_parsed": int(st[2]), "n_skipped": int(st[3])}
