@@ -5,13 +5,12 @@
 // lowercase acgt are upper-cased, a read holding any other symbol or shorter
 // than min_length is dropped and counted.  Same output as gdbg_pack_reads.
 //
-//   k_pk_check  a warp per 32 reads, one read at a time: validity and kept
-//               length
+//   k_pk_check  one warp per read: validity and kept length
 //   scans       kept bases and kept reads (exclusive, 32-bit)
-//   k_pk_write  a warp per 32 reads, each kept read 32 bases per step:
-//               codes merged into words by shuffles, written by each word's
-//               first lane (atomic OR for words shared with a neighbour read
-//               or split between steps); the reads' end offsets
+//   k_pk_write  one warp per kept read, 32 bases per step: codes merged
+//               into words by shuffles, written by each word's first lane
+//               (atomic OR for words shared with a neighbour read or split
+//               between steps); the read's end offset
 //   k_pk_final  counts and offsets[0]
 #include <cuda_runtime.h>
 
@@ -31,12 +30,6 @@ __device__ __forceinline__ uint32_t pk_code(unsigned char c) {
     return lc == 'a' ? 0u : lc == 'c' ? 1u : lc == 'g' ? 2u : lc == 't' ? 3u : 4u;
 }
 
-// Both kernels take the reads in groups of 32 per warp: lane l loads read
-// g + l's bounds (one coalesced load per group) and the warp goes through
-// the group's reads with them broadcast by shuffles; a read's byte loads for
-// up to PK_STEPS steps of 32 bases are issued together.
-constexpr uint32_t PK_STEPS = 8;
-
 __global__ void __launch_bounds__(PK_BLOCK)
 k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ starts,
            const uint64_t* __restrict__ ends, uint64_t n,
@@ -44,49 +37,29 @@ k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
            uint32_t* err, uint32_t* both) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_warps = (uint64_t)gridDim.x * PK_BLOCK / 32;
-    for (uint64_t g = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32 * 32; g < n; g += n_warps * 32) {
-        const uint64_t rr = g + lane;
-        const uint64_t ma = rr < n ? starts[rr] : 0, mb = rr < n ? ends[rr] : 0;
-        const uint32_t cnt = n - g < 32 ? (uint32_t)(n - g) : 32u;
-        uint32_t my_len = 0, my_flag = 0;
-        for (uint32_t k = 0; k < cnt; ++k) {
-            const uint64_t a = __shfl_sync(0xFFFFFFFFu, ma, k), b = __shfl_sync(0xFFFFFFFFu, mb, k);
-            bool ok = b >= a && b - a < (1ull << 31);
-            if (!ok && lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
-            const uint64_t L = ok ? b - a : 0;
-            for (uint64_t i0 = 0; i0 < L && ok; i0 += 32 * PK_STEPS) {
-                unsigned char c[PK_STEPS];
-#pragma unroll
-                for (uint32_t st = 0; st < PK_STEPS; ++st) {
-                    const uint64_t i = i0 + st * 32 + lane;
-                    c[st] = i < L ? seqs[a + i] : (unsigned char)'A';
-                }
-                bool v = true;
-#pragma unroll
-                for (uint32_t st = 0; st < PK_STEPS; ++st) v = v && pk_code(c[st]) < 4u;
-                ok = __all_sync(0xFFFFFFFFu, v);
-            }
-            const bool kept = ok && L >= min_len;
-            if (lane == k) {
-                my_len = kept ? (uint32_t)L : 0u;
-                my_flag = kept ? 1u : 0u;
-            }
+    for (uint64_t r = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32; r < n; r += n_warps) {
+        const uint64_t a = starts[r], b = ends[r];
+        bool ok = b >= a && b - a < (1ull << 31);
+        if (!ok && lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
+        const uint64_t L = ok ? b - a : 0;
+        for (uint64_t i = lane; i < L && ok; i += 32) ok = pk_code(seqs[a + i]) < 4u;
+        ok = __all_sync(0xFFFFFFFFu, ok);
+        const bool kept = ok && L >= min_len;
+        if (lane == 0) {
+            klen[r] = kept ? (uint32_t)L : 0u;
+            kflag[r] = kept ? 1u : 0u;
             // FastxParser counts a read that is invalid and short twice
-            if (both && lane == 0 && !ok && L < min_len) atomicAdd(both, 1u);
-        }
-        if (rr < n) {
-            klen[rr] = my_len;
-            kflag[rr] = my_flag;
+            if (both && !ok && L < min_len) atomicAdd(both, 1u);
         }
     }
 }
 
-// Each kept read, 32 bases per step: lane l converts base i0 + l into its
-// 2-bit code at output position p; the lanes of one output word (at most 16
-// consecutive lanes) OR their codes together by shuffles, and the word's
-// first lane writes it -- a plain store when all 16 of the word's bases are
-// in this step, an atomic OR for a word split between two steps or shared
-// with a neighbour read at either end.
+// One warp per kept read, 32 bases per step: lane l converts base i0 + l
+// (coalesced byte loads) into its 2-bit code at output position p; the
+// lanes of one output word (at most 16 consecutive lanes) OR their codes
+// together by shuffles, and the word's first lane writes it -- a plain store
+// when all 16 of the word's bases are in this step, an atomic OR for a word
+// split between two steps or shared with a neighbour read at either end.
 __global__ void __launch_bounds__(PK_BLOCK)
 k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ starts, uint64_t n,
            const uint32_t* __restrict__ klen, const uint32_t* __restrict__ kflag,
@@ -95,53 +68,33 @@ k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
            uint32_t* err) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_warps = (uint64_t)gridDim.x * PK_BLOCK / 32;
-    for (uint64_t g = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32 * 32; g < n; g += n_warps * 32) {
-        const uint64_t rr = g + lane;
-        const bool in = rr < n;
-        const uint32_t mflag = in ? kflag[rr] : 0u, mlen = in ? klen[rr] : 0u;
-        const uint64_t mstart = in ? starts[rr] : 0, mob0 = in ? kbase[rr] : 0;
-        // kept reads include empty ones (min_length 0)
-        if (mflag) offsets[(uint64_t)kidx[rr] + 1] = mob0 + mlen;
-        const uint32_t cnt = n - g < 32 ? (uint32_t)(n - g) : 32u;
-        for (uint32_t k = 0; k < cnt; ++k) {
-            if (!__shfl_sync(0xFFFFFFFFu, mflag, k)) continue;
-            const uint64_t L = __shfl_sync(0xFFFFFFFFu, mlen, k);
-            const uint64_t a = __shfl_sync(0xFFFFFFFFu, mstart, k);
-            const uint64_t ob0 = __shfl_sync(0xFFFFFFFFu, mob0, k), ob1 = ob0 + L;
-            if (L && (ob1 - 1) / 16 >= packed_words) {
-                if (lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
-                continue;
+    for (uint64_t r = ((uint64_t)blockIdx.x * PK_BLOCK + threadIdx.x) / 32; r < n; r += n_warps) {
+        if (!kflag[r]) continue;   // kept reads include empty ones (min_length 0)
+        const uint64_t L = klen[r];
+        const uint64_t a = starts[r], ob0 = kbase[r], ob1 = ob0 + L;
+        if (L && (ob1 - 1) / 16 >= packed_words) {
+            if (lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
+            continue;
+        }
+        for (uint64_t i0 = 0; i0 < L; i0 += 32) {
+            const uint64_t i = i0 + lane;
+            const uint64_t p = ob0 + i;
+            const uint32_t q = (uint32_t)(p & 15u);
+            uint32_t v = i < L ? pk_code(seqs[a + i]) << (2u * q) : 0u;
+#pragma unroll
+            for (uint32_t o = 1; o < 16; o <<= 1) {
+                const uint32_t y = __shfl_down_sync(0xFFFFFFFFu, v, o);
+                if (lane + o < 32 && q + o < 16) v |= y;
             }
-            for (uint64_t i0 = 0; i0 < L; i0 += 32 * PK_STEPS) {
-                unsigned char c[PK_STEPS];
-#pragma unroll
-                for (uint32_t st = 0; st < PK_STEPS; ++st) {
-                    const uint64_t i = i0 + st * 32 + lane;
-                    c[st] = i < L ? seqs[a + i] : (unsigned char)'A';
-                }
-#pragma unroll
-                for (uint32_t st = 0; st < PK_STEPS; ++st) {
-                    if (i0 + st * 32 >= L) break;
-                    const uint64_t i = i0 + st * 32 + lane;
-                    const uint64_t p = ob0 + i;
-                    const uint32_t q = (uint32_t)(p & 15u);
-                    uint32_t v = i < L ? pk_code(c[st]) << (2u * q) : 0u;
-#pragma unroll
-                    for (uint32_t o = 1; o < 16; o <<= 1) {
-                        const uint32_t y = __shfl_down_sync(0xFFFFFFFFu, v, o);
-                        if (lane + o < 32 && q + o < 16) v |= y;
-                    }
-                    if (i < L && (q == 0 || lane == 0)) {
-                        // a word whose 16 bases are all this step's gets a plain
-                        // store; one split between steps or shared with a
-                        // neighbour read, ORs
-                        const uint64_t w = p >> 4;
-                        if (q == 0 && lane + 15 < 32 && i + 16 <= L) packed[w] = v;
-                        else atomicOr(packed + w, v);
-                    }
-                }
+            if (i < L && (q == 0 || lane == 0)) {
+                // a word whose 16 bases are all this step's gets a plain store;
+                // one split between steps or shared with a neighbour read, ORs
+                const uint64_t w = p >> 4;
+                if (q == 0 && lane + 15 < 32 && i + 16 <= L) packed[w] = v;
+                else atomicOr(packed + w, v);
             }
         }
+        if (lane == 0) offsets[(uint64_t)kidx[r] + 1] = ob1;
     }
 }
 
@@ -220,7 +173,7 @@ int pack_device_run(const char* seqs, const uint64_t* starts, const uint64_t* en
     if ((e = cudaMemsetAsync(err, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess ||
         (packed_words && (e = cudaMemsetAsync(packed, 0, packed_words * sizeof(uint32_t), st)) != cudaSuccess))
         return done(GDBG_ERR_CUDA, cudaGetErrorString(e));
-    uint64_t grid = (n_seqs + PK_BLOCK - 1) / PK_BLOCK;   // a warp per 32 reads
+    uint64_t grid = (n_seqs * 32 + PK_BLOCK - 1) / PK_BLOCK;
     if (grid > 152 * 32) grid = 152 * 32;
     if (grid == 0) grid = 1;
     k_pk_check<<<(unsigned)grid, PK_BLOCK, 0, st>>>((const unsigned char*)seqs, starts, ends, n_seqs,
