@@ -127,6 +127,8 @@ def parse_fastx_device(text, min_length=0, stream=None):
     FASTA / four-line FASTQ layouts raises GoetiaError with code
     ERR_UNSUPPORTED: parse it on the host."""
     import torch
+    if text.dtype != torch.uint8 or not text.is_cuda or not text.is_contiguous():
+        raise ValueError("parse_fastx_device: text must be a contiguous uint8 CUDA tensor")
     dev = text.device
     n = int(text.numel())
     words = n // 16 + 1

@@ -189,7 +189,9 @@ int gdbg_pack_reads_device(const char* seqs, const uint64_t* seq_offsets, uint64
  * and shorter than min_length counts twice).  offsets needs stats[2] + 1
  * entries (GDBG_ERR_INVALID_ARG with stats[2] set otherwise), packed the
  * sequence bytes / 16 + 1 words (n_bytes / 16 + 1 always suffices).  Runs
- * on `stream` and returns when done. */
+ * on `stream` and returns when done.  Its scratch, and the device packer's,
+ * comes from a memory pool of the library's own per device that keeps up
+ * to 2 GiB reserved between calls (for the process's lifetime). */
 int gdbg_parse_fastx_device(const char* text, uint64_t n_bytes, uint32_t min_length,
                             uint32_t* packed, uint64_t packed_words, uint64_t* offsets,
                             uint64_t offsets_cap, uint64_t* stats, void* stream);
