@@ -12,8 +12,9 @@
 //          whole quality string);
 //   FASTA  no line starts with '+'; lines starting with '>' or '@' are
 //          headers, every other line belongs to the sequence of the header
-//          above it (blank lines add nothing, nor does a lone '\r' under a
-//          sequence line with bytes; a lone '\r' anywhere else is refused);
+//          above it (blank lines add nothing, nor does a lone '\r' line under
+//          a sequence line with bytes; a lone '\r' that ends the text is
+//          kept; a lone '\r' line anywhere else is refused);
 // in both the text starts with the header character and does not end in a
 // one-byte header line.  Sequences are the lines' bytes less one trailing
 // '\r' (ks_getuntil2 drops it from a line string longer than one byte; a
@@ -191,9 +192,12 @@ k_fx_classify(const unsigned char* __restrict__ text, uint64_t n, const uint32_t
         if (header && len == 1 && j >= n_nl) ok = false;
         hf = header ? 1u : 0u;
         cl = header ? 0u : fx_eff_len(text, s, e);
-        if (len == 1 && c0 == '\r') {
+        if (len == 1 && c0 == '\r' && j < n_nl) {
             // kseq drops the '\r' when the sequence above already has bytes:
-            // taken when the line above is a sequence line with bytes
+            // taken when the line above is a sequence line with bytes.  (A
+            // lone '\r' that ends the text stays, cl = 1: kseq's read of the
+            // rest of that line meets the end of the text and returns before
+            // it would drop it, so the read is dropped as invalid.)
             cl = 0;
             if (j == 0) {
                 ok = false;

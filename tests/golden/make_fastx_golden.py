@@ -7,11 +7,12 @@ case and min_length, the sequences next() returned, n_parsed, n_skipped and
 whether next() threw InvalidRead.  The texts cover the regular layouts the
 GPU parser takes (four-line FASTQ records; FASTA with sequences over any
 number of lines, '>' or '@' headers, blank lines) with lower case, 'N' and
-other symbols, CRLF line ends, empty sequences and a last line without a
-newline, and layouts it refuses (quality over several lines, junk before the
-first header, trailing blank lines after a FASTQ record, a '+' line in
-FASTA, a line holding only '\\r', a one-byte header at the end, a quality
-line longer than its sequence).
+other symbols, CRLF line ends, empty sequences, a last line without a
+newline and a lone '\\r' ending the text, and layouts it refuses (quality
+over several lines, junk before the first header, trailing blank lines
+after a FASTQ record, a '+' line in FASTA, a line holding only '\\r' under
+a header, a one-byte header at the end, a quality line longer than its
+sequence).
 
     GOETIA_REF=<goetia checkout> python tests/golden/make_fastx_golden.py
 
@@ -83,6 +84,10 @@ def cases():
     c["empty"] = b""
     c["fa_header_only_eof"] = b">a\nACGT\n>b desc"
     c["fq_cr_only_seq"] = b"@a\n\r\n+\n\r\n@b\nACGT\n+\nIIII\n"
+    # a lone '\r' that ends the text stays in the sequence (its line read
+    # meets the end first); one under a sequence line elsewhere is dropped
+    c["fa_cr_at_end"] = b">a\nACGT\n\r\nGG\n>b\nACGT\r\n\r"
+    c["fa_cr_at_end_after_header"] = b">a\nACGT\n>b\n\r"
     # layouts the GPU parser refuses
     c["x_fq_multiline_qual"] = b"@a\nACGTACGT\n+\nIIII\nIIII\n@b\nAC\n+\nII\n"
     c["x_fq_multiline_seq"] = b"@a\nACGT\nACGT\n+\nIIIIIIII\n"
