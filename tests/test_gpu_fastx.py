@@ -154,3 +154,28 @@ def test_fastx_batch_inserts_like_host_packed(cuda_ready):
     assert np.array_equal(d_new.cpu().numpy(), np.asarray(n_new_host, np.int64))
     for ta, tb in zip(a.get_raw(), b.get_raw()):
         assert np.array_equal(ta, tb)
+
+
+def test_fastx_kernel_follows_the_per_line_rule(cuda_ready):
+    """Seeded random FASTA / FASTQ-like texts (the line kinds of
+    tests/test_fastx_rule.py): the GPU parser declines exactly the texts the
+    per-line rule declines, and elsewhere gives kseq's reads and counts."""
+    import test_fastx_rule as rule
+    rng = np.random.default_rng(5)
+    seen = {True: 0, False: 0}
+    for _ in range(800):
+        text = rule.random_text(rng)
+        d = device_text(text, int(rng.integers(0, 4)))
+        for ml in (0, 4):
+            expect = rule.per_line_rule(text, ml)
+            seen[expect is None] += 1
+            if expect is None:
+                with pytest.raises(_lib.GoetiaError) as ei:
+                    G.reads.parse_fastx_device(d, ml)
+                assert ei.value.code == _lib.ERR_UNSUPPORTED, text
+                continue
+            seqs, st, status = oracle.parse_fastx(text, ml)
+            assert status == 0 and (seqs, st["n_parsed"], st["n_skipped"]) == expect, text
+            packed, offsets, stats = G.reads.parse_fastx_device(d, ml)
+            check_against(seqs, (st["n_parsed"], st["n_skipped"]), packed, offsets, stats, text)
+    assert seen[True] > 80 and seen[False] > 80
