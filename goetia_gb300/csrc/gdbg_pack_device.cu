@@ -7,10 +7,9 @@
 //
 //   k_pk_check  one warp per read: validity and kept length
 //   scans       kept bases and kept reads (exclusive, 32-bit)
-//   k_pk_write  one warp per kept read, 32 bases per step: codes merged
-//               into words by shuffles, written by each word's first lane
-//               (atomic OR for words shared with a neighbour read or split
-//               between steps); the read's end offset
+//   k_pk_write  one warp per kept read, one lane per output word, codes by
+//               arithmetic on the bytes (atomic OR for the words shared
+//               with neighbour reads); the read's end offset
 //   k_pk_final  counts and offsets[0]
 #include <cuda_runtime.h>
 
@@ -54,12 +53,13 @@ k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
     }
 }
 
-// One warp per kept read, 32 bases per step: lane l converts base i0 + l
-// (coalesced byte loads) into its 2-bit code at output position p; the
-// lanes of one output word (at most 16 consecutive lanes) OR their codes
-// together by shuffles, and the word's first lane writes it -- a plain store
-// when all 16 of the word's bases are in this step, an atomic OR for a word
-// split between two steps or shared with a neighbour read at either end.
+// One warp per kept read, one lane per output word: lane l builds word
+// w0 + l (+ 32, ...) from its (up to) 16 bases, each base's code by
+// arithmetic on its byte -- ((c >> 1) & 3) gives A 0, C 1, G 3, T 2 for
+// upper and lower case, and x ^ (x >> 1) swaps G and T (the reads here are
+// valid: k_pk_check kept them).  A word that lies inside the read is
+// stored; the read's first and last words, which neighbour reads share, are
+// ORed in.
 __global__ void __launch_bounds__(PK_BLOCK)
 k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ starts, uint64_t n,
            const uint32_t* __restrict__ klen, const uint32_t* __restrict__ kflag,
@@ -76,21 +76,22 @@ k_pk_write(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
             if (lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
             continue;
         }
-        for (uint64_t i0 = 0; i0 < L; i0 += 32) {
-            const uint64_t i = i0 + lane;
-            const uint64_t p = ob0 + i;
-            const uint32_t q = (uint32_t)(p & 15u);
-            uint32_t v = i < L ? pk_code(seqs[a + i]) << (2u * q) : 0u;
+        if (L) {
+            const uint64_t w1 = (ob1 - 1) >> 4;
+            for (uint64_t w = (ob0 >> 4) + lane; w <= w1; w += 32) {
+                const uint64_t lo = w * 16 > ob0 ? w * 16 : ob0;
+                const uint64_t hi = w * 16 + 16 < ob1 ? w * 16 + 16 : ob1;
+                const unsigned char* src = seqs + a + (lo - ob0);
+                const uint32_t q0 = (uint32_t)(lo & 15u), nb = (uint32_t)(hi - lo);
+                uint32_t v = 0;
 #pragma unroll
-            for (uint32_t o = 1; o < 16; o <<= 1) {
-                const uint32_t y = __shfl_down_sync(0xFFFFFFFFu, v, o);
-                if (lane + o < 32 && q + o < 16) v |= y;
-            }
-            if (i < L && (q == 0 || lane == 0)) {
-                // a word whose 16 bases are all this step's gets a plain store;
-                // one split between steps or shared with a neighbour read, ORs
-                const uint64_t w = p >> 4;
-                if (q == 0 && lane + 15 < 32 && i + 16 <= L) packed[w] = v;
+                for (uint32_t k = 0; k < 16; ++k) {
+                    if (k < nb) {
+                        const uint32_t x = ((uint32_t)src[k] >> 1) & 3u;
+                        v |= (x ^ (x >> 1)) << (2u * (q0 + k));
+                    }
+                }
+                if (nb == 16) packed[w] = v;
                 else atomicOr(packed + w, v);
             }
         }
