@@ -133,3 +133,41 @@ def test_rule_agrees_with_kseq_when_it_accepts(seed):
             assert status == 0, text
             assert got == (seqs, st["n_parsed"], st["n_skipped"]), text
     assert accepted > 200   # the random texts do exercise accepted layouts
+
+
+def random_fastq(rng):
+    """Mostly four-line FASTQ records whose lines carry the bytes kseq
+    treats specially ('@', '>', '+', '\\r', blanks) in odd places."""
+    lines = []
+    for _ in range(int(rng.integers(1, 6))):
+        L = int(rng.integers(0, 7))
+        seq = rng.choice(list(b"ACGTNacgt\r@>+I"), L,
+                         p=[.12, .12, .12, .12, .04, .08, .08, .08, .08, .04, .03, .03, .02, .04])
+        qual = rng.choice(list(b"I@+>\r#"), L)
+        head = b"@" + rng.choice(list(b"r \t\r@>+"), int(rng.integers(0, 4))).astype(np.uint8).tobytes()
+        plus = b"+" + rng.choice(list(b"r \r@"), int(rng.integers(0, 3))).astype(np.uint8).tobytes()
+        rec = [head, seq.astype(np.uint8).tobytes(), plus, qual.astype(np.uint8).tobytes()]
+        if rng.random() < 0.3:
+            k = int(rng.integers(1, 4))
+            rec[k] += b"\r"
+        lines += rec
+    eol = b"\r\n" if rng.random() < 0.2 else b"\n"
+    text = eol.join(lines)
+    return text + eol if rng.random() < 0.6 else text
+
+
+@pytest.mark.parametrize("seed", range(2))
+def test_rule_agrees_with_kseq_on_fastq(seed):
+    rng = np.random.default_rng(200 + seed)
+    accepted = 0
+    for _ in range(3000):
+        text = random_fastq(rng)
+        for ml in (0, 3):
+            got = per_line_rule(text, ml)
+            if got is None:
+                continue
+            accepted += 1
+            seqs, st, status = oracle.parse_fastx(text, ml)
+            assert status == 0, text
+            assert got == (seqs, st["n_parsed"], st["n_skipped"]), text
+    assert accepted > 2000
