@@ -24,9 +24,11 @@ namespace gdbg {
 
 constexpr int PK_BLOCK = 256;
 
-__device__ __forceinline__ uint32_t pk_code(unsigned char c) {
-    const unsigned char lc = c | 0x20u;   // 'A'..'Z' -> 'a'..'z'; leaves other symbols non-letters
-    return lc == 'a' ? 0u : lc == 'c' ? 1u : lc == 'g' ? 2u : lc == 't' ? 3u : 4u;
+// A DNA_SIMPLE symbol (ACGT, either case): (c | 0x20) - 'a' is 0, 2, 6 or 19
+// exactly for them.
+__device__ __forceinline__ bool pk_valid(unsigned char c) {
+    const uint32_t d = (uint32_t)(c | 0x20u) - (uint32_t)'a';
+    return d < 20u && ((0x80045u >> d) & 1u);
 }
 
 __global__ void __launch_bounds__(PK_BLOCK)
@@ -41,7 +43,7 @@ k_pk_check(const unsigned char* __restrict__ seqs, const uint64_t* __restrict__ 
         bool ok = b >= a && b - a < (1ull << 31);
         if (!ok && lane == 0) atomicOr(err, GDBG_ERR_BAD_OFFSETS);
         const uint64_t L = ok ? b - a : 0;
-        for (uint64_t i = lane; i < L && ok; i += 32) ok = pk_code(seqs[a + i]) < 4u;
+        for (uint64_t i = lane; i < L && ok; i += 32) ok = pk_valid(seqs[a + i]);
         ok = __all_sync(0xFFFFFFFFu, ok);
         const bool kept = ok && L >= min_len;
         if (lane == 0) {
