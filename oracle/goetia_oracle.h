@@ -2,13 +2,15 @@
  * CPU oracle for the goetia dBG hot path -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference algorithm (sequential rolling
- * cyclic hash, Bit/Byte/Nibble storages, dBG insert/query, neighbour masks).
+ * cyclic hash, Bit/Byte/Nibble storages, dBG insert/query, neighbour masks,
+ * and the FASTA/FASTQ reader in front of them: kseq and FastxParser).
  * Only tests, the smoke check and the CPU-baseline leg of the benchmark use
  * it, as the checker; the product path never links or calls it.
  *
  * Parity is pinned two ways: the K=27 known-answer hash from the reference's
  * tests (tests/test_hashing.py:15-19), and golden fixtures generated by the
- * reference's own C++ objects (oracle/Makefile + oracle/ref_driver.cc).
+ * reference's own C++ objects (oracle/Makefile + oracle/ref_driver.cc, and
+ * oracle/ref_fastx.cc for the reader).
  *
  * Read encoding (shared with the GPU library): bases are 2-bit codes
  * A=0 C=1 G=2 T=3, packed 16 per uint32_t little-endian (base j is bits
